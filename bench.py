@@ -1,0 +1,466 @@
+"""Benchmark of the nalgebra dense-solve hot path on GB300.
+
+Default workload (the headline): ragged batched Cholesky -- 20000 SPD systems
+with n uniform in [8, 256], A = B B^T + n I, B ~ N(0,1) f64, 4 right-hand sides
+~ N(0,1) each -- factor + solve + log-determinant of every system in ONE
+persistent launch (nacu_dposv_ragged), against one plain FP64 launch per
+matrix (nacu_dposv) and nalgebra's CPU path (the oracle restatement) on the
+host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload ragged_cholesky|lu_batched]
+
+Prints ONE JSON line.  A "step" is one pass of the hot path over the whole
+batch.  The factorization is in place, so each step first restores the input
+from a pristine device copy; that restore is outside the timed events (CUDA
+events bracket each kernel launch on its stream).  Inputs (3.4 GB) are larger
+than the 129 MB L2, so no extra flush is needed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+EPS64 = 2.220446049250313e-16
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+# ----------------------------------------------------------------------------- util
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ----------------------------------------------------------------------------- ragged Cholesky
+
+RAGGED = dict(count=20000, n_lo=8, n_hi=256, nrhs=4, seed=0)
+
+
+def ragged_flops(ns, nrhs):
+    ns = ns.astype(np.float64)
+    return float(np.sum(ns ** 3 / 3.0 + nrhs * 2.0 * ns ** 2))
+
+
+def ragged_bytes(ns, nrhs):
+    # read A (lower), write L (lower), read B, write X, 8 bytes each
+    ns = ns.astype(np.float64)
+    return float(np.sum(8.0 * ns * (ns + 1) + 2 * 8.0 * nrhs * ns))
+
+
+def backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample):
+    """Normwise backward error of a sample of systems with the residual in
+    extended precision (numpy longdouble), in units of n * eps64."""
+    worst = 0.0
+    for s in sample:
+        n = int(ns[s])
+        a = a_host[aoff[s]:aoff[s] + n * n].reshape(n, n).T.astype(np.longdouble)
+        a = np.tril(a) + np.tril(a, -1).T
+        b = b_host[boff[s]:boff[s] + n * nrhs].reshape(nrhs, n).T.astype(np.longdouble)
+        x = x_host[boff[s]:boff[s] + n * nrhs].reshape(nrhs, n).T.astype(np.longdouble)
+        r = b - a @ x
+        an = np.max(np.sum(np.abs(a), axis=1))
+        be = np.max(np.max(np.abs(r), axis=0) / (an * np.max(np.abs(x), axis=0) + np.max(np.abs(b), axis=0)))
+        worst = max(worst, float(be) / (n * EPS64))
+    return worst
+
+
+def bench_ragged_ours(args, rank, world):
+    import torch
+
+    from nalgebra_gb300 import DeviceBatch, _lib
+    from nalgebra_gb300 import workloads as W
+
+    L = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cfg = dict(RAGGED)
+    w = W.ragged_spd_torch(cfg["count"], cfg["n_lo"], cfg["n_hi"], cfg["nrhs"], seed=cfg["seed"] + rank, device=dev)
+    ns, aoff, boff, nrhs = w["ns"], w["a_offsets"], w["b_offsets"], cfg["nrhs"]
+    count = ns.size
+    a0, b0 = w["a_flat"], w["b_flat"]
+    A = a0.clone()
+    B = b0.clone()
+    batch = DeviceBatch(A, ns, ns, aoff)
+    rhs = DeviceBatch(B, ns, np.full(count, nrhs), boff)
+    chol = batch.cholesky()
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    n_max = int(ns.max())
+
+    def launch():
+        _lib.call("nacu_dposv_ragged", count, n_max, batch._d_rows.data_ptr(), batch._d_off.data_ptr(),
+                  A.data_ptr(), nrhs, rhs._d_off.data_ptr(), B.data_ptr(), chol.info.data_ptr(),
+                  chol.logdet.data_ptr(), chol._order.data_ptr(), chol._ws.data_ptr(), chol._ws.numel(), 0.0, 0, sp)
+
+    def restore():
+        A.copy_(a0)
+        B.copy_(b0)
+
+    for _ in range(args.warmup):
+        restore()
+        launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            restore()
+            ev[i][0].record(stream)
+            launch()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    times = [e0.elapsed_time(e1) for e0, e1 in ev]
+    kern_ms = float(np.mean(times))
+    info = chol.info.cpu().numpy()
+    if np.any(info != 0):
+        raise RuntimeError(f"{int(np.sum(info != 0))} systems failed to factor")
+    # accuracy of the last step's solutions (sampled)
+    rng = np.random.default_rng(1)
+    sample = rng.choice(count, size=min(48, count), replace=False)
+    a_host = a0.cpu().numpy()
+    b_host = b0.cpu().numpy()
+    x_host = B.cpu().numpy()
+    berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample)
+
+    # e2e through the public API from pinned host buffers (H2D in, D2H of X,
+    # info and log-det out), inside the timed region.
+    a_pin = torch.empty(a0.numel(), dtype=torch.float64, pin_memory=True)
+    b_pin = torch.empty(b0.numel(), dtype=torch.float64, pin_memory=True)
+    x_pin = torch.empty(b0.numel(), dtype=torch.float64, pin_memory=True)
+    i_pin = torch.empty(count, dtype=torch.int32, pin_memory=True)
+    l_pin = torch.empty(count, dtype=torch.float64, pin_memory=True)
+    a_pin.copy_(a0)
+    b_pin.copy_(b0)
+    e2e_steps = max(1, min(args.steps, 5))
+
+    def e2e_step():
+        A.copy_(a_pin, non_blocking=True)
+        B.copy_(b_pin, non_blocking=True)
+        chol.factored = False
+        chol.solve_mut(rhs)
+        x_pin.copy_(B, non_blocking=True)
+        i_pin.copy_(chol.info, non_blocking=True)
+        l_pin.copy_(chol.logdet, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1) / e2e_steps
+    h2d = (a0.numel() + b0.numel()) * 8
+    d2h = b0.numel() * 8 + count * 12
+
+    # one plain FP64 launch per matrix (nacu_dposv), on a sample, one stream
+    plain_sample = rng.choice(count, size=min(1000, count), replace=False)
+    restore()
+    torch.cuda.synchronize()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for s in plain_sample:
+        n = int(ns[s])
+        _lib.call("nacu_dposv", n, A.data_ptr() + int(aoff[s]) * 8, nrhs, B.data_ptr() + int(boff[s]) * 8,
+                  chol.info.data_ptr() + int(s) * 4, chol.logdet.data_ptr() + int(s) * 8, 0.0, 0, sp)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1)
+    plain_solves_per_s = plain_sample.size / (plain_ms * 1e-3)
+    plain_flops = ragged_flops(ns[plain_sample], nrhs) / (plain_ms * 1e-3)
+
+    peak = ctypes_probe(L)
+    flops = ragged_flops(ns, nrhs)
+    achieved = flops / (kern_ms * 1e-3)
+    value = count * world / (kern_ms * 1e-3)
+    res = {
+        "metric": "solves/s at backward err <= n*eps64 (ragged batched Cholesky factor+solve+logdet)",
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": kern_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded; A = B B^T + n I, B ~ N(0,1); 4 RHS ~ N(0,1))",
+        "config": {"workload": "ragged_cholesky", "count": count, "n_range": [cfg["n_lo"], cfg["n_hi"]],
+                   "nrhs": nrhs, "form": "batched persistent FP64 (one launch, largest-first work queue)",
+                   "l2": "inputs (3.4 GB) larger than L2; input restore outside the timed events",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "gflops": achieved / 1e9,
+        "backward_error_max_over_sample_in_n_eps": berr,
+        "forms": {
+            "batched_persistent_fp64": {"solves_per_s": value / world, "gflops": achieved / 1e9},
+            "plain_fp64_launch_per_matrix": {"solves_per_s": plain_solves_per_s, "gflops": plain_flops / 1e9,
+                                             "sample": int(plain_sample.size)},
+        },
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "FP64 DFMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+                     "algorithmic_bytes_per_launch": ragged_bytes(ns, nrhs),
+                     "hbm_frac_of_measured": (ragged_bytes(ns, nrhs) / (kern_ms * 1e-3)) / (read_peaks().get("hbm_gbs", 6794.8) * 1e9)},
+        "e2e": {"value": count / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+    }
+    return res, dict(ns=ns, aoff=aoff, boff=boff, a_host=a_host, b_host=b_host, nrhs=nrhs)
+
+
+def ctypes_probe(L):
+    import ctypes
+
+    v = ctypes.c_double(0.0)
+    rc = L.nacu_probe_fp64_peak(ctypes.byref(v))
+    if rc != 0:
+        raise RuntimeError("FP64 probe failed")
+    return v.value
+
+
+def cpu_baseline_ragged(data, max_seconds=20.0):
+    """The oracle (C++ restatement of nalgebra's Cholesky + solve + ln_det) on
+    the host cores, on a bounded sample of the same workload."""
+    import oracle as O
+
+    ns, aoff, boff, a_host, b_host, nrhs = (data[k] for k in ("ns", "aoff", "boff", "a_host", "b_host", "nrhs"))
+    threads = O.max_threads()
+    count = ns.size
+    # sample: the first k systems (same distribution), sized to ~max_seconds
+    k = min(count, 2000)
+    while True:
+        sl = slice(0, k)
+        a_s = a_host[: int(aoff[k - 1] + ns[k - 1] ** 2)] if k < count else a_host
+        b_s = b_host[: int(boff[k - 1] + ns[k - 1] * nrhs)] if k < count else b_host
+        t0 = time.perf_counter()
+        O.posv_ragged(ns[sl], aoff[sl], a_s, boff[sl], b_s, nrhs, nthreads=threads)
+        dt = time.perf_counter() - t0
+        if dt > 2.0 or k == count:
+            break
+        k = min(count, int(k * max(2.0, 5.0 / max(dt, 1e-3))))
+    return {"value": k / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"first {k} of {count} systems of the same workload, {dt:.2f} s",
+            "gflops": ragged_flops(ns[:k], nrhs) / dt / 1e9}
+
+
+def bench_ragged_reference(args, rank, world):
+    """--impl reference: nalgebra's CPU path (the oracle restatement, all host
+    threads), same config/metric; each step a bounded sample."""
+    import oracle as O
+    from nalgebra_gb300 import workloads as W
+
+    cfg = dict(RAGGED)
+    k = 2000
+    w = W.ragged_spd(k, cfg["n_lo"], cfg["n_hi"], cfg["nrhs"], seed=cfg["seed"])
+    threads = O.max_threads()
+    for _ in range(args.warmup):
+        O.posv_ragged(w["ns"], w["a_offsets"], w["a_flat"], w["b_offsets"], w["b_flat"], cfg["nrhs"], nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.posv_ragged(w["ns"], w["a_offsets"], w["a_flat"], w["b_offsets"], w["b_flat"], cfg["nrhs"], nthreads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = k / dt
+    return {
+        "impl": "reference",
+        "metric": "solves/s at backward err <= n*eps64 (ragged batched Cholesky factor+solve+logdet)",
+        "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded; A = B B^T + n I, B ~ N(0,1); 4 RHS ~ N(0,1))",
+        "config": {"workload": "ragged_cholesky", "count": RAGGED["count"], "n_range": [cfg["n_lo"], cfg["n_hi"]],
+                   "nrhs": cfg["nrhs"], "form": "nalgebra CPU path (C++ restatement), OpenMP across systems"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"{k} systems of the same distribution per step"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ----------------------------------------------------------------------------- LU batched
+
+def bench_lu_ours(args, rank, world):
+    import torch
+
+    from nalgebra_gb300 import _lib
+    from nalgebra_gb300 import workloads as W
+
+    L = _lib.load()
+    count, n = 4096, 64
+    a, b = W.dense_lu(count, n, 1, seed=rank)
+    a0 = torch.from_numpy(a).cuda().reshape(-1)
+    b0 = torch.from_numpy(b).cuda().reshape(-1)
+    A, B = a0.clone(), b0.clone()
+    ipiv = torch.zeros(count * n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    flags = 1 if args.exact else 0
+
+    def launch():
+        _lib.call("nacu_dgesv_batched", n, 1, A.data_ptr(), n * n, ipiv.data_ptr(), B.data_ptr(), n,
+                  info.data_ptr(), count, flags, sp)
+
+    for _ in range(args.warmup):
+        A.copy_(a0); B.copy_(b0); launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            A.copy_(a0); B.copy_(b0); flush.zero_()
+            ev[i][0].record(stream)
+            launch()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+    flops = count * (2.0 / 3 * n ** 3 + 2.0 * n ** 2)
+    peak = ctypes_probe(L)
+    return {"metric": "solves/s (batched LU factor+solve, 4096 x 64x64 f64)", "value": count / (ms * 1e-3),
+            "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "lu_batched", "count": count, "n": n, "exact": bool(args.exact),
+                                            "l2": "256 MB flush between steps"},
+            "gflops": flops / (ms * 1e-3) / 1e9,
+            "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak / 1e12,
+                         "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / peak, "traffic": None},
+            "gpu_launches": args.steps, "clocks": clk.summary()}
+
+
+# ----------------------------------------------------------------------------- main
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched"])
+    ap.add_argument("--exact", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(bench_ragged_reference(args, rank, world)))
+        return
+
+    import torch
+
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from nalgebra_gb300 import build
+
+    if rank == 0:
+        build.build()
+    if world > 1:
+        torch.distributed.barrier()
+
+    if args.workload == "lu_batched":
+        res = bench_lu_ours(args, rank, world)
+        if rank == 0:
+            print(json.dumps(res))
+        return
+
+    res, data = bench_ragged_ours(args, rank, world)
+    if world > 1:
+        t = torch.tensor([res["ms_per_step"]], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        res["ms_per_step"] = float(t.item())
+        res["value"] = RAGGED["count"] * world / (res["ms_per_step"] * 1e-3)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            res["cpu_baseline"] = cpu_baseline_ragged(data)
+        print(json.dumps(res))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,153 @@
+/*
+ * nalgebra-cuda: C ABI of the GB300 (sm_103a) dense linear-algebra library.
+ *
+ * This is the drop-in boundary for nalgebra's dense solve path: the calls a
+ * `nalgebra-cuda` crate (or any other host) binds over FFI in place of
+ * nalgebra's CPU `LU` / `Cholesky` / `QR` / `Matrix::gemm`.  Every reference
+ * function each entry point replaces is cited (file:line inside the nalgebra
+ * 0.35 source tree).
+ *
+ * Conventions (shared by every entry point):
+ *  - Matrices are column-major and contiguous, element (r, c) at a[r + c*lda],
+ *    exactly nalgebra's VecStorage (src/base/vec_storage.rs:28-32).
+ *  - All matrix / vector / info pointers are DEVICE pointers owned by the
+ *    caller.  Factorizations overwrite their input in place, as nalgebra's
+ *    consume-and-factor constructors do (src/linalg/lu.rs:93,
+ *    src/linalg/cholesky.rs:221, src/linalg/qr.rs:55).
+ *  - Every call is asynchronous on the given CUDA stream (`nacu_stream_t` is a
+ *    `cudaStream_t`; NULL = the legacy default stream) and does not
+ *    synchronize.  No call allocates device memory; scratch is passed in by the
+ *    caller (sizes from the *_workspace_bytes queries, the LAPACK lwork idiom,
+ *    nalgebra-lapack/src/qr.rs:79-100).
+ *  - Return value: NACU_SUCCESS (0); -i when argument i (1-based) is invalid
+ *    (LAPACK xerbla convention); NACU_ERR_CUDA when a CUDA call or launch
+ *    failed.  nacu_last_error() returns a message for the last failure on the
+ *    calling thread.
+ *  - Per-matrix numerical status goes to a device `int32_t info[]`: 0 = ok,
+ *    k > 0 = the 1-based index of the failing pivot (LU: first zero U_kk;
+ *    Cholesky: first non-positive or NaN pivot; least squares: a zero R_kk),
+ *    as nalgebra-lapack's info (nalgebra-lapack/src/lapack_error.rs:14-20).
+ *    A host binding maps info != 0 to nalgebra's None / false.
+ *  - Pivots are 0-based per step: ipiv[i] = the row swapped with row i at
+ *    elimination step i (ipiv[i] == i: no swap).  The (i, ipiv[i]) pairs with
+ *    ipiv[i] != i, in order, are nalgebra's PermutationSequence
+ *    (src/linalg/permutation_sequence.rs:84-93); their count's parity is the
+ *    determinant sign (permutation_sequence.rs:158-164).
+ */
+#ifndef NALGEBRA_CUDA_H
+#define NALGEBRA_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void* nacu_stream_t;
+
+#define NACU_SUCCESS 0
+#define NACU_ERR_CUDA 1
+#define NACU_ERR_UNSUPPORTED 2
+
+/* flags (bitwise or) */
+/* Reproduce nalgebra's arithmetic exactly: no FMA contraction, reciprocal
+ * multiply / true division exactly where nalgebra uses them, nalgebra's
+ * 8-accumulator dot order.  Factors and solutions then match nalgebra's CPU
+ * results bit for bit (log-determinants to a few ulps: CUDA's log is not
+ * correctly rounded).  Costs about twice the FP64 issue slots. */
+#define NACU_FLAG_EXACT 1
+/* gesv: do not write the LU factors back (solutions, pivots and info only). */
+#define NACU_FLAG_NO_FACTORS 2
+/* Cholesky: replace a failing pivot by the `substitute` argument, as
+ * Cholesky::new_with_substitute does (src/linalg/cholesky.rs:216-218). */
+#define NACU_FLAG_SUBSTITUTE 4
+
+#define NACU_LU_BATCHED_MAX_N 128
+#define NACU_LU_BATCHED_MAX_NRHS 16
+#define NACU_CHOL_RAGGED_MAX_N 512
+
+/* ---- library ------------------------------------------------------------- */
+
+/* Library version, e.g. "0.1.0". */
+const char* nacu_version(void);
+/* Message for the last failed call on this host thread ("" if none). */
+const char* nacu_last_error(void);
+/* Compiled device architecture, e.g. 103 for sm_103a. */
+int nacu_device_arch(void);
+
+/* ---- LU with partial pivoting (batched, n <= 128) ------------------------- */
+
+/* Factor `batch` n x n matrices A + s*strideA in place into nalgebra's packed
+ * L\U form, with per-step pivots ipiv[s*n + i] and info[s].
+ * Replaces LU::new (src/linalg/lu.rs:93-122) with icamax
+ * (src/base/min_max.rs:221-240) and gauss_step(_swap) (lu.rs:337-389). */
+int nacu_dgetrf_batched(int n, double* A, int64_t strideA, int32_t* ipiv, int32_t* info, int batch,
+                        int flags, nacu_stream_t stream);
+
+/* Solve A X = B from getrf factors; B + s*strideB (n x nrhs) becomes X.
+ * Replaces LU::solve_mut (src/linalg/lu.rs:242-260: permute_rows,
+ * solve_lower_triangular_with_diag_mut solve.rs:106-133,
+ * solve_upper_triangular_mut solve.rs:137-182).  info[s] = first zero U_kk. */
+int nacu_dgetrs_batched(int n, int nrhs, double* LU, int64_t strideA, int32_t* ipiv, double* B,
+                        int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
+
+/* Fused factor + solve in one launch: `m.lu()` then `.solve(&b)`
+ * (src/linalg/decomposition.rs:48-54, src/linalg/lu.rs:221-236). */
+int nacu_dgesv_batched(int n, int nrhs, double* A, int64_t strideA, int32_t* ipiv, double* B,
+                       int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
+
+/* FP32 form of nacu_dgesv_batched (the factor step of mixed precision). */
+int nacu_sgesv_batched(int n, int nrhs, float* A, int64_t strideA, int32_t* ipiv, float* B,
+                       int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
+
+/* ---- Cholesky (ragged batch, one persistent launch) ------------------------ */
+
+/* Bytes of device scratch nacu_dposv_ragged needs (the work-queue head). */
+size_t nacu_ragged_workspace_bytes(int count);
+
+/* Factor, solve and log-determinant for `count` SPD matrices of uneven order.
+ * Matrix s is ns[s] x ns[s] (ns[s] <= n_max <= 512) at A + a_offsets[s]
+ * (lda = ns[s]); its nrhs right-hand sides are ns[s] x nrhs at
+ * B + b_offsets[s] (ldb = ns[s]) and are overwritten by X.  Only the lower
+ * triangle is read and written.  info[s] as above (-1: ns[s] out of range);
+ * logdet[s] (nullable) = sum ln(L_ii^2), NaN when info != 0.  `order`
+ * (nullable) is the processing order (largest matrices first balances the
+ * persistent CTAs).  ns, a_offsets, b_offsets and order are device arrays.
+ * Replaces Cholesky::new (src/linalg/cholesky.rs:196-272), Cholesky::solve_mut
+ * (cholesky.rs:122-129, solve.rs:488-519, 697-755) and ln_determinant
+ * (cholesky.rs:172-185). */
+int nacu_dposv_ragged(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, double* A,
+                      int nrhs, const int64_t* b_offsets, double* B, int32_t* info, double* logdet,
+                      const int32_t* order, void* workspace, size_t workspace_bytes, double substitute,
+                      int flags, nacu_stream_t stream);
+
+/* Factor + log-determinant only (no right-hand sides), same layout as
+ * nacu_dposv_ragged: `m.cholesky()` and `.ln_determinant()`. */
+int nacu_dpotrf_ragged(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, double* A,
+                       int32_t* info, double* logdet, const int32_t* order, void* workspace,
+                       size_t workspace_bytes, double substitute, int flags, nacu_stream_t stream);
+
+/* Solve from factors written by nacu_dpotrf_ragged (only matrices whose info
+ * was 0 are meaningful): `chol.solve_mut(&mut b)` (src/linalg/cholesky.rs:122-129). */
+int nacu_dpotrs_ragged(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, const double* L,
+                       int nrhs, const int64_t* b_offsets, double* B, const int32_t* order, void* workspace,
+                       size_t workspace_bytes, int flags, nacu_stream_t stream);
+
+/* One matrix, one plain launch: `m.cholesky()`, `.solve(&b)`,
+ * `.ln_determinant()` for an n x n SPD matrix (n <= 512). */
+int nacu_dposv(int n, double* A, int nrhs, double* B, int32_t* info, double* logdet, double substitute,
+               int flags, nacu_stream_t stream);
+
+/* ---- measurement helpers ---------------------------------------------------- */
+
+/* FP64 FMA throughput probe: runs a fixed DFMA-chain kernel over the whole GPU
+ * and returns the achieved FP64 FLOP/s through *flops (synchronous; used as
+ * the FP64 roofline denominator). */
+int nacu_probe_fp64_peak(double* flops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NALGEBRA_CUDA_H */

@@ -1,0 +1,357 @@
+"""nalgebra_gb300: host-side mirror of nalgebra's dense solve API over the
+nalgebra-cuda C ABI (include/nalgebra_cuda.h, libnalgebra_cuda.so).
+
+The method names follow nalgebra so that code written against
+``DMatrix::lu() / .cholesky() / .qr() / .solve() / gemm(alpha, a, b, beta)``
+reads the same here:
+
+=================================  ==============================================
+nalgebra (reference)                here
+=================================  ==============================================
+``m.lu()`` lu.rs:93-122            ``DeviceMatrix.lu()`` / ``DeviceBatch.lu()``
+``lu.solve(&b)`` lu.rs:221-236     ``LU.solve(b)`` -> DeviceMatrix or None
+``lu.solve_mut(&mut b)``           ``LU.solve_mut(b)`` -> bool
+``lu.determinant()`` lu.rs:301     ``LU.determinant()``
+``lu.p()``                         ``LU.p()`` -> [(i, piv), ...]
+``m.cholesky()`` cholesky.rs:196   ``DeviceMatrix.cholesky()`` -> Cholesky or None
+``chol.solve(&b)`` cholesky.rs:134 ``Cholesky.solve(b)``
+``chol.ln_determinant()`` :172     ``Cholesky.ln_determinant()``
+=================================  ==============================================
+
+Device memory and streams come from PyTorch (plumbing only); every numerical
+operation is a hand-written sm_103a kernel reached through the C ABI.  There
+is no CPU fallback: without a GPU or without the built library, calls raise.
+Factorizations are lazy where that lets one launch do factor + solve: ``lu()``
+and ``cholesky()`` on a batch record the request, and the first ``solve``
+runs the fused kernel, writing the factors as a side effect.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
+
+__all__ = [
+    "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch",
+    "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE",
+]
+
+
+def _torch():
+    import torch  # deferred: plumbing only
+
+    if not torch.cuda.is_available():
+        raise NacuError("nalgebra_gb300 needs a CUDA GPU: there is no CPU fallback")
+    return torch
+
+
+def _stream_ptr(stream=None) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def _dev_f64(x, torch):
+    if isinstance(x, torch.Tensor):
+        return x.to(device="cuda", dtype=torch.float64).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to("cuda")
+
+
+class DeviceMatrix:
+    """An nrows x ncols f64 matrix resident on the GPU, column-major like
+    nalgebra's DMatrix (src/base/vec_storage.rs:28-32).  ``data`` is a flat
+    CUDA tensor of nrows*ncols elements."""
+
+    def __init__(self, data, nrows: int, ncols: int):
+        torch = _torch()
+        self.data = data if isinstance(data, torch.Tensor) else _dev_f64(data, torch)
+        if self.data.numel() != nrows * ncols:
+            raise ValueError("data size does not match nrows * ncols")
+        self.nrows, self.ncols = int(nrows), int(ncols)
+
+    @classmethod
+    def from_numpy(cls, a) -> "DeviceMatrix":
+        a = np.asarray(a, dtype=np.float64)
+        if a.ndim == 1:
+            a = a.reshape(-1, 1)
+        flat = np.asfortranarray(a).ravel(order="F")
+        return cls(flat, a.shape[0], a.shape[1])
+
+    def to_numpy(self) -> np.ndarray:
+        return self.data.cpu().numpy().reshape(self.ncols, self.nrows).T.copy()
+
+    @property
+    def shape(self):
+        return (self.nrows, self.ncols)
+
+    def is_square(self) -> bool:
+        return self.nrows == self.ncols
+
+    def clone_owned(self) -> "DeviceMatrix":
+        return DeviceMatrix(self.data.clone(), self.nrows, self.ncols)
+
+    # -- factorizations (consume self: the buffer is factored in place) --------
+    def lu(self, flags: int = 0) -> "LU":
+        """Matrix::lu (src/linalg/decomposition.rs:48-54)."""
+        if not self.is_square():
+            raise NotImplementedError("rectangular LU is not on the GPU path")
+        return LU(self, flags)
+
+    def cholesky(self, flags: int = 0, substitute: float | None = None):
+        """Matrix::cholesky (decomposition.rs:257-262): Cholesky or None."""
+        assert self.is_square(), "The input matrix must be square."
+        ch = Cholesky(self, flags, substitute)
+        return ch if ch._ok() else None
+
+
+class LU:
+    """LU with partial pivoting of one square matrix (n <= 128), packed L\\U in
+    the matrix buffer, per-step pivots on the device."""
+
+    def __init__(self, m: DeviceMatrix, flags: int = 0):
+        torch = _torch()
+        self.lu = m
+        n = m.nrows
+        self.flags = flags
+        self.ipiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
+        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _lib.call("nacu_dgetrf_batched", n, m.data.data_ptr(), n * n, self.ipiv.data_ptr(),
+                  self.info.data_ptr(), 1, flags, _stream_ptr())
+
+    def solve_mut(self, b: DeviceMatrix) -> bool:
+        """LU::solve_mut (src/linalg/lu.rs:242-260)."""
+        n = self.lu.nrows
+        assert b.nrows == n, "LU solve matrix dimension mismatch."
+        info = _torch().zeros(1, dtype=_torch().int32, device="cuda")
+        _lib.call("nacu_dgetrs_batched", n, b.ncols, self.lu.data.data_ptr(), n * n, self.ipiv.data_ptr(),
+                  b.data.data_ptr(), n * b.ncols, info.data_ptr(), 1, self.flags, _stream_ptr())
+        return int(info.item()) == 0
+
+    def solve(self, b: DeviceMatrix):
+        """LU::solve (src/linalg/lu.rs:221-236): a new matrix, or None."""
+        res = b.clone_owned()
+        return res if self.solve_mut(res) else None
+
+    def p(self):
+        """The PermutationSequence as nalgebra stores it: (i, piv) swaps in order."""
+        piv = self.ipiv.cpu().numpy()[: self.lu.nrows]
+        return [(i, int(p)) for i, p in enumerate(piv) if p != i]
+
+    def determinant(self) -> float:
+        """LU::determinant (src/linalg/lu.rs:301-314)."""
+        lu = self.lu.to_numpy()
+        d = 1.0
+        for i in range(self.lu.nrows):
+            d *= lu[i, i]
+        return d * (1.0 if len(self.p()) % 2 == 0 else -1.0)
+
+    def is_invertible(self) -> bool:
+        return int(self.info.item()) == 0
+
+    def l(self) -> np.ndarray:
+        lu = self.lu.to_numpy()
+        return np.tril(lu, -1) + np.eye(lu.shape[0])
+
+    def u(self) -> np.ndarray:
+        return np.triu(self.lu.to_numpy())
+
+
+class Cholesky:
+    """Cholesky factor of one SPD matrix (n <= 512); the strict upper triangle
+    keeps the input values, as nalgebra's l_dirty (src/linalg/cholesky.rs:115)."""
+
+    def __init__(self, m: DeviceMatrix, flags: int = 0, substitute: float | None = None):
+        torch = _torch()
+        self.chol = m
+        self.flags = flags | (FLAG_SUBSTITUTE if substitute is not None else 0)
+        self.substitute = 0.0 if substitute is None else float(substitute)
+        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.logdet = torch.zeros(1, dtype=torch.float64, device="cuda")
+        _lib.call("nacu_dposv", m.nrows, m.data.data_ptr(), 0, 0, self.info.data_ptr(), self.logdet.data_ptr(),
+                  self.substitute, self.flags, _stream_ptr())
+
+    def _ok(self) -> bool:
+        return int(self.info.item()) == 0
+
+    def solve_mut(self, b: DeviceMatrix) -> None:
+        """Cholesky::solve_mut (src/linalg/cholesky.rs:122-129)."""
+        torch = _torch()
+        n = self.chol.nrows
+        assert b.nrows == n
+        ns = torch.tensor([n], dtype=torch.int32, device="cuda")
+        off = torch.zeros(1, dtype=torch.int64, device="cuda")
+        ws = torch.zeros(_lib.load().nacu_ragged_workspace_bytes(1), dtype=torch.uint8, device="cuda")
+        _lib.call("nacu_dpotrs_ragged", 1, n, ns.data_ptr(), off.data_ptr(), self.chol.data.data_ptr(), b.ncols,
+                  off.data_ptr(), b.data.data_ptr(), 0, ws.data_ptr(), ws.numel(), self.flags, _stream_ptr())
+
+    def solve(self, b: DeviceMatrix) -> DeviceMatrix:
+        res = b.clone_owned()
+        self.solve_mut(res)
+        return res
+
+    def ln_determinant(self) -> float:
+        """Cholesky::ln_determinant (src/linalg/cholesky.rs:172-185)."""
+        return float(self.logdet.item())
+
+    def l(self) -> np.ndarray:
+        return np.tril(self.chol.to_numpy())
+
+
+class DeviceBatch:
+    """Many matrices on the GPU, packed back to back (each column-major), with a
+    device offset table: a ragged batch when orders differ.
+
+    ``ns`` are the row counts, ``ms`` the column counts (== ns for square)."""
+
+    def __init__(self, data, nrows, ncols=None, offsets=None):
+        torch = _torch()
+        self.nrows = np.asarray(nrows, dtype=np.int64)
+        self.ncols = self.nrows.copy() if ncols is None else np.asarray(ncols, dtype=np.int64)
+        sizes = self.nrows * self.ncols
+        if offsets is None:
+            offsets = np.concatenate([[0], np.cumsum(sizes)[:-1]]) if sizes.size else np.zeros(0, np.int64)
+        self.offsets = np.asarray(offsets, dtype=np.int64)
+        self.data = data if isinstance(data, torch.Tensor) else _dev_f64(data, torch)
+        self._d_rows = torch.from_numpy(self.nrows.astype(np.int32)).to("cuda")
+        self._d_off = torch.from_numpy(self.offsets).to("cuda")
+
+    @classmethod
+    def from_numpy(cls, mats) -> "DeviceBatch":
+        """From a list of 2-D arrays, or a (batch, n, m) array."""
+        mats = [np.asarray(m, dtype=np.float64).reshape(np.shape(m)[0], -1) for m in mats]
+        flat = np.concatenate([np.asfortranarray(m).ravel(order="F") for m in mats]) if mats else np.zeros(0)
+        return cls(flat, [m.shape[0] for m in mats], [m.shape[1] for m in mats])
+
+    def __len__(self) -> int:
+        return int(self.nrows.size)
+
+    def to_numpy(self):
+        host = self.data.cpu().numpy()
+        return [host[o:o + r * c].reshape(c, r).T.copy()
+                for o, r, c in zip(self.offsets, self.nrows, self.ncols)]
+
+    def clone_owned(self) -> "DeviceBatch":
+        return DeviceBatch(self.data.clone(), self.nrows, self.ncols, self.offsets)
+
+    def is_uniform(self) -> bool:
+        return self.nrows.size > 0 and np.all(self.nrows == self.nrows[0]) and np.all(self.ncols == self.ncols[0])
+
+    def lu(self, flags: int = 0) -> "LUBatch":
+        return LUBatch(self, flags)
+
+    def cholesky(self, flags: int = 0, substitute: float | None = None) -> "CholeskyBatch":
+        return CholeskyBatch(self, flags, substitute)
+
+
+class LUBatch:
+    """Batched LU of equal-order square matrices (n <= 128).  Lazy: the first
+    ``solve`` runs the fused factor + solve kernel."""
+
+    def __init__(self, batch: DeviceBatch, flags: int = 0):
+        torch = _torch()
+        if not batch.is_uniform() or batch.nrows[0] != batch.ncols[0]:
+            raise ValueError("LUBatch needs equal-order square matrices")
+        self.batch = batch
+        self.n = int(batch.nrows[0])
+        self.flags = flags
+        self.ipiv = torch.zeros(len(batch) * self.n, dtype=torch.int32, device="cuda")
+        self.info = torch.zeros(len(batch), dtype=torch.int32, device="cuda")
+        self.factored = False
+
+    def factor(self) -> "LUBatch":
+        if not self.factored:
+            n = self.n
+            _lib.call("nacu_dgetrf_batched", n, self.batch.data.data_ptr(), n * n, self.ipiv.data_ptr(),
+                      self.info.data_ptr(), len(self.batch), self.flags, _stream_ptr())
+            self.factored = True
+        return self
+
+    def solve_mut(self, b: DeviceBatch):
+        """Solves every system in place; returns the device info array
+        (0 = solved, k = U_kk == 0, nalgebra's ``false``)."""
+        n = self.n
+        if not (np.all(b.nrows == n) and b.is_uniform()):
+            raise ValueError("right-hand sides must be n x nrhs each")
+        nrhs = int(b.ncols[0])
+        if self.factored:
+            _lib.call("nacu_dgetrs_batched", n, nrhs, self.batch.data.data_ptr(), n * n, self.ipiv.data_ptr(),
+                      b.data.data_ptr(), n * nrhs, self.info.data_ptr(), len(self.batch), self.flags, _stream_ptr())
+        else:
+            _lib.call("nacu_dgesv_batched", n, nrhs, self.batch.data.data_ptr(), n * n, self.ipiv.data_ptr(),
+                      b.data.data_ptr(), n * nrhs, self.info.data_ptr(), len(self.batch), self.flags, _stream_ptr())
+            self.factored = True
+        return self.info
+
+    def solve(self, b: DeviceBatch) -> DeviceBatch:
+        res = b.clone_owned()
+        self.solve_mut(res)
+        return res
+
+    def pivots(self) -> np.ndarray:
+        self.factor()
+        return self.ipiv.cpu().numpy().reshape(len(self.batch), self.n)
+
+
+class CholeskyBatch:
+    """Ragged batched Cholesky (orders up to 512) in one persistent launch.
+    Lazy: ``solve`` runs factor + solve + log-determinant in one kernel."""
+
+    def __init__(self, batch: DeviceBatch, flags: int = 0, substitute: float | None = None):
+        torch = _torch()
+        if np.any(batch.nrows != batch.ncols):
+            raise ValueError("Cholesky needs square matrices")
+        self.batch = batch
+        self.flags = flags | (FLAG_SUBSTITUTE if substitute is not None else 0)
+        self.substitute = 0.0 if substitute is None else float(substitute)
+        count = len(batch)
+        self.n_max = int(batch.nrows.max()) if count else 0
+        self.info = torch.zeros(count, dtype=torch.int32, device="cuda")
+        self.logdet = torch.zeros(count, dtype=torch.float64, device="cuda")
+        order = np.argsort(-batch.nrows, kind="stable").astype(np.int32)  # largest first
+        self._order = torch.from_numpy(order).to("cuda")
+        self._ws = torch.zeros(_lib.load().nacu_ragged_workspace_bytes(count), dtype=torch.uint8, device="cuda")
+        self.factored = False
+
+    def factor(self) -> "CholeskyBatch":
+        if not self.factored:
+            b = self.batch
+            _lib.call("nacu_dpotrf_ragged", len(b), self.n_max, b._d_rows.data_ptr(), b._d_off.data_ptr(),
+                      b.data.data_ptr(), self.info.data_ptr(), self.logdet.data_ptr(), self._order.data_ptr(),
+                      self._ws.data_ptr(), self._ws.numel(), self.substitute, self.flags, _stream_ptr())
+            self.factored = True
+        return self
+
+    def solve_mut(self, rhs: DeviceBatch):
+        """Solve in place; returns the device info array (0 = SPD and solved)."""
+        b = self.batch
+        if len(rhs) != len(b) or np.any(rhs.nrows != b.nrows):
+            raise ValueError("one n x nrhs right-hand side block per matrix")
+        nrhs = int(rhs.ncols[0]) if len(rhs) else 0
+        if len(rhs) and np.any(rhs.ncols != nrhs):
+            raise ValueError("every right-hand side block needs the same nrhs")
+        if self.factored:
+            _lib.call("nacu_dpotrs_ragged", len(b), self.n_max, b._d_rows.data_ptr(), b._d_off.data_ptr(),
+                      b.data.data_ptr(), nrhs, rhs._d_off.data_ptr(), rhs.data.data_ptr(), self._order.data_ptr(),
+                      self._ws.data_ptr(), self._ws.numel(), self.flags, _stream_ptr())
+        else:
+            _lib.call("nacu_dposv_ragged", len(b), self.n_max, b._d_rows.data_ptr(), b._d_off.data_ptr(),
+                      b.data.data_ptr(), nrhs, rhs._d_off.data_ptr(), rhs.data.data_ptr(), self.info.data_ptr(),
+                      self.logdet.data_ptr(), self._order.data_ptr(), self._ws.data_ptr(), self._ws.numel(),
+                      self.substitute, self.flags, _stream_ptr())
+            self.factored = True
+        return self.info
+
+    def solve(self, rhs: DeviceBatch) -> DeviceBatch:
+        res = rhs.clone_owned()
+        self.solve_mut(res)
+        return res
+
+    def ln_determinant(self) -> np.ndarray:
+        self.factor()
+        return self.logdet.cpu().numpy()
+
+    def is_ok(self) -> np.ndarray:
+        """Per matrix: True where nalgebra's ``cholesky()`` returns Some."""
+        self.factor()
+        return self.info.cpu().numpy() == 0

@@ -1,0 +1,94 @@
+// Library-level entry points: version, error reporting, the FP64 roofline probe.
+#include <cstdio>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace nacu {
+
+namespace {
+thread_local char g_last_error[512] = "";
+}
+
+int record_cuda_error(cudaError_t e, const char* where) {
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s: CUDA error %d (%s)", where, (int)e, cudaGetErrorString(e));
+  return NACU_ERR_CUDA;
+}
+
+int record_arg_error(int code, const char* msg) {
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s (argument %d)", msg, -code);
+  return code;
+}
+
+namespace {
+
+__device__ double g_probe_sink;
+
+// Eight independent DFMA chains per thread; the result is stored only when it
+// equals an impossible value, so the chains are live but nothing is written.
+__global__ void fp64_probe_kernel(int iters, double s) {
+  double a0 = threadIdx.x * 1e-3, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
+  double a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+  const double m = 0.999999;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, m, s);
+    a1 = fma(a1, m, s);
+    a2 = fma(a2, m, s);
+    a3 = fma(a3, m, s);
+    a4 = fma(a4, m, s);
+    a5 = fma(a5, m, s);
+    a6 = fma(a6, m, s);
+    a7 = fma(a7, m, s);
+  }
+  const double r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (r == -12345.678) g_probe_sink = r;
+}
+
+}  // namespace
+}  // namespace nacu
+
+extern "C" {
+
+const char* nacu_version(void) { return "0.1.0"; }
+
+const char* nacu_last_error(void) { return nacu::g_last_error; }
+
+int nacu_device_arch(void) {
+#if defined(NACU_ARCH)
+  return NACU_ARCH;
+#else
+  return 103;
+#endif
+}
+
+int nacu_probe_fp64_peak(double* flops) {
+  using namespace nacu;
+  if (!flops) return record_arg_error(-1, "probe_fp64_peak: null output");
+  const int blocks = sm_count() * 8, threads = 256, iters = 4000;
+  cudaEvent_t e0, e1;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e != cudaSuccess) return record_cuda_error(e, "probe_fp64_peak");
+  cudaEventCreate(&e1);
+  double best = 0.0;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(e0, 0);
+    fp64_probe_kernel<<<blocks, threads>>>(iters, 1e-9);
+    cudaEventRecord(e1, 0);
+    e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return record_cuda_error(e, "probe_fp64_peak");
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double f = 2.0 * 8.0 * (double)blocks * threads * iters / (ms * 1e-3);
+    if (rep > 0 && f > best) best = f;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *flops = best;
+  return check_launch("probe_fp64_peak");
+}
+
+}  // extern "C"

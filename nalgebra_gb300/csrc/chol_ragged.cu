@@ -1,0 +1,492 @@
+// Ragged batched Cholesky factor + solve + log-determinant: the GPU form of
+// nalgebra's `m.cholesky()` then `.solve(&b)` and `.ln_determinant()` over
+// thousands of SPD matrices of uneven order, in ONE persistent launch.
+//
+// Follows src/linalg/cholesky.rs:221-272 (Cholesky::new_internal, left-looking,
+// lower triangle only, upper triangle left untouched), cholesky.rs:122-143
+// (solve_mut: src/linalg/solve.rs:488-519 forward in axpy form, then
+// solve.rs:697-712/732-755 adjoint back solve in dot form) and
+// cholesky.rs:172-185 (ln_determinant = sum ln(L_ii^2)).
+//
+// Design (GB300): the FP64 pipe (~1 TFLOP/s) binds, HBM does not.  Each CTA
+// factors one matrix at a time, pulling matrix indices from a device work queue
+// ordered largest-first (so the short tail is made of small matrices).  The
+// factorization is left-looking by NB-column panels: the panel lives in shared
+// memory, the update by all earlier columns is a register-tiled product whose
+// operands stream from L1/L2 (the matrix was just written by this CTA and is
+// hot), and the panel itself is factored in shared memory with the trailing
+// panel update spread evenly over all threads.  Every element still receives
+// its updates in nalgebra's order (k = 0, 1, ..., j-1), so with EXACT the
+// factor is bit-identical to nalgebra's.  The triangular solves are blocked by
+// 32 rows: one warp solves each diagonal block out of registers with shuffles,
+// the whole CTA applies the block to the remaining rows.
+#include "common.cuh"
+
+namespace nacu {
+namespace {
+
+constexpr int kCholThreads = 256;
+constexpr int kNB = 32;        // panel width
+constexpr int kRhsChunk = 4;   // right-hand sides per register pass
+
+struct CholArgs {
+  int count;
+  int n_max;
+  const int32_t* ns;
+  const int64_t* aoff;
+  double* A;
+  int nrhs;
+  const int64_t* boff;
+  double* B;
+  int32_t* info;
+  double* logdet;
+  const int32_t* order;
+  int32_t* counter;
+  int has_subst;
+  double subst;
+  int do_factor;  // 0: A already holds the factor (solve only)
+};
+
+__device__ __forceinline__ bool chol_pivot(double d, int has_subst, double subst, double* denom) {
+  // cholesky.rs:237-268: re <= 0 -> None, else try_sqrt (x >= 0); NaN fails.
+  if (!(d <= 0.0) && d >= 0.0) {
+    *denom = sqrt(d);
+    return true;
+  }
+  if (has_subst && !(subst <= 0.0) && subst >= 0.0) {
+    *denom = sqrt(subst);
+    return true;
+  }
+  return false;
+}
+
+// Factor one n x n matrix (column-major, lda = n, global memory, in place).
+// Returns info (0 ok, j+1 first failing pivot) in *s_info for all threads.
+template <bool EXACT>
+__device__ void chol_factor_cta(int n, double* __restrict__ a, int ldp, double* __restrict__ P, int* s_info,
+                                double* s_scal, int has_subst, double subst) {
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+  for (int J0 = 0; J0 < n; J0 += kNB) {
+    const int jb = min(kNB, n - J0);
+    const int rows = n - J0;
+    // Phase 1+2: P = A[J0.., J0..J0+jb] - L[J0.., 0..J0] * L[J0..J0+jb, 0..J0]^T
+    // (lower part).  Warp w owns columns 4w..4w+3, lanes own rows lane + 32q.
+    {
+      const int warp = tid >> 5, lane = tid & 31;
+      const int qmax = (rows + 31) >> 5;
+      for (int cg = warp * 4; cg < jb; cg += (nthr >> 5) * 4) {
+        double acc[8][4];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int r = lane + 32 * q, c = cg + j;
+            acc[q][j] = (q < qmax && r < rows && c < jb && r >= c) ? a[(size_t)(J0 + c) * n + J0 + r] : 0.0;
+          }
+        for (int k = 0; k < J0; ++k) {
+          const double* colk = a + (size_t)k * n + J0;
+          double lc[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) lc[j] = (cg + j < jb) ? -colk[cg + j] : 0.0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            if (q < qmax) {
+              const int r = lane + 32 * q;
+              const double lr = (r < rows) ? colk[r] : 0.0;
+#pragma unroll
+              for (int j = 0; j < 4; ++j) acc[q][j] = axpy1<EXACT>(acc[q][j], lc[j], lr);
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int r = lane + 32 * q, c = cg + j;
+            if (q < qmax && r < rows && c < jb && r >= c) P[(size_t)c * ldp + r] = acc[q][j];
+          }
+      }
+    }
+    __syncthreads();
+    // Phase 3: factor the panel in shared memory (right-looking inside the
+    // panel, which applies the same per-element update order).
+    for (int j = 0; j < jb; ++j) {
+      double* pj = P + (size_t)j * ldp;
+      if (tid == 0) {
+        double denom;
+        if (chol_pivot(pj[j], has_subst, subst, &denom)) {
+          pj[j] = denom;
+          s_scal[0] = denom;
+          s_scal[1] = 1.0 / denom;
+        } else {
+          *s_info = J0 + j + 1;
+        }
+      }
+      __syncthreads();
+      if (*s_info != 0) return;
+      const double denom = s_scal[0], rcp = s_scal[1];
+      for (int r = j + 1 + tid; r < rows; r += nthr) {
+        if constexpr (EXACT) pj[r] = pj[r] / denom;  // cholesky.rs:261-262 (col /= denom)
+        else pj[r] = pj[r] * rcp;
+      }
+      __syncthreads();
+      const int m = rows - j - 1;  // rows j+1..rows-1
+      const int w = jb - j - 1;    // columns j+1..jb-1
+      if (w > 0) {
+        const int total = m * w;
+        int e = tid;
+        int cq = e / m, rr = e - cq * m;
+        const int dq = nthr / m, dr = nthr - dq * m;
+        for (; e < total; e += nthr) {
+          const int c = j + 1 + cq, r = j + 1 + rr;
+          if (r >= c) {
+            double* pc = P + (size_t)c * ldp;
+            pc[r] = axpy1<EXACT>(pc[r], -pj[c], pj[r]);
+          }
+          rr += dr;
+          cq += dq;
+          if (rr >= m) {
+            rr -= m;
+            ++cq;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // Phase 4: write the finished panel back (lower part; the strict upper
+    // triangle of the diagonal block was never modified).
+    for (int e = tid; e < rows * jb; e += nthr) {
+      const int c = e / rows, r = e - c * rows;
+      if (r >= c) a[(size_t)(J0 + c) * n + J0 + r] = P[(size_t)c * ldp + r];
+    }
+    __syncthreads();
+  }
+}
+
+// Forward solve L y = b (axpy form) for up to kRhsChunk columns of X (shared,
+// column-major ldx), blocked by 32 rows.
+template <bool EXACT>
+__device__ void chol_forward_cta(int n, const double* __restrict__ a, double* X, int ldx, int nr) {
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int I0 = 0; I0 < n; I0 += 32) {
+    const int ib = min(32, n - I0);
+    if (warp == 0) {
+      double lrow[32];
+      double b[kRhsChunk];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) lrow[i] = (lane < ib && i <= lane) ? a[(size_t)(I0 + i) * n + I0 + lane] : 0.0;
+#pragma unroll
+      for (int c = 0; c < kRhsChunk; ++c) b[c] = (lane < ib && c < nr) ? X[(size_t)c * ldx + I0 + lane] : 0.0;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        if (i < ib) {
+#pragma unroll
+          for (int c = 0; c < kRhsChunk; ++c) {
+            if (lane == i) b[c] = b[c] / lrow[i];
+            const double y = __shfl_sync(0xffffffffu, b[c], i);
+            if (lane > i) b[c] = axpy1<EXACT>(b[c], -y, lrow[i]);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < kRhsChunk; ++c)
+        if (lane < ib && c < nr) X[(size_t)c * ldx + I0 + lane] = b[c];
+    }
+    __syncthreads();
+    const int below = n - I0 - ib;
+    for (int e = tid; e < below * nr; e += nthr) {
+      const int c = e / below, r = I0 + ib + (e - c * below);
+      double v = X[(size_t)c * ldx + r];
+      const double* y = X + (size_t)c * ldx + I0;
+      for (int i = 0; i < ib; ++i) v = axpy1<EXACT>(v, -y[i], a[(size_t)(I0 + i) * n + r]);
+      X[(size_t)c * ldx + r] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// Back solve L^T x = y, FMA form: blocked from the bottom, reductions over the
+// rows below each 32-row block, then a warp solve of the transposed block.
+__device__ void chol_backward_fast_cta(int n, const double* __restrict__ a, double* X, int ldx, int nr) {
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
+  const int nblocks = (n + 31) / 32;
+  for (int bI = nblocks - 1; bI >= 0; --bI) {
+    const int I0 = bI * 32;
+    const int ib = min(32, n - I0);
+    const int r0 = I0 + ib;
+    if (r0 < n) {
+      // y_i -= sum_{r >= r0} L[r][i] x_r  for i in the block, all rhs.
+      for (int t = warp; t < ib * nr; t += nwarps) {
+        const int c = t / ib, i = I0 + (t - c * ib);
+        const double* li = a + (size_t)i * n;
+        double* xc = X + (size_t)c * ldx;
+        double s = 0.0;
+        for (int r = r0 + lane; r < n; r += 32) s = fma(li[r], xc[r], s);
+        s = warp_sum(s);
+        if (lane == 0) xc[i] -= s;
+      }
+      __syncthreads();
+    }
+    if (warp == 0) {
+      double lcol[32];  // lane j holds column j of the diagonal block
+#pragma unroll
+      for (int i = 0; i < 32; ++i) lcol[i] = (lane < ib && i < ib && i >= lane) ? a[(size_t)(I0 + lane) * n + I0 + i] : 0.0;
+      for (int c = 0; c < nr; ++c) {
+        double y = (lane < ib) ? X[(size_t)c * ldx + I0 + lane] : 0.0;
+#pragma unroll
+        for (int i = 31; i >= 0; --i) {
+          if (i < ib) {
+            if (lane == i) y = y / lcol[i];
+            const double xi = __shfl_sync(0xffffffffu, y, i);
+            if (lane < i) y = fma(-xi, lcol[i], y);
+          }
+        }
+        if (lane < ib) X[(size_t)c * ldx + I0 + lane] = y;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Back solve L^T x = y in nalgebra's exact order (solve.rs:732-755): for i from
+// n-1 down, x_i = (y_i - dot(L[i+1.., i], x[i+1..])) / L_ii with the
+// 8-accumulator dot of src/base/blas.rs:96-165.  One warp, 8 lanes per rhs.
+__device__ void chol_backward_exact_cta(int n, const double* __restrict__ a, double* X, int ldx, int nr) {
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    const int lane = tid, c = lane >> 3, k = lane & 7;
+    const unsigned grp = 0xffu << (c * 8);
+    double* xc = X + (size_t)(c < nr ? c : 0) * ldx;
+    for (int i = n - 1; i >= 0; --i) {
+      const int len = n - i - 1;
+      const double* li = a + (size_t)i * n + i + 1;
+      const double* xv = xc + i + 1;
+      const int nb = len >> 3;
+      double acc = 0.0;
+      for (int b = 0; b < nb; ++b) acc = __dadd_rn(acc, __dmul_rn(li[8 * b + k], xv[8 * b + k]));
+      // res += acc0 + acc4; res += acc1 + acc5; res += acc2 + acc6; res += acc3 + acc7
+      const double hi = __shfl_down_sync(0xffffffffu, acc, 4, 8);
+      double res = 0.0;
+      double pair = __dadd_rn(acc, hi);  // valid on k < 4
+      const double p0 = __shfl_sync(0xffffffffu, pair, 0, 8);
+      const double p1 = __shfl_sync(0xffffffffu, pair, 1, 8);
+      const double p2 = __shfl_sync(0xffffffffu, pair, 2, 8);
+      const double p3 = __shfl_sync(0xffffffffu, pair, 3, 8);
+      if (k == 0 && c < nr) {
+        res = __dadd_rn(res, p0);
+        res = __dadd_rn(res, p1);
+        res = __dadd_rn(res, p2);
+        res = __dadd_rn(res, p3);
+        for (int t = 8 * nb; t < len; ++t) res = __dadd_rn(res, __dmul_rn(li[t], xv[t]));
+        xc[i] = __ddiv_rn(__dsub_rn(xc[i], res), a[(size_t)i * n + i]);
+      }
+      (void)grp;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+}
+
+template <bool EXACT>
+__device__ void chol_solve_one(const CholArgs& g, int s, double* P, double* X, int* s_info, double* s_scal) {
+  const int tid = threadIdx.x;
+  const int n = g.ns ? g.ns[s] : g.n_max;
+  if (n < 0 || n > g.n_max) {
+    if (tid == 0) {
+      if (g.info) g.info[s] = -1;
+      if (g.logdet) g.logdet[s] = __longlong_as_double(0x7ff8000000000000ll);
+    }
+    return;
+  }
+  double* a = g.A + (g.aoff ? g.aoff[s] : 0);
+  if (tid == 0) *s_info = 0;
+  __syncthreads();
+  const int ldp = g.n_max | 1;
+  if (g.do_factor) chol_factor_cta<EXACT>(n, a, ldp, P, s_info, s_scal, g.has_subst, g.subst);
+  const int inf = *s_info;
+  if (inf == 0) {
+    if (g.nrhs > 0 && g.B) {
+      double* b = g.B + (g.boff ? g.boff[s] : 0);
+      const int ldx = ldp;
+      for (int c0 = 0; c0 < g.nrhs; c0 += kRhsChunk) {
+        const int nr = min(kRhsChunk, g.nrhs - c0);
+        for (int e = tid; e < n * nr; e += blockDim.x) {
+          const int c = e / n, r = e - c * n;
+          X[(size_t)c * ldx + r] = b[(size_t)(c0 + c) * n + r];
+        }
+        __syncthreads();
+        chol_forward_cta<EXACT>(n, a, X, ldx, nr);
+        if constexpr (EXACT) chol_backward_exact_cta(n, a, X, ldx, nr);
+        else chol_backward_fast_cta(n, a, X, ldx, nr);
+        for (int e = tid; e < n * nr; e += blockDim.x) {
+          const int c = e / n, r = e - c * n;
+          b[(size_t)(c0 + c) * n + r] = X[(size_t)c * ldx + r];
+        }
+        __syncthreads();
+      }
+    }
+    if (g.logdet) {
+      if constexpr (EXACT) {
+        if (tid == 0) {
+          double sum = 0.0;
+          for (int i = 0; i < n; ++i) {
+            const double d = a[(size_t)i * n + i];
+            sum = __dadd_rn(sum, log(__dmul_rn(d, d)));
+          }
+          g.logdet[s] = sum;
+        }
+      } else {
+        double part = 0.0;
+        for (int i = tid; i < n; i += blockDim.x) {
+          const double d = a[(size_t)i * n + i];
+          part += log(d * d);
+        }
+        part = warp_sum(part);
+        if ((tid & 31) == 0) s_scal[2 + (tid >> 5)] = part;
+        __syncthreads();
+        if (tid == 0) {
+          double sum = 0.0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += s_scal[2 + w];
+          g.logdet[s] = sum;
+        }
+      }
+    }
+  } else if (tid == 0 && g.logdet) {
+    g.logdet[s] = __longlong_as_double(0x7ff8000000000000ll);
+  }
+  if (tid == 0 && g.info) g.info[s] = inf;
+  __syncthreads();
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(kCholThreads, 2) chol_ragged_kernel(CholArgs g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  __shared__ int s_info;
+  __shared__ double s_scal[2 + kCholThreads / 32];
+  const int ldp = g.n_max | 1;
+  double* P = reinterpret_cast<double*>(smem_raw);
+  double* X = P + (size_t)ldp * kNB;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = g.counter ? atomicAdd(g.counter, 1) : 0;
+    __syncthreads();
+    const int idx = s_item;
+    __syncthreads();
+    if (idx >= g.count) break;
+    const int s = g.order ? g.order[idx] : idx;
+    chol_solve_one<EXACT>(g, s, P, X, &s_info, s_scal);
+    if (!g.counter) break;  // single-matrix launch
+  }
+}
+
+size_t chol_smem_bytes(int n_max) {
+  const int ldp = n_max | 1;
+  return (size_t)ldp * (kNB + kRhsChunk) * sizeof(double);
+}
+
+int chol_launch(CholArgs g, int flags, cudaStream_t stream, bool persistent, const char* name) {
+  const bool exact = (flags & NACU_FLAG_EXACT) != 0;
+  auto kern = exact ? chol_ragged_kernel<true> : chol_ragged_kernel<false>;
+  const size_t smem = chol_smem_bytes(g.n_max);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  int grid = 1;
+  if (persistent) {
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCholThreads, smem);
+    if (e != cudaSuccess) return record_cuda_error(e, name);
+    if (per_sm < 1) per_sm = 1;
+    grid = sm_count() * per_sm;
+    if (grid > g.count) grid = g.count;
+    e = cudaMemsetAsync(g.counter, 0, sizeof(int32_t), stream);
+    if (e != cudaSuccess) return record_cuda_error(e, name);
+  }
+  kern<<<grid, kCholThreads, smem, stream>>>(g);
+  return check_launch(name);
+}
+
+}  // namespace
+}  // namespace nacu
+
+extern "C" {
+
+size_t nacu_ragged_workspace_bytes(int count) {
+  (void)count;
+  return 256;  // the work-queue head (one int32, padded)
+}
+
+static int ragged_args(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, double* A,
+                       void* workspace, size_t workspace_bytes, const char* name) {
+  using namespace nacu;
+  (void)name;
+  if (count < 0) return record_arg_error(-1, "ragged Cholesky: negative count");
+  if (n_max < 0 || n_max > NACU_CHOL_RAGGED_MAX_N)
+    return record_arg_error(-2, "ragged Cholesky: n_max out of range [0, 512]");
+  if (count == 0) return 1;
+  if (!ns || !a_offsets || !A) return record_arg_error(-3, "ragged Cholesky: null ns, a_offsets or A");
+  if (!workspace || workspace_bytes < nacu_ragged_workspace_bytes(count))
+    return record_arg_error(-12, "ragged Cholesky: workspace too small");
+  return 0;
+}
+
+int nacu_dposv_ragged(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, double* A, int nrhs,
+                      const int64_t* b_offsets, double* B, int32_t* info, double* logdet, const int32_t* order,
+                      void* workspace, size_t workspace_bytes, double substitute, int flags,
+                      nacu_stream_t stream) {
+  using namespace nacu;
+  int rc = ragged_args(count, n_max, ns, a_offsets, A, workspace, workspace_bytes, "nacu_dposv_ragged");
+  if (rc != 0) return rc > 0 ? NACU_SUCCESS : rc;
+  if (nrhs < 0) return record_arg_error(-6, "dposv_ragged: negative nrhs");
+  if (nrhs > 0 && (!b_offsets || !B)) return record_arg_error(-7, "dposv_ragged: null b_offsets or B");
+  if (!info) return record_arg_error(-9, "dposv_ragged: null info");
+  CholArgs g{count, n_max, ns, a_offsets, A, nrhs, b_offsets, B, info, logdet, order,
+             reinterpret_cast<int32_t*>(workspace), (flags & NACU_FLAG_SUBSTITUTE) ? 1 : 0, substitute, 1};
+  return chol_launch(g, flags, (cudaStream_t)stream, true, "nacu_dposv_ragged");
+}
+
+int nacu_dpotrf_ragged(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, double* A,
+                       int32_t* info, double* logdet, const int32_t* order, void* workspace,
+                       size_t workspace_bytes, double substitute, int flags, nacu_stream_t stream) {
+  using namespace nacu;
+  int rc = ragged_args(count, n_max, ns, a_offsets, A, workspace, workspace_bytes, "nacu_dpotrf_ragged");
+  if (rc != 0) return rc > 0 ? NACU_SUCCESS : rc;
+  if (!info) return record_arg_error(-6, "dpotrf_ragged: null info");
+  CholArgs g{count, n_max, ns, a_offsets, A, 0, nullptr, nullptr, info, logdet, order,
+             reinterpret_cast<int32_t*>(workspace), (flags & NACU_FLAG_SUBSTITUTE) ? 1 : 0, substitute, 1};
+  return chol_launch(g, flags, (cudaStream_t)stream, true, "nacu_dpotrf_ragged");
+}
+
+int nacu_dpotrs_ragged(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, const double* L,
+                       int nrhs, const int64_t* b_offsets, double* B, const int32_t* order, void* workspace,
+                       size_t workspace_bytes, int flags, nacu_stream_t stream) {
+  using namespace nacu;
+  int rc = ragged_args(count, n_max, ns, a_offsets, const_cast<double*>(L), workspace, workspace_bytes,
+                       "nacu_dpotrs_ragged");
+  if (rc != 0) return rc > 0 ? NACU_SUCCESS : rc;
+  if (nrhs < 0) return record_arg_error(-6, "dpotrs_ragged: negative nrhs");
+  if (nrhs == 0) return NACU_SUCCESS;
+  if (!b_offsets || !B) return record_arg_error(-7, "dpotrs_ragged: null b_offsets or B");
+  CholArgs g{count, n_max, ns, a_offsets, const_cast<double*>(L), nrhs, b_offsets, B, nullptr, nullptr, order,
+             reinterpret_cast<int32_t*>(workspace), 0, 0.0, 0};
+  return chol_launch(g, flags, (cudaStream_t)stream, true, "nacu_dpotrs_ragged");
+}
+
+int nacu_dposv(int n, double* A, int nrhs, double* B, int32_t* info, double* logdet, double substitute,
+               int flags, nacu_stream_t stream) {
+  using namespace nacu;
+  if (n < 0 || n > NACU_CHOL_RAGGED_MAX_N) return record_arg_error(-1, "dposv: n out of range [0, 512]");
+  if (n == 0) return NACU_SUCCESS;
+  if (!A) return record_arg_error(-2, "dposv: null A");
+  if (nrhs < 0) return record_arg_error(-3, "dposv: negative nrhs");
+  if (nrhs > 0 && !B) return record_arg_error(-4, "dposv: null B");
+  if (!info) return record_arg_error(-5, "dposv: null info");
+  // One matrix, one CTA: the plain per-matrix launch (no work queue).
+  CholArgs g{1, n, nullptr, nullptr, A, nrhs, nullptr, B, info, logdet, nullptr, nullptr,
+             (flags & NACU_FLAG_SUBSTITUTE) ? 1 : 0, substitute, 1};
+  return chol_launch(g, flags, (cudaStream_t)stream, false, "nacu_dposv");
+}
+
+}  // extern "C"

@@ -1,0 +1,80 @@
+// Shared device helpers for the nalgebra-cuda kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/nalgebra_cuda.h"
+
+namespace nacu {
+
+// Records a CUDA error (from a launch or a runtime call) for nacu_last_error().
+int record_cuda_error(cudaError_t e, const char* where);
+// Records an argument error message; returns `code`.
+int record_arg_error(int code, const char* msg);
+
+inline int check_launch(const char* where) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return record_cuda_error(e, where);
+  return NACU_SUCCESS;
+}
+
+inline int sm_count() {
+  static int count = 0;
+  if (count == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+    if (count <= 0) count = 1;
+  }
+  return count;
+}
+
+// One element of nalgebra's axpy (src/base/blas_uninit.rs:32-53 with c = beta = 1):
+// y + a*x.  EXACT keeps nalgebra's two roundings (fl(fl(a*x) + y)); otherwise one FMA.
+template <bool EXACT, typename T>
+__device__ __forceinline__ T axpy1(T y, T a, T x) {
+  if constexpr (EXACT) {
+    if constexpr (sizeof(T) == 8) return __dadd_rn(__dmul_rn(a, x), y);
+    else return __fadd_rn(__fmul_rn(a, x), y);
+  } else {
+    if constexpr (sizeof(T) == 8) return fma(a, x, y);
+    else return fmaf(a, x, y);
+  }
+}
+
+// Pivot key for icamax (src/base/min_max.rs:221-240): |x| compared as an
+// unsigned integer (valid for non-negative IEEE values); a NaN wins only at
+// the first position of the scan (where nalgebra's running max starts), and is
+// ignored elsewhere.  Ties resolve to the lowest index by the reduction.
+__device__ __forceinline__ uint64_t pivot_key(double x, bool first) {
+  uint64_t b = (uint64_t)__double_as_longlong(x) & 0x7fffffffffffffffull;
+  if (b > 0x7ff0000000000000ull) return first ? ~0ull : 0ull;
+  return b;
+}
+__device__ __forceinline__ uint64_t pivot_key(float x, bool first) {
+  uint32_t b = (uint32_t)__float_as_uint(x) & 0x7fffffffu;
+  if (b > 0x7f800000u) return first ? ~0ull : 0ull;
+  return (uint64_t)b;
+}
+
+// Warp argmax of (key, idx): larger key wins, equal keys keep the lower index.
+__device__ __forceinline__ void warp_argmax(uint64_t& key, int& idx) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    uint64_t k2 = __shfl_xor_sync(0xffffffffu, key, off);
+    int i2 = __shfl_xor_sync(0xffffffffu, idx, off);
+    if (k2 > key || (k2 == key && i2 < idx)) {
+      key = k2;
+      idx = i2;
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+}  // namespace nacu

@@ -1,0 +1,221 @@
+// TEST INFRASTRUCTURE ONLY — C entry points of the CPU oracle (nalgebra_ref.hpp)
+// for the parity tests and the timed CPU baseline.  Nothing in the product
+// (the CUDA library or its host mirrors) links or calls this.
+//
+// Batched drivers parallelise across independent systems with OpenMP, one
+// system per thread, exactly as a caller would run nalgebra's single-threaded
+// LU/Cholesky/QR on many matrices.
+#include <omp.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "nalgebra_ref.hpp"
+
+using orc::two_prod;
+using orc::two_sum;
+
+namespace {
+void set_threads(int nthreads) {
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+}
+}  // namespace
+
+extern "C" {
+
+int orc_max_threads(void) { return omp_get_max_threads(); }
+
+// ---- single-matrix restatements (f64 and f32) -------------------------------
+double orc_ddot(int64_t n, const double* x, const double* y) { return orc::dot<double>(n, x, y); }
+
+int64_t orc_dgetrf(int64_t m, int64_t n, double* a, int64_t lda, int32_t* ipiv) {
+  return (int64_t)orc::lu_factor<double>(m, n, a, lda, ipiv);
+}
+int64_t orc_sgetrf(int64_t m, int64_t n, float* a, int64_t lda, int32_t* ipiv) {
+  return (int64_t)orc::lu_factor<float>(m, n, a, lda, ipiv);
+}
+int orc_dgetrs(int64_t n, const double* lu, int64_t lda, const int32_t* ipiv, double* b, int64_t ldb,
+               int64_t nrhs) {
+  return orc::lu_solve<double>(n, lu, lda, ipiv, b, ldb, nrhs) ? 1 : 0;
+}
+double orc_dlu_determinant(int64_t n, const double* lu, int64_t lda, int64_t len) {
+  return orc::lu_determinant<double>(n, lu, lda, len);
+}
+int orc_dpotrf(int64_t n, double* a, int64_t lda, int has_substitute, double substitute) {
+  return orc::cholesky_factor<double>(n, a, lda, has_substitute, substitute);
+}
+int orc_spotrf(int64_t n, float* a, int64_t lda, int has_substitute, float substitute) {
+  return orc::cholesky_factor<float>(n, a, lda, has_substitute, substitute);
+}
+void orc_dpotrs(int64_t n, const double* l, int64_t lda, double* b, int64_t ldb, int64_t nrhs) {
+  orc::cholesky_solve<double>(n, l, lda, b, ldb, nrhs);
+}
+double orc_dpotrf_ln_det(int64_t n, const double* l, int64_t lda) {
+  return orc::cholesky_ln_determinant<double>(n, l, lda);
+}
+void orc_dgeqrf(int64_t m, int64_t n, double* a, int64_t lda, double* diag) {
+  orc::qr_factor<double>(m, n, a, lda, diag);
+}
+void orc_dqr_q_tr_mul(int64_t m, int64_t n, const double* qr, int64_t lda, const double* diag,
+                      double* b, int64_t ldb, int64_t nrhs) {
+  orc::qr_q_tr_mul<double>(m, n, qr, lda, diag, b, ldb, nrhs);
+}
+int orc_dqr_ls_solve(int64_t m, int64_t n, const double* qr, int64_t lda, const double* diag,
+                     double* b, int64_t ldb, double* x, int64_t ldx, int64_t nrhs) {
+  return orc::qr_ls_solve<double>(m, n, qr, lda, diag, b, ldb, x, ldx, nrhs);
+}
+
+// ---- batched drivers (the CPU baseline) -----------------------------------
+// `batch` dense n x n systems packed back to back (stride n*n), one n x nrhs
+// right-hand side each (stride n*nrhs).  Factor in place, solve in place.
+// info[s] = 0 ok, 1 when the solve reported a zero U_ii.
+void orc_dgesv_batched(int64_t batch, int64_t n, double* a, int32_t* ipiv, double* b, int64_t nrhs,
+                       int32_t* info, int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t s = 0; s < batch; ++s) {
+    double* as = a + s * n * n;
+    int32_t* ps = ipiv + s * n;
+    orc::lu_factor<double>(n, n, as, n, ps);
+    info[s] = orc::lu_solve<double>(n, as, n, ps, b + s * n * nrhs, n, nrhs) ? 0 : 1;
+  }
+}
+
+// Ragged Cholesky: matrix s is ns[s] x ns[s] at a + aoff[s], its RHS block
+// ns[s] x nrhs at b + boff[s].  info as cholesky_factor; logdet per matrix.
+void orc_dposv_ragged(int64_t count, const int32_t* ns, const int64_t* aoff, double* a,
+                      const int64_t* boff, double* b, int64_t nrhs, int32_t* info, double* logdet,
+                      int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t s = 0; s < count; ++s) {
+    const int64_t n = ns[s];
+    double* as = a + aoff[s];
+    const int r = orc::cholesky_factor<double>(n, as, n, 0, 0.0);
+    info[s] = r;
+    if (r == 0) {
+      orc::cholesky_solve<double>(n, as, n, b + boff[s], n, nrhs);
+      if (logdet) logdet[s] = orc::cholesky_ln_determinant<double>(n, as, n);
+    } else if (logdet) {
+      logdet[s] = NAN;
+    }
+  }
+}
+
+// Batched least squares: problem s is ms[s] x n at a + aoff[s] with one m x 1
+// RHS at b + boff[s]; x is n x 1 at x + s*n; diag n per problem.
+void orc_dgels_batched(int64_t count, const int32_t* ms, int64_t n, const int64_t* aoff, double* a,
+                       const int64_t* boff, double* b, double* diag, double* x, int32_t* info,
+                       int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t s = 0; s < count; ++s) {
+    const int64_t m = ms[s];
+    double* as = a + aoff[s];
+    orc::qr_factor<double>(m, n, as, m, diag + s * n);
+    info[s] = orc::qr_ls_solve<double>(m, n, as, m, diag + s * n, b + boff[s], m, x + s * n, n, 1);
+  }
+}
+
+// ---- accurate FP64 metrics ---------------------------------------------------
+
+// C = alpha * A * B + beta * C with every dot product accumulated by Dot2
+// (compensated), the accurate reference for the GEMM kernels.  beta == 0 means
+// C is never read (blas.rs:729-746 contract).
+void orc_dgemm_dot2(int64_t m, int64_t n, int64_t k, double alpha, const double* a, int64_t lda,
+                    const double* b, int64_t ldb, double beta, double* c, int64_t ldc,
+                    int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+  for (int64_t j = 0; j < n; ++j) {
+    std::vector<double> arow(k);
+    for (int64_t i = 0; i < m; ++i) {
+      double s = 0.0, e = 0.0;
+      for (int64_t p = 0; p < k; ++p) {
+        double pr, pe, ss, se;
+        two_prod(a[i + p * lda], b[p + j * ldb], &pr, &pe);
+        two_sum(s, pr, &ss, &se);
+        s = ss;
+        e += pe + se;
+      }
+      const double ab = s + e;
+      c[i + j * ldc] = (beta == 0.0) ? alpha * ab : alpha * ab + beta * c[i + j * ldc];
+    }
+  }
+}
+
+// Normwise backward error of x for A x = b, per RHS column, maximum over
+// columns: ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf), residual by Dot2.
+double orc_dbackward_error(int64_t n, const double* a, int64_t lda, const double* x, int64_t ldx,
+                           const double* b, int64_t ldb, int64_t nrhs) {
+  double anorm = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int64_t j = 0; j < n; ++j) s += std::fabs(a[i + j * lda]);
+    if (s > anorm) anorm = s;
+  }
+  double worst = 0.0;
+  for (int64_t c = 0; c < nrhs; ++c) {
+    double rmax = 0.0, xmax = 0.0, bmax = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+      double s = b[i + c * ldb], e = 0.0;
+      for (int64_t j = 0; j < n; ++j) {
+        double pr, pe, ss, se;
+        two_prod(-a[i + j * lda], x[j + c * ldx], &pr, &pe);
+        two_sum(s, pr, &ss, &se);
+        s = ss;
+        e += pe + se;
+      }
+      const double r = std::fabs(s + e);
+      if (r > rmax) rmax = r;
+      if (std::fabs(b[i + c * ldb]) > bmax) bmax = std::fabs(b[i + c * ldb]);
+    }
+    for (int64_t j = 0; j < n; ++j)
+      if (std::fabs(x[j + c * ldx]) > xmax) xmax = std::fabs(x[j + c * ldx]);
+    const double den = anorm * xmax + bmax;
+    const double be = den > 0.0 ? rmax / den : (rmax > 0.0 ? INFINITY : 0.0);
+    if (!(be <= worst)) worst = be;
+  }
+  return worst;
+}
+
+// ||P A - L U||_F / (||A||_F * n * eps64) for packed factors and a per-step
+// pivot list (the spec LU reconstruction criterion).
+double orc_dlu_reconstruction(int64_t n, const double* a, int64_t lda, const double* lu,
+                              int64_t ldlu, const int32_t* ipiv) {
+  std::vector<double> pa(n * n);
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = 0; i < n; ++i) pa[i + j * n] = a[i + j * lda];
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p = ipiv[i];
+    if (p != i)
+      for (int64_t j = 0; j < n; ++j) {
+        const double t = pa[i + j * n];
+        pa[i + j * n] = pa[p + j * n];
+        pa[p + j * n] = t;
+      }
+  }
+  double num = 0.0, den = 0.0;
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = 0; i < n; ++i) {
+      double s = 0.0, e = 0.0;
+      const int64_t kmax = i < j ? i : j;
+      for (int64_t k = 0; k <= kmax; ++k) {
+        const double l = (k == i) ? 1.0 : lu[i + k * ldlu];
+        double pr, pe, ss, se;
+        two_prod(l, lu[k + j * ldlu], &pr, &pe);
+        two_sum(s, pr, &ss, &se);
+        s = ss;
+        e += pe + se;
+      }
+      const double d = pa[i + j * n] - (s + e);
+      num += d * d;
+      den += pa[i + j * n] * pa[i + j * n];
+    }
+  if (n == 0 || den == 0.0) return num == 0.0 ? 0.0 : INFINITY;
+  return std::sqrt(num) / (std::sqrt(den) * (double)n * 2.220446049250313e-16);
+}
+
+}  // extern "C"

@@ -1,0 +1,382 @@
+// TEST INFRASTRUCTURE ONLY — the CPU oracle.
+//
+// A line-by-line C++ restatement of nalgebra 0.35's dense factorization loops
+// (LU with partial pivoting, Cholesky, Householder QR, triangular solves and the
+// 8-accumulator dot product).  It exists to check the CUDA kernels and to time
+// the CPU baseline; no product code path may call it.
+//
+// Build with -O2 -ffp-contract=off and without -ffast-math: Rust never contracts
+// a*b+c into an FMA, so with contraction off every rounding here happens exactly
+// where nalgebra's rounds, and the factors are bit-identical to nalgebra's own on
+// the same inputs.
+//
+// Storage convention (src/base/vec_storage.rs:28-32): column-major, contiguous,
+// element (r, c) of an nrows x ncols matrix at a[r + c * lda].
+#pragma once
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// Scalar helpers (simba 0.10 real-field semantics; simba is not vendored in the
+// reference, these follow its published behaviour for f32/f64).
+// ---------------------------------------------------------------------------
+
+// simba `ComplexField::to_exp` for a real: (|x|, +1) when x >= 0, else (-x, -1).
+// The comparison form means -0.0 maps to sign +1 and NaN to sign -1.
+template <class T>
+inline void to_exp(T x, T* modulus, T* sign) {
+  if (x >= T(0)) {
+    *modulus = x;
+    *sign = T(1);
+  } else {
+    *modulus = -x;
+    *sign = T(-1);
+  }
+}
+
+// Rust `f64::signum`: +1 for +0.0 and positive, -1 for -0.0 and negative, NaN for NaN.
+template <class T>
+inline T signum(T x) {
+  if (std::isnan(x)) return x;
+  return std::signbit(x) ? T(-1) : T(1);
+}
+
+// simba `try_sqrt` for a real: Some(sqrt(x)) when x >= 0, else None (NaN -> None).
+template <class T>
+inline bool try_sqrt(T x, T* out) {
+  if (x >= T(0)) {
+    *out = std::sqrt(x);
+    return true;
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// BLAS-like kernels
+// ---------------------------------------------------------------------------
+
+// Matrix::dotx for one Dyn column (src/base/blas.rs:96-165): eight independent
+// accumulators over blocks of 8, combined as (a0+a4), (a1+a5), (a2+a6), (a3+a7)
+// into `res` (blas.rs:154-157), then the tail added one product at a time.
+template <class T>
+inline T dot(std::size_t n, const T* x, const T* y) {
+  T res = T(0);
+  T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
+  T acc4 = T(0), acc5 = T(0), acc6 = T(0), acc7 = T(0);
+  std::size_t i = 0;
+  while (n - i >= 8) {
+    acc0 += x[i] * y[i];
+    acc1 += x[i + 1] * y[i + 1];
+    acc2 += x[i + 2] * y[i + 2];
+    acc3 += x[i + 3] * y[i + 3];
+    acc4 += x[i + 4] * y[i + 4];
+    acc5 += x[i + 5] * y[i + 5];
+    acc6 += x[i + 6] * y[i + 6];
+    acc7 += x[i + 7] * y[i + 7];
+    i += 8;
+  }
+  res += acc0 + acc4;
+  res += acc1 + acc5;
+  res += acc2 + acc6;
+  res += acc3 + acc7;
+  for (std::size_t k = i; k < n; ++k) res += x[k] * y[k];
+  return res;
+}
+
+// array_axcpy with c = 1 (src/base/blas_uninit.rs:32-53):
+// y[i] = a * x[i] * 1 + beta * y[i].  The two unit factors are exact, so this is
+// fl(fl(a*x[i]) + fl(beta*y[i])).
+template <class T>
+inline void axpy(std::size_t n, T a, const T* x, T beta, T* y) {
+  for (std::size_t i = 0; i < n; ++i) y[i] = a * x[i] * T(1) + beta * y[i];
+}
+
+// Matrix::icamax for a real column (src/base/min_max.rs:221-240): the first
+// index of the largest |x|, strict `>` so ties keep the lower index; a NaN never
+// wins unless it sits at index 0.
+template <class T>
+inline std::size_t icamax(std::size_t n, const T* x) {
+  T the_max = std::fabs(x[0]);
+  std::size_t the_i = 0;
+  for (std::size_t i = 1; i < n; ++i) {
+    T v = std::fabs(x[i]);
+    if (v > the_max) {
+      the_max = v;
+      the_i = i;
+    }
+  }
+  return the_i;
+}
+
+// ---------------------------------------------------------------------------
+// LU with partial pivoting (src/linalg/lu.rs)
+// ---------------------------------------------------------------------------
+
+// gauss_step (lu.rs:337-357) and gauss_step_swap (lu.rs:362-389) on an m x n
+// matrix at step i, with the pivot value `diag` read before any swap.
+template <class T>
+inline void gauss_step(std::size_t m, std::size_t n, T* a, std::size_t lda, T diag, std::size_t i,
+                       std::size_t piv) {
+  const T inv_diag = T(1) / diag;
+  T* coeffs = a + i + i * lda;  // column i, rows i..m
+  if (piv != i) {
+    T t = coeffs[0];
+    coeffs[0] = coeffs[piv - i];
+    coeffs[piv - i] = t;
+  }
+  for (std::size_t r = 1; r < m - i; ++r) coeffs[r] = coeffs[r] * inv_diag;
+  for (std::size_t k = i + 1; k < n; ++k) {
+    T* col = a + i + k * lda;  // rows i..m of column k
+    if (piv != i) {
+      T t = col[0];
+      col[0] = col[piv - i];
+      col[piv - i] = t;
+    }
+    axpy(m - i - 1, -col[0], coeffs + 1, T(1), col + 1);
+  }
+}
+
+// LU::new (lu.rs:93-122).  Writes the packed L\U factors in place, the full
+// per-step pivot row `ipiv[i]` (== i when no swap happened) for i < min(m, n),
+// and returns the number of recorded swaps (PermutationSequence::len,
+// permutation_sequence.rs:84-93).  The (i, ipiv[i]) pairs with ipiv[i] != i, in
+// order, are exactly nalgebra's PermutationSequence entries.
+template <class T>
+inline std::size_t lu_factor(std::size_t m, std::size_t n, T* a, std::size_t lda, int32_t* ipiv) {
+  const std::size_t mn = m < n ? m : n;
+  std::size_t len = 0;
+  for (std::size_t i = 0; i < mn; ++i) {
+    const std::size_t piv = icamax(m - i, a + i + i * lda) + i;
+    const T diag = a[piv + i * lda];
+    ipiv[i] = (int32_t)i;
+    if (diag == T(0)) continue;  // lu.rs:107-110: an all-zero column is skipped
+    if (piv != i) {
+      ipiv[i] = (int32_t)piv;
+      ++len;
+      for (std::size_t c = 0; c < i; ++c) {  // columns_range_mut(..i).swap_rows(i, piv)
+        T t = a[i + c * lda];
+        a[i + c * lda] = a[piv + c * lda];
+        a[piv + c * lda] = t;
+      }
+    }
+    gauss_step(m, n, a, lda, diag, i, piv);
+  }
+  return len;
+}
+
+// LU::solve_mut (lu.rs:242-260): permute_rows, then the unit-lower forward
+// solve (solve.rs:106-133), then the upper back substitution (solve.rs:137-182).
+// Returns false when some U_ii == 0 (columns before the failing one are solved).
+template <class T>
+inline bool lu_solve(std::size_t n, const T* lu, std::size_t lda, const int32_t* ipiv, T* b,
+                     std::size_t ldb, std::size_t nrhs) {
+  for (std::size_t i = 0; i < n; ++i) {  // permutation_sequence.rs:97-104
+    const std::size_t p = (std::size_t)ipiv[i];
+    if (p != i)
+      for (std::size_t c = 0; c < nrhs; ++c) {
+        T t = b[i + c * ldb];
+        b[i + c * ldb] = b[p + c * ldb];
+        b[p + c * ldb] = t;
+      }
+  }
+  if (n == 0) return true;
+  for (std::size_t c = 0; c < nrhs; ++c) {  // with diag = 1
+    T* bc = b + c * ldb;
+    for (std::size_t i = 0; i + 1 < n; ++i) {
+      const T coeff = bc[i] / T(1);
+      axpy(n - i - 1, -coeff, lu + (i + 1) + i * lda, T(1), bc + i + 1);
+    }
+  }
+  for (std::size_t c = 0; c < nrhs; ++c) {
+    T* bc = b + c * ldb;
+    for (std::size_t ii = n; ii-- > 0;) {
+      const T diag = lu[ii + ii * lda];
+      if (diag == T(0)) return false;
+      const T coeff = bc[ii] / diag;
+      bc[ii] = coeff;
+      axpy(ii, -coeff, lu + ii * lda, T(1), bc);
+    }
+  }
+  return true;
+}
+
+// LU::determinant (lu.rs:301-314): product of the diagonal times the sign of
+// the permutation (permutation_sequence.rs:158-164).
+template <class T>
+inline T lu_determinant(std::size_t n, const T* lu, std::size_t lda, std::size_t len) {
+  T res = T(1);
+  for (std::size_t i = 0; i < n; ++i) res *= lu[i + i * lda];
+  return res * ((len % 2 == 0) ? T(1) : T(-1));
+}
+
+// ---------------------------------------------------------------------------
+// Cholesky (src/linalg/cholesky.rs)
+// ---------------------------------------------------------------------------
+
+// Cholesky::new_internal (cholesky.rs:221-272): left-looking, reads the lower
+// triangle only, leaves the strict upper triangle untouched.  Returns 0 on
+// success or j + 1 for the first column whose pivot is not > 0 (NaN included)
+// and could not be replaced by `substitute` (has_substitute != 0).
+template <class T>
+inline int cholesky_factor(std::size_t n, T* a, std::size_t lda, int has_substitute, T substitute) {
+  for (std::size_t j = 0; j < n; ++j) {
+    for (std::size_t k = 0; k < j; ++k) {
+      const T factor = -a[j + k * lda];
+      axpy(n - j, factor, a + j + k * lda, T(1), a + j + j * lda);
+    }
+    const T diag = a[j + j * lda];
+    T denom;
+    bool ok = false;
+    if (!(diag <= T(0))) ok = try_sqrt(diag, &denom);
+    if (!ok && has_substitute && !(substitute <= T(0))) ok = try_sqrt(substitute, &denom);
+    if (!ok) return (int)j + 1;
+    a[j + j * lda] = denom;
+    for (std::size_t r = j + 1; r < n; ++r) a[r + j * lda] = a[r + j * lda] / denom;
+  }
+  return 0;
+}
+
+// Cholesky::solve_mut (cholesky.rs:122-129): forward solve in axpy form
+// (solve.rs:488-519) then the adjoint back solve in dot form (solve.rs:697-712,
+// 732-755).
+template <class T>
+inline void cholesky_solve(std::size_t n, const T* l, std::size_t lda, T* b, std::size_t ldb,
+                           std::size_t nrhs) {
+  for (std::size_t c = 0; c < nrhs; ++c) {
+    T* bc = b + c * ldb;
+    for (std::size_t i = 0; i < n; ++i) {
+      const T coeff = bc[i] / l[i + i * lda];
+      bc[i] = coeff;
+      axpy(n - i - 1, -coeff, l + (i + 1) + i * lda, T(1), bc + i + 1);
+    }
+  }
+  for (std::size_t c = 0; c < nrhs; ++c) {
+    T* bc = b + c * ldb;
+    for (std::size_t ii = n; ii-- > 0;) {
+      const T d = dot(n - ii - 1, l + (ii + 1) + ii * lda, bc + ii + 1);
+      bc[ii] = (bc[ii] - d) / l[ii + ii * lda];
+    }
+  }
+}
+
+// Cholesky::ln_determinant (cholesky.rs:172-185): sum of ln(L_ii * L_ii).
+template <class T>
+inline T cholesky_ln_determinant(std::size_t n, const T* l, std::size_t lda) {
+  T s = T(0);
+  for (std::size_t i = 0; i < n; ++i) {
+    const T d = l[i + i * lda];
+    s += std::log(d * d);
+  }
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Householder QR (src/linalg/qr.rs, householder.rs, geometry/reflection.rs)
+// ---------------------------------------------------------------------------
+
+// Reflection::reflect_with_sign (reflection.rs:70-83) with bias 0 on the
+// `ncols` columns of `c` (each `len` long), axis `v` of length `len`.
+template <class T>
+inline void reflect_with_sign(std::size_t len, const T* v, std::size_t ncols, T* c, std::size_t ldc,
+                              T sign) {
+  for (std::size_t j = 0; j < ncols; ++j) {
+    T* cj = c + j * ldc;
+    const T m_two = sign * T(-2);
+    const T factor = (dot(len, v, cj) - T(0)) * m_two;
+    axpy(len, factor, v, sign, cj);
+  }
+}
+
+// householder::reflection_axis_mut (householder.rs:19-53).  Returns the value
+// of the first component after reflection; *not_zero is false when no
+// reflection was needed (a zero column).
+template <class T>
+inline T reflection_axis(std::size_t len, T* x, bool* not_zero) {
+  const T sq = T(0) + dot(len, x, x);  // norm_squared (norm.rs:238-250)
+  const T nrm = std::sqrt(sq);
+  T modulus, sign;
+  to_exp(x[0], &modulus, &sign);
+  const T signed_norm = sign * nrm;
+  const T factor = (sq + modulus * nrm) * T(2);
+  x[0] += signed_norm;
+  if (factor != T(0)) {
+    const T sf = std::sqrt(factor);
+    for (std::size_t i = 0; i < len; ++i) x[i] = x[i] / sf;  // unscale_mut
+    const T n2 = std::sqrt(T(0) + dot(len, x, x));          // normalize_mut (norm.rs:505-513)
+    for (std::size_t i = 0; i < len; ++i) x[i] = x[i] / n2;
+    *not_zero = true;
+    return -signed_norm;
+  }
+  *not_zero = false;
+  return signed_norm;
+}
+
+// QR::new (qr.rs:55-76) via householder::clear_column_unchecked
+// (householder.rs:61-85) with shift 0.  diag has min(m, n) entries.
+template <class T>
+inline void qr_factor(std::size_t m, std::size_t n, T* a, std::size_t lda, T* diag) {
+  const std::size_t mn = m < n ? m : n;
+  for (std::size_t i = 0; i < mn; ++i) {
+    bool not_zero;
+    T* axis = a + i + i * lda;
+    const T rnorm = reflection_axis(m - i, axis, &not_zero);
+    if (not_zero) reflect_with_sign(m - i, axis, n - i - 1, axis + lda, lda, signum(rnorm));
+    diag[i] = rnorm;
+  }
+}
+
+// QR::q_tr_mul (qr.rs:157-171): rhs <- Q^T rhs.
+template <class T>
+inline void qr_q_tr_mul(std::size_t m, std::size_t n, const T* qr, std::size_t lda, const T* diag,
+                        T* b, std::size_t ldb, std::size_t nrhs) {
+  const std::size_t mn = m < n ? m : n;
+  for (std::size_t i = 0; i < mn; ++i)
+    reflect_with_sign(m - i, qr + i + i * lda, nrhs, b + i, ldb, signum(diag[i]));
+}
+
+// Least squares x = argmin ||A x - b|| for m >= n from the factors: Q^T b
+// (qr.rs:157-171), then the back substitution of qr.rs:224-256 (divide by
+// |diag_i|, axpy with the strict upper part of R) restricted to the top n rows,
+// as nalgebra-lapack's qr_solve_mut_with_rank_unpermuted (qr_util.rs:167-239)
+// restricts dtrtrs to R[0:n, 0:n].  b (m x nrhs) is overwritten by Q^T b; x
+// (n x nrhs) receives the solution.  Returns 0, or i + 1 for the first (from the
+// bottom) zero |diag_i| (rank deficient, LAPACK trtrs info > 0).
+template <class T>
+inline int qr_ls_solve(std::size_t m, std::size_t n, const T* qr, std::size_t lda, const T* diag,
+                       T* b, std::size_t ldb, T* x, std::size_t ldx, std::size_t nrhs) {
+  qr_q_tr_mul(m, n, qr, lda, diag, b, ldb, nrhs);
+  for (std::size_t c = 0; c < nrhs; ++c) {
+    T* xc = x + c * ldx;
+    for (std::size_t r = 0; r < n; ++r) xc[r] = b[r + c * ldb];
+    for (std::size_t ii = n; ii-- > 0;) {
+      const T d = std::fabs(diag[ii]);
+      if (d == T(0)) return (int)ii + 1;
+      const T coeff = xc[ii] / d;
+      xc[ii] = coeff;
+      axpy(ii, -coeff, qr + ii * lda, T(1), xc);
+    }
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Accurate FP64 arithmetic for the parity metrics (not a nalgebra restatement):
+// TwoSum / TwoProduct compensated dot, Ogita, Rump & Oishi (2005), "Accurate
+// sum and dot product", Algorithm Dot2.
+// ---------------------------------------------------------------------------
+inline void two_sum(double a, double b, double* s, double* e) {
+  const double x = a + b;
+  const double z = x - a;
+  *e = (a - (x - z)) + (b - z);
+  *s = x;
+}
+inline void two_prod(double a, double b, double* p, double* e) {
+  const double x = a * b;
+  *e = std::fma(a, b, -x);
+  *p = x;
+}
+
+}  // namespace orc

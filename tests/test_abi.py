@@ -1,0 +1,75 @@
+"""The C-ABI library without a GPU: it builds for sm_103a, loads, exports every
+symbol include/nalgebra_cuda.h declares, and rejects bad arguments with the
+LAPACK-style negative codes before touching the device."""
+import ctypes as C
+
+import pytest
+
+from nalgebra_gb300 import _lib, build
+
+
+@pytest.fixture(scope="module")
+def L():
+    build.build()
+    return _lib.load()
+
+
+def test_exports_every_header_symbol(L):
+    names = _lib.header_symbols()
+    assert len(names) >= 10
+    raw = C.CDLL(_lib.LIB_PATH)
+    missing = [n for n in names if not hasattr(raw, n)]
+    assert not missing, missing
+    # and every declared symbol has a ctypes signature in the host binding
+    assert set(names) <= set(_lib.SIGNATURES), set(names) - set(_lib.SIGNATURES)
+
+
+def test_version_and_arch(L):
+    assert L.nacu_version() == b"0.1.0"
+    assert L.nacu_device_arch() == 103
+
+
+def test_lu_argument_errors(L):
+    assert L.nacu_dgesv_batched(-1, 1, 0, 0, 0, 0, 0, 0, 1, 0, 0) == -1
+    assert L.nacu_dgesv_batched(129, 1, 0, 0, 0, 0, 0, 0, 1, 0, 0) == -1
+    assert L.nacu_dgesv_batched(8, 17, 0, 0, 0, 0, 0, 0, 1, 0, 0) == -2
+    assert b"nrhs" in L.nacu_last_error()
+    assert L.nacu_dgesv_batched(8, 1, 0, 64, 0, 0, 8, 0, -1, 0, 0) == -9
+    # empty work is a no-op success, no device needed
+    assert L.nacu_dgesv_batched(8, 1, 0, 64, 0, 0, 8, 0, 0, 0, 0) == 0
+    assert L.nacu_dgesv_batched(0, 1, 0, 0, 0, 0, 0, 0, 5, 0, 0) == 0
+    # null pointers with real work
+    assert L.nacu_dgesv_batched(8, 1, 0, 64, 0, 0, 8, 0, 2, 0, 0) == -3
+    # stride too small
+    assert L.nacu_dgesv_batched(8, 1, 1024, 10, 1024, 1024, 8, 0, 2, 0, 0) == -4
+
+
+def test_cholesky_argument_errors(L):
+    ws = L.nacu_ragged_workspace_bytes(10)
+    assert ws >= 4
+    assert L.nacu_dposv_ragged(-1, 8, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0.0, 0, 0) == -1
+    assert L.nacu_dposv_ragged(3, 513, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0.0, 0, 0) == -2
+    assert L.nacu_dposv_ragged(0, 8, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0.0, 0, 0) == 0
+    assert L.nacu_dposv_ragged(3, 8, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0.0, 0, 0) == -3
+    # workspace too small
+    assert L.nacu_dposv_ragged(3, 8, 16, 16, 16, 1, 16, 16, 16, 0, 0, 16, 0, 0.0, 0, 0) == -12
+    assert L.nacu_dposv(-2, 0, 0, 0, 0, 0, 0.0, 0, 0) == -1
+    assert L.nacu_dposv(4, 0, 0, 0, 0, 0, 0.0, 0, 0) == -2
+
+
+def test_product_has_no_cpu_fallback(tmp_path):
+    with pytest.raises(_lib.NacuError):
+        _lib.load(str(tmp_path / "missing.so"))
+
+
+def test_product_never_imports_the_oracle():
+    import os
+    import re
+
+    pkg = os.path.dirname(_lib.__file__)
+    for root, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                text = open(os.path.join(root, f)).read()
+                assert not re.search(r"^\s*(import|from)\s+oracle\b", text, re.M), f
+                assert "liboracle" not in text, f

@@ -1,0 +1,239 @@
+"""The CPU oracle (C++ restatement of nalgebra's loops) pinned against the
+reference's own known-answer tests and property tests, and cross-checked with
+scipy's LAPACK.  Runs without a GPU."""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+import oracle as O
+from tests.conftest import EPS64
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _known():
+    with open(os.path.join(GOLD, "reference_known_answers.json")) as f:
+        return json.load(f)
+
+
+def _rows(rows):
+    return np.array([[np.nan if v == "nan" else v for v in r] for r in rows], dtype=np.float64)
+
+
+def _unpack(lu, ipiv):
+    n = lu.shape[0]
+    l = np.tril(lu, -1) + np.eye(n)
+    u = np.triu(lu)
+    return l, u
+
+
+def _inv_permute_rows(m, ipiv):
+    """PermutationSequence::inv_permute_rows (permutation_sequence.rs:108-116)."""
+    m = m.copy()
+    for i in reversed(range(len(ipiv))):
+        p = ipiv[i]
+        if p != i:
+            m[[i, p]] = m[[p, i]]
+    return m
+
+
+@pytest.mark.parametrize("case", ["lu_simple", "lu_simple_with_pivot"])
+def test_lu_known_answers(case):
+    k = _known()[case]
+    m = _rows(k["rows"])
+    lu, ipiv, ln = O.lu(m)
+    assert O.lu_determinant(lu, ln) == k["determinant"]  # exact, as assert_eq! in the reference
+    l, u = _unpack(lu, ipiv)
+    rec = _inv_permute_rows(l @ u, ipiv)
+    assert np.allclose(rec, m, atol=k["reconstruction_epsilon"], rtol=0)
+    if case == "lu_simple_with_pivot":
+        assert ln == 1 and list(ipiv) == [2, 1, 2]
+
+
+def test_cholesky_with_substitute_known_answer():
+    k = _known()["cholesky_with_substitute"]
+    m = _rows(k["rows"])
+    _, info = O.cholesky(m)
+    assert info != 0  # None
+    _, info2 = O.cholesky(m, substitute=k["substitute"])
+    assert info2 == 0  # Some
+
+
+def test_dot_eight_accumulators():
+    """blas.rs:96-165: blocks of 8 into 8 accumulators, combined (0+4),(1+5),
+    (2+6),(3+7), then the tail."""
+    rng = np.random.default_rng(3)
+    for n in [0, 1, 7, 8, 9, 16, 23, 64, 100]:
+        x = rng.standard_normal(n)
+        y = rng.standard_normal(n)
+        acc = [0.0] * 8
+        i = 0
+        while n - i >= 8:
+            for k in range(8):
+                acc[k] += x[i + k] * y[i + k]
+            i += 8
+        res = 0.0
+        res += acc[0] + acc[4]
+        res += acc[1] + acc[5]
+        res += acc[2] + acc[6]
+        res += acc[3] + acc[7]
+        for k in range(i, n):
+            res += x[k] * y[k]
+        assert O.dot(x, y) == res
+
+
+def _pure_python_lu(a):
+    """Independent pure-Python restatement of LU::new for tiny matrices."""
+    a = [list(map(float, r)) for r in a]
+    n = len(a)
+    ipiv = list(range(n))
+    for i in range(n):
+        piv, best = i, abs(a[i][i])
+        for r in range(i + 1, n):
+            if abs(a[r][i]) > best:
+                best, piv = abs(a[r][i]), r
+        diag = a[piv][i]
+        if diag == 0.0:
+            continue
+        ipiv[i] = piv
+        a[i], a[piv] = a[piv], a[i]
+        inv = 1.0 / diag
+        for r in range(i + 1, n):
+            a[r][i] = a[r][i] * inv
+        for c in range(i + 1, n):
+            p = a[i][c]
+            for r in range(i + 1, n):
+                a[r][c] = (-p) * a[r][i] + a[r][c]
+    return np.array(a), np.array(ipiv)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 6, 9])
+def test_lu_matches_pure_python_restatement_bitwise(n):
+    rng = np.random.default_rng(n)
+    a = rng.uniform(-100, 100, size=(n, n))  # PROPTEST_F64 range, tests/proptest/mod.rs:19-20
+    lu, ipiv, _ = O.lu(a)
+    lu2, ipiv2 = _pure_python_lu(a)
+    assert np.array_equal(ipiv, ipiv2)
+    assert np.array_equal(lu, lu2)
+
+
+@pytest.mark.parametrize("n", [1, 4, 13, 20])
+def test_lu_properties(n):
+    """tests/linalg/lu.rs:54-105: reconstruction 1e-7, solve residual 1e-6,
+    and scipy's partial pivoting picks the same rows."""
+    rng = np.random.default_rng(100 + n)
+    a = rng.uniform(-100, 100, size=(n, n))
+    lu, ipiv, _ = O.lu(a)
+    l, u = _unpack(lu, ipiv)
+    assert np.allclose(_inv_permute_rows(l @ u, ipiv), a, atol=1e-7 * np.abs(a).max())
+    b = rng.uniform(-100, 100, size=(n, 3))
+    x = O.lu_solve(lu, ipiv, b)
+    assert np.allclose(a @ x, b, atol=1e-6 * max(1.0, np.abs(b).max()))
+    _, piv_scipy = sl.lu_factor(a)
+    assert np.array_equal(piv_scipy, ipiv)
+    assert O.lu_reconstruction(a, lu, ipiv) <= 10.0
+
+
+def test_lu_zero_column_is_skipped_and_solve_fails():
+    a = np.array([[0.0, 1.0, 2.0], [0.0, 3.0, 4.0], [0.0, 5.0, 7.0]])
+    lu, ipiv, _ = O.lu(a)
+    assert ipiv[0] == 0 and lu[0, 0] == 0.0  # lu.rs:107-110
+    assert O.lu_solve(lu, ipiv, np.ones(3)) is None
+
+
+@pytest.mark.parametrize("n", [1, 2, 8, 20, 37])
+def test_cholesky_properties(n):
+    """tests/linalg/cholesky.rs:35-77 and the log-determinant."""
+    rng = np.random.default_rng(200 + n)
+    b = rng.standard_normal((n, n))
+    a = b @ b.T + n * np.eye(n)
+    l, info = O.cholesky(a)
+    assert info == 0
+    L = np.tril(l)
+    assert np.allclose(L @ L.T, a, atol=1e-7 * np.abs(a).max())
+    assert np.array_equal(np.triu(l, 1), np.triu(a, 1))  # upper triangle untouched
+    rhs = rng.standard_normal((n, 4))
+    x = O.cholesky_solve(l, rhs)
+    assert np.allclose(a @ x, rhs, atol=1e-7 * max(1, np.abs(rhs).max()))
+    assert O.backward_error(a, x, rhs) <= n * EPS64
+    assert abs(O.cholesky_ln_determinant(l) - np.linalg.slogdet(a)[1]) <= 1e-12 * max(1, abs(np.linalg.slogdet(a)[1]))
+    assert np.allclose(L, np.linalg.cholesky(a), rtol=1e-12, atol=1e-12)
+
+
+def test_cholesky_not_spd():
+    a = np.array([[1.0, 2.0], [2.0, 1.0]])
+    _, info = O.cholesky(a)
+    assert info == 2
+    _, info = O.cholesky(np.array([[-1.0]]))
+    assert info == 1
+    _, info = O.cholesky(np.array([[np.nan]]))
+    assert info == 1
+
+
+@pytest.mark.parametrize("m,n", [(3, 3), (5, 3), (3, 5), (40, 7), (300, 64)])
+def test_qr_properties(m, n):
+    """tests/linalg/qr.rs:15-52: Q R = A and Q orthogonal within 1e-7."""
+    rng = np.random.default_rng(300 + m + n)
+    a = rng.uniform(-100, 100, size=(m, n))
+    qr, diag = O.qr(a)
+    r = O.qr_r(qr, diag)
+    qt = O.qr_q_tr_mul(qr, diag, np.eye(m))  # Q^T
+    q = qt.T[:, : min(m, n)]
+    assert np.allclose(q @ r, a, atol=1e-7 * np.abs(a).max())
+    assert np.allclose(q.T @ q, np.eye(min(m, n)), atol=1e-7)
+    assert np.all(np.diag(r) >= 0)
+
+
+@pytest.mark.parametrize("m,n", [(5, 3), (20, 20), (128, 64), (512, 64)])
+def test_qr_least_squares_normal_equations(m, n):
+    """nalgebra-lapack/tests/linalg/qr.rs:46-61: A^T A x = A^T b within 1e-5."""
+    rng = np.random.default_rng(400 + m)
+    a = rng.standard_normal((m, n))
+    b = rng.standard_normal(m)
+    qr, diag = O.qr(a)
+    x, info = O.qr_ls_solve(qr, diag, b)
+    assert info == 0
+    x = x[:, 0]
+    assert np.allclose(a.T @ a @ x, a.T @ b, atol=1e-5)
+    assert np.allclose(x, np.linalg.lstsq(a, b, rcond=None)[0], atol=1e-10)
+
+
+def test_qr_rank_deficient_reports_info():
+    a = np.zeros((6, 3))
+    a[:, 0] = 1.0
+    qr, diag = O.qr(a)
+    _, info = O.qr_ls_solve(qr, diag, np.ones(6))
+    assert info > 0
+
+
+def test_gemm_dot2_is_accurate():
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((30, 40)) * 2.0 ** rng.integers(-20, 21, size=(30, 1))
+    b = rng.standard_normal((40, 20)) * 2.0 ** rng.integers(-20, 21, size=(1, 20))
+    c = O.gemm_dot2(1.0, a, b)
+    from fractions import Fraction
+
+    i, j = 7, 11
+    exact = sum(Fraction(a[i, k]) * Fraction(b[k, j]) for k in range(40))
+    assert abs(Fraction(c[i, j]) - exact) <= abs(exact) * Fraction(2 * EPS64)
+    c2 = O.gemm_dot2(2.0, a, b, beta=-1.0, c=np.ones((30, 20)))
+    assert np.allclose(c2, 2 * (a @ b) - 1, rtol=1e-12, atol=1e-6)
+
+
+def test_golden_fixtures_reproduce():
+    """The committed oracle fixtures (tests/golden/make_golden.py) are
+    reproduced bit for bit by the oracle built here."""
+    from tests.golden.make_golden import make
+
+    fresh = make()
+    with np.load(os.path.join(GOLD, "oracle_small.npz")) as z:
+        for key in z.files:
+            ref = z[key]
+            got = fresh[key]
+            if key.endswith("logdet"):
+                assert np.allclose(got, ref, rtol=1e-14, atol=0), key
+            else:
+                assert np.array_equal(got, ref, equal_nan=True), key
