@@ -149,6 +149,8 @@ def bench_ragged_ours(args, rank, world):
     L = _lib.load()
     dev = torch.device("cuda", torch.cuda.current_device())
     cfg = dict(RAGGED)
+    if args.count:
+        cfg["count"] = args.count
     w = W.ragged_spd_torch(cfg["count"], cfg["n_lo"], cfg["n_hi"], cfg["nrhs"], seed=cfg["seed"] + rank, device=dev)
     ns, aoff, boff, nrhs = w["ns"], w["a_offsets"], w["b_offsets"], cfg["nrhs"]
     count = ns.size
@@ -190,6 +192,8 @@ def bench_ragged_ours(args, rank, world):
         torch.distributed.barrier()
     times = [e0.elapsed_time(e1) for e0, e1 in ev]
     kern_ms = float(np.mean(times))
+    if args.profile:
+        return {"workload": "ragged_cholesky", "count": count, "ms_per_step": kern_ms}, None
     info = chol.info.cpu().numpy()
     if np.any(info != 0):
         raise RuntimeError(f"{int(np.sum(info != 0))} systems failed to factor")
@@ -419,6 +423,8 @@ def main():
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--count", type=int, default=0, help="ragged_cholesky: override the number of systems")
+    ap.add_argument("--profile", action="store_true", help="timed kernel only (for ncu captures)")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -449,6 +455,9 @@ def main():
         return
 
     res, data = bench_ragged_ours(args, rank, world)
+    if args.profile:
+        print(json.dumps(res))
+        return
     if world > 1:
         t = torch.tensor([res["ms_per_step"]], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)

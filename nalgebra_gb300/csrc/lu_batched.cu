@@ -28,7 +28,7 @@ namespace {
 constexpr int kLuThreads = 128;
 
 template <typename T, bool EXACT>
-__device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_info, bool factor) {
+__device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_info, T* s_rcp, bool factor) {
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
   const int ncols = n + nrhs;
@@ -47,7 +47,11 @@ __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_inf
           }
         }
         warp_argmax(key, idx);
-        if (tid == 0) s_piv[i] = idx;
+        if (tid == 0) {
+          s_piv[i] = idx;
+          const T d = coli[idx];
+          s_rcp[0] = (d == T(0)) ? T(0) : T(1) / d;  // one division per step, not per thread
+        }
       }
       __syncthreads();
       const int piv = s_piv[i];
@@ -57,7 +61,7 @@ __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_inf
         __syncthreads();
         continue;
       }
-      const T inv_diag = T(1) / diag;
+      const T inv_diag = s_rcp[0];
       // Swap rows i and piv in every column but i (L part, U part and the
       // right-hand sides), and rewrite column i as [diag; coeffs * inv_diag].
       if (piv != i) {
@@ -150,12 +154,19 @@ __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_inf
   if (nrhs == 0 || *s_info != 0) return;
   // Back substitution (solve.rs:155-182), one warp per right-hand side:
   // coeff = b[i] / U_ii (true division), then b[0..i] += (-coeff) * U[0..i][i].
+  if constexpr (!EXACT) {
+    for (int i = tid; i < n; i += nthr) s_rcp[1 + i] = T(1) / sa[(size_t)i * ld + i];
+    __syncthreads();
+  }
   const int warp = tid >> 5, lane = tid & 31;
   for (int c = warp; c < nrhs; c += (nthr >> 5)) {
     T* bcol = sa + (size_t)(n + c) * ld;
     for (int i = n - 1; i >= 0; --i) {
       const T* ucol = sa + (size_t)i * ld;
-      if (lane == 0) bcol[i] = bcol[i] / ucol[i];
+      if (lane == 0) {
+        if constexpr (EXACT) bcol[i] = bcol[i] / ucol[i];
+        else bcol[i] = bcol[i] * s_rcp[1 + i];
+      }
       __syncwarp();
       const T coeff = bcol[i];
       for (int r = lane; r < i; r += 32) bcol[r] = axpy1<EXACT>(bcol[r], -coeff, ucol[r]);
@@ -177,7 +188,8 @@ __global__ void __launch_bounds__(kLuThreads) lu_batched_kernel(int n, int nrhs,
   const int ld = n | 1;
   const int ncols = n + nrhs;
   T* sa = reinterpret_cast<T*>(smem_raw);
-  int* s_piv = reinterpret_cast<int*>(sa + (size_t)ld * ncols);
+  T* s_rcp = sa + (size_t)ld * ncols;  // [0]: 1/pivot of the current step; [1+i]: 1/U_ii
+  int* s_piv = reinterpret_cast<int*>(s_rcp + n + 1);
   int* s_info = s_piv + n;
   const int tid = threadIdx.x;
   for (int s = blockIdx.x; s < batch; s += gridDim.x) {
@@ -196,7 +208,7 @@ __global__ void __launch_bounds__(kLuThreads) lu_batched_kernel(int n, int nrhs,
     if (mode == 2)
       for (int i = tid; i < n; i += blockDim.x) s_piv[i] = ipiv[(size_t)s * n + i];
     __syncthreads();
-    lu_system<T, EXACT>(n, nrhs, ld, sa, s_piv, s_info, mode != 2);
+    lu_system<T, EXACT>(n, nrhs, ld, sa, s_piv, s_info, s_rcp, mode != 2);
     if (mode != 2) {
       if (write_factors) {
         T* aw = A + (size_t)s * strideA;
@@ -222,7 +234,7 @@ __global__ void __launch_bounds__(kLuThreads) lu_batched_kernel(int n, int nrhs,
 template <typename T>
 size_t lu_smem_bytes(int n, int nrhs) {
   const int ld = n | 1;
-  return (size_t)ld * (n + nrhs) * sizeof(T) + (size_t)(n + 1) * sizeof(int);
+  return (size_t)ld * (n + nrhs) * sizeof(T) + (size_t)(n + 1) * sizeof(T) + (size_t)(n + 1) * sizeof(int);
 }
 
 template <typename T>
