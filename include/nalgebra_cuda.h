@@ -139,6 +139,25 @@ int nacu_dpotrs_ragged(int count, int n_max, const int32_t* ns, const int64_t* a
 int nacu_dposv(int n, double* A, int nrhs, double* B, int32_t* info, double* logdet, double substitute,
                int flags, nacu_stream_t stream);
 
+/* Largest batch nacu_dposv_ragged_noalloc accepts. */
+#define NACU_RAGGED_NOALLOC_MAX_COUNT 65536
+
+/* nacu_dposv_ragged without any caller scratch, for hosts that cannot
+ * allocate device memory when they solve (allocator callbacks, real-time or
+ * certified hosts that allocate only at start-up, plugins whose framework owns
+ * every allocation).  No counterpart in nalgebra: it exists for callers of
+ * this library.  Scratch (the work-queue head and the largest-first order) is
+ * a fixed 256 KiB array inside the library's device image, held on every GPU
+ * that loads the library until the process exits.  count <= 65536, else the
+ * call returns -1 with a message.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls share the one array: calls that overlap on
+ * the GPU race on it and must be ordered by the caller.  Arguments and results
+ * are those of nacu_dposv_ragged; allocates nothing. */
+int nacu_dposv_ragged_noalloc(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, double* A,
+                              int nrhs, const int64_t* b_offsets, double* B, int32_t* info, double* logdet,
+                              double substitute, int flags, nacu_stream_t stream);
+
 /* ---- measurement helpers ---------------------------------------------------- */
 
 /* FP64 FMA throughput probe: runs a fixed DFMA-chain kernel over the whole GPU

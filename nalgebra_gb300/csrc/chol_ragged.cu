@@ -566,3 +566,118 @@ int nacu_dposv(int n, double* A, int nrhs, double* B, int32_t* info, double* log
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of nacu_dposv_ragged.
+//
+// Some callers cannot allocate device memory at the point where they solve:
+// code running inside a custom allocator or memory-pool callback, real-time or
+// safety-certified hosts that forbid allocation after start-up, and plugins
+// whose host framework owns every device allocation and hands out no scratch.
+// For them this entry point keeps its scratch -- the work-queue head and the
+// largest-first processing order -- in a fixed array in the library's own
+// device memory (loaded with the module; every GPU that loads the library
+// holds it until the process exits).  The caller still passes all inputs and
+// outputs.  Calls share that one array, so two calls that overlap on the GPU
+// (different streams, no ordering between them) race on it; order such calls.
+// ---------------------------------------------------------------------------
+namespace nacu {
+namespace {
+
+constexpr int kNoAllocMaxCount = NACU_RAGGED_NOALLOC_MAX_COUNT;
+
+// [0]: work-queue head; [1 .. count]: processing order.
+static __device__ __align__(256) int32_t g_ragged_noalloc_scratch[1 + kNoAllocMaxCount];
+
+int32_t* g_noalloc_scratch_ptr[64] = {nullptr};
+
+// Builds the largest-first order (a counting sort on n, one CTA) into the
+// scratch and clears the queue head, so every call starts from zero.
+__global__ void __launch_bounds__(1024) ragged_order_kernel(int count, int n_max, const int32_t* __restrict__ ns,
+                                                            int32_t* __restrict__ scratch) {
+  __shared__ int hist[NACU_CHOL_RAGGED_MAX_N + 2];
+  const int nb = n_max + 1;
+  for (int i = threadIdx.x; i <= nb; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (int s = threadIdx.x; s < count; s += blockDim.x) {
+    int n = ns[s];
+    n = (n < 0 || n > n_max) ? 0 : n;  // out-of-range orders still get a slot (info = -1 later)
+    atomicAdd(&hist[n], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // exclusive prefix sum over n, largest n first
+    int run = 0;
+    for (int n = n_max; n >= 0; --n) {
+      const int h = hist[n];
+      hist[n] = run;
+      run += h;
+    }
+    scratch[0] = 0;
+  }
+  __syncthreads();
+  for (int s = threadIdx.x; s < count; s += blockDim.x) {
+    int n = ns[s];
+    n = (n < 0 || n > n_max) ? 0 : n;
+    scratch[1 + atomicAdd(&hist[n], 1)] = s;
+  }
+}
+
+// Device address of the scratch array for the current device, looked up once
+// per device (the array's host-side name is not a device address).
+int noalloc_scratch(int32_t** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return record_cuda_error(e, "nacu_dposv_ragged_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= 64) return record_arg_error(-99, "nacu_dposv_ragged_noalloc: device index >= 64");
+  if (g_noalloc_scratch_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_ragged_noalloc_scratch);
+    if (e != cudaSuccess) return record_cuda_error(e, "nacu_dposv_ragged_noalloc: cudaGetSymbolAddress");
+    g_noalloc_scratch_ptr[dev] = static_cast<int32_t*>(p);
+  }
+  *out = g_noalloc_scratch_ptr[dev];
+  return NACU_SUCCESS;
+}
+
+}  // namespace
+}  // namespace nacu
+
+extern "C" int nacu_dposv_ragged_noalloc(int count, int n_max, const int32_t* ns, const int64_t* a_offsets,
+                                         double* A, int nrhs, const int64_t* b_offsets, double* B, int32_t* info,
+                                         double* logdet, double substitute, int flags, nacu_stream_t stream) {
+  using namespace nacu;
+  if (count < 0) return record_arg_error(-1, "dposv_ragged_noalloc: negative count");
+  if (count > kNoAllocMaxCount)
+    return record_arg_error(-1, "dposv_ragged_noalloc: count exceeds NACU_RAGGED_NOALLOC_MAX_COUNT (65536); "
+                                "use nacu_dposv_ragged with a caller workspace or split the batch");
+  if (n_max < 0 || n_max > NACU_CHOL_RAGGED_MAX_N)
+    return record_arg_error(-2, "dposv_ragged_noalloc: n_max out of range [0, 512]");
+  if (count == 0) return NACU_SUCCESS;
+  if (!ns || !a_offsets || !A) return record_arg_error(-3, "dposv_ragged_noalloc: null ns, a_offsets or A");
+  if (nrhs < 0) return record_arg_error(-6, "dposv_ragged_noalloc: negative nrhs");
+  if (nrhs > 0 && (!b_offsets || !B)) return record_arg_error(-7, "dposv_ragged_noalloc: null b_offsets or B");
+  if (!info) return record_arg_error(-9, "dposv_ragged_noalloc: null info");
+  int32_t* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc != NACU_SUCCESS) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  ragged_order_kernel<<<1, 1024, 0, s>>>(count, n_max, ns, scratch);
+  rc = check_launch("nacu_dposv_ragged_noalloc: order");
+  if (rc != NACU_SUCCESS) return rc;
+  CholArgs g{count, n_max, ns, a_offsets, A, nrhs, b_offsets, B, info, logdet, scratch + 1, scratch,
+             (flags & NACU_FLAG_SUBSTITUTE) ? 1 : 0, substitute, 1};
+  // The queue head was cleared by the order kernel (same stream, in order).
+  const bool exact = (flags & NACU_FLAG_EXACT) != 0;
+  auto kern = exact ? chol_ragged_kernel<true> : chol_ragged_kernel<false>;
+  const size_t smem = chol_smem_bytes(g.n_max);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return record_cuda_error(e, "nacu_dposv_ragged_noalloc");
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCholThreads, smem);
+  if (e != cudaSuccess) return record_cuda_error(e, "nacu_dposv_ragged_noalloc");
+  if (per_sm < 1) per_sm = 1;
+  int grid = sm_count() * per_sm;
+  if (grid > count) grid = count;
+  kern<<<grid, kCholThreads, smem, s>>>(g);
+  return check_launch("nacu_dposv_ragged_noalloc");
+}
