@@ -412,6 +412,64 @@ def bench_lu_ours(args, rank, world):
             "gpu_launches": args.steps, "clocks": clk.summary()}
 
 
+# ----------------------------------------------------------------------------- QR least squares
+
+def bench_ls_ours(args, rank, world):
+    import torch
+
+    from nalgebra_gb300 import _lib
+    from nalgebra_gb300 import workloads as W
+
+    L = _lib.load()
+    count = args.count or 8192
+    n = 64
+    w = W.ragged_ls(count, 128, 512, n, seed=rank)
+    ms = w["ms"]
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    a0, b0 = d(w["a_flat"]), d(w["b_flat"])
+    A, B = a0.clone(), b0.clone()
+    dms, daoff, dboff = d(ms), d(w["a_offsets"]), d(w["b_offsets"])
+    X = torch.zeros(count * n, dtype=torch.float64, device="cuda")
+    diag = torch.zeros(count * n, dtype=torch.float64, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    ws = torch.zeros(L.nacu_qr_workspace_bytes(count), dtype=torch.uint8, device="cuda")
+    order = d(np.argsort(-ms, kind="stable").astype(np.int32))
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+
+    def launch():
+        _lib.call("nacu_dgels_batched", count, n, int(ms.max()), dms.data_ptr(), daoff.data_ptr(), A.data_ptr(),
+                  dboff.data_ptr(), B.data_ptr(), X.data_ptr(), diag.data_ptr(), info.data_ptr(),
+                  order.data_ptr(), ws.data_ptr(), ws.numel(), 0, sp)
+
+    for _ in range(args.warmup):
+        A.copy_(a0); B.copy_(b0); launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            A.copy_(a0); B.copy_(b0)
+            ev[i][0].record(stream)
+            launch()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    ms_step = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+    m = ms.astype(np.float64)
+    flops = float(np.sum(2 * m * n * n - 2.0 * n ** 3 / 3 + 4 * m * n + n * n))
+    peak = ctypes_probe(L)
+    if np.any(info.cpu().numpy() != 0):
+        raise RuntimeError("rank-deficient problems in the LS workload")
+    return {"metric": "solves/s (batched Householder QR least squares, 8192 x m in [128,512] x 64 f64)",
+            "value": count / (ms_step * 1e-3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "ls_qr", "count": count, "m_range": [128, 512], "n": n},
+            "gflops": flops / (ms_step * 1e-3) / 1e9,
+            "roofline": {"bound": "fp64", "achieved": flops / (ms_step * 1e-3) / 1e12, "peak": peak / 1e12,
+                         "unit": "TFLOP/s", "frac": flops / (ms_step * 1e-3) / peak, "traffic": None},
+            "gpu_launches": args.steps, "clocks": clk.summary()}
+
+
 # ----------------------------------------------------------------------------- main
 
 def main():
@@ -420,7 +478,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched"])
+    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=0, help="ragged_cholesky: override the number of systems")
@@ -448,8 +506,8 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
-    if args.workload == "lu_batched":
-        res = bench_lu_ours(args, rank, world)
+    if args.workload in ("lu_batched", "ls_qr"):
+        res = (bench_lu_ours if args.workload == "lu_batched" else bench_ls_ours)(args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

@@ -66,6 +66,8 @@ typedef void* nacu_stream_t;
 #define NACU_LU_BATCHED_MAX_N 128
 #define NACU_LU_BATCHED_MAX_NRHS 16
 #define NACU_CHOL_RAGGED_MAX_N 512
+#define NACU_QR_MAX_N 64
+#define NACU_QR_MAX_M 2048
 
 /* ---- library ------------------------------------------------------------- */
 
@@ -138,6 +140,28 @@ int nacu_dpotrs_ragged(int count, int n_max, const int32_t* ns, const int64_t* a
  * `.ln_determinant()` for an n x n SPD matrix (n <= 512). */
 int nacu_dposv(int n, double* A, int nrhs, double* B, int32_t* info, double* logdet, double substitute,
                int flags, nacu_stream_t stream);
+
+/* ---- Householder QR and least squares (batched, tall-skinny) ------------- */
+
+/* Bytes of device scratch nacu_dgels_batched needs (the work-queue head). */
+size_t nacu_qr_workspace_bytes(int count);
+
+/* Householder QR of `count` tall matrices with n <= 64 columns and
+ * ms[s] >= n rows (ms[s] <= m_max <= 2048), A + a_offsets[s] (lda = ms[s]),
+ * factored in place into nalgebra's QR layout: unit reflection axes on and
+ * below the diagonal, R strictly above it, and diag[s*n + i] = the signed
+ * diagonal (R_ii = |diag_i|), exactly nalgebra's sign convention
+ * (src/linalg/qr.rs:55-76, householder.rs:19-85, reflection.rs:70-83).
+ * With b_offsets/B set, each B + b_offsets[s] (ms[s] x 1) is replaced by
+ * Q^T b (qr.rs:157-171) and X + s*n receives the least-squares solution
+ * argmin ||A x - b|| (R[0:n,0:n] x = (Q^T b)[0:n], as
+ * nalgebra-lapack/src/qr_util.rs:167-239).  info[s] (nullable): 0 ok,
+ * k = first zero R_kk (rank deficient), -1 = ms[s] out of range.
+ * NACU_FLAG_EXACT is not available for QR (returns -15). */
+int nacu_dgels_batched(int count, int n, int m_max, const int32_t* ms, const int64_t* a_offsets, double* A,
+                       const int64_t* b_offsets, double* B, double* X, double* diag, int32_t* info,
+                       const int32_t* order, void* workspace, size_t workspace_bytes, int flags,
+                       nacu_stream_t stream);
 
 /* Largest batch nacu_dposv_ragged_noalloc accepts. */
 #define NACU_RAGGED_NOALLOC_MAX_COUNT 65536

@@ -33,7 +33,7 @@ from . import _lib
 from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 
 __all__ = [
-    "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch",
+    "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch",
     "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE",
 ]
 
@@ -243,6 +243,9 @@ class DeviceBatch:
     def cholesky(self, flags: int = 0, substitute: float | None = None) -> "CholeskyBatch":
         return CholeskyBatch(self, flags, substitute)
 
+    def qr(self) -> "QRBatch":
+        return QRBatch(self)
+
 
 class LUBatch:
     """Batched LU of equal-order square matrices (n <= 128).  Lazy: the first
@@ -355,3 +358,66 @@ class CholeskyBatch:
         """Per matrix: True where nalgebra's ``cholesky()`` returns Some."""
         self.factor()
         return self.info.cpu().numpy() == 0
+
+
+class QRBatch:
+    """Batched Householder QR of tall matrices (equal column count n <= 64,
+    ragged row counts m >= n, m <= 2048), nalgebra's stored layout and sign
+    convention (src/linalg/qr.rs:55-76).  Lazy: ``solve`` runs factor + Q^T b +
+    least squares in one launch."""
+
+    def __init__(self, batch: DeviceBatch):
+        torch = _torch()
+        if len(batch) and not np.all(batch.ncols == batch.ncols[0]):
+            raise ValueError("QRBatch needs the same column count in every matrix")
+        self.batch = batch
+        self.n = int(batch.ncols[0]) if len(batch) else 0
+        if np.any(batch.nrows < self.n):
+            raise ValueError("least squares needs m >= n (nalgebra-lapack Error::Underdetermined)")
+        count = len(batch)
+        self.m_max = int(batch.nrows.max()) if count else 0
+        self.diag = torch.zeros(max(count * self.n, 1), dtype=torch.float64, device="cuda")
+        self.info = torch.zeros(max(count, 1), dtype=torch.int32, device="cuda")
+        order = np.argsort(-batch.nrows, kind="stable").astype(np.int32)
+        self._order = torch.from_numpy(order).to("cuda")
+        self._ws = torch.zeros(_lib.load().nacu_qr_workspace_bytes(count), dtype=torch.uint8, device="cuda")
+        self.factored = False
+
+    def _launch(self, rhs: "DeviceBatch | None", x):
+        b = self.batch
+        _lib.call("nacu_dgels_batched", len(b), self.n, self.m_max, b._d_rows.data_ptr(), b._d_off.data_ptr(),
+                  b.data.data_ptr(), rhs._d_off.data_ptr() if rhs is not None else 0,
+                  rhs.data.data_ptr() if rhs is not None else 0, x.data_ptr() if x is not None else 0,
+                  self.diag.data_ptr(), self.info.data_ptr(), self._order.data_ptr(), self._ws.data_ptr(),
+                  self._ws.numel(), 0, _stream_ptr())
+        self.factored = True
+
+    def factor(self) -> "QRBatch":
+        if not self.factored:
+            self._launch(None, None)
+        return self
+
+    def solve_mut(self, rhs: DeviceBatch):
+        """Least squares for one m x 1 right-hand side per matrix; rhs becomes
+        Q^T b (as QR::q_tr_mul) and the n x 1 solutions are returned as a flat
+        (count * n) device tensor.  Factor + solve run in one launch."""
+        if self.factored:
+            raise NotImplementedError("solve after a separate factor(): call solve on a fresh QRBatch")
+        if len(rhs) != len(self.batch) or np.any(rhs.nrows != self.batch.nrows) or np.any(rhs.ncols != 1):
+            raise ValueError("one m x 1 right-hand side per matrix")
+        x = _torch().zeros(max(len(self.batch) * self.n, 1), dtype=_torch().float64, device="cuda")
+        self._launch(rhs, x)
+        return x
+
+    def solve(self, rhs: DeviceBatch) -> np.ndarray:
+        """nalgebra-lapack QR::solve (nalgebra-lapack/src/qr/abstraction.rs:48-77):
+        the (count, n) least-squares solutions (host), rank-deficient rows NaN."""
+        res = rhs.clone_owned()
+        x = self.solve_mut(res).cpu().numpy()[: len(self.batch) * self.n].reshape(len(self.batch), self.n)
+        bad = self.info.cpu().numpy()[: len(self.batch)] != 0
+        x[bad] = np.nan
+        return x
+
+    def diag_host(self) -> np.ndarray:
+        self.factor()
+        return self.diag.cpu().numpy()[: len(self.batch) * self.n].reshape(len(self.batch), self.n)

@@ -42,6 +42,8 @@ SIGNATURES = {
     "nacu_dpotrs_ragged": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_dposv": (_i, [_i, _vp, _i, _vp, _vp, _vp, _d, _i, _vp]),
     "nacu_dposv_ragged_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _d, _i, _vp]),
+    "nacu_qr_workspace_bytes": (_sz, [_i]),
+    "nacu_dgels_batched": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_probe_fp64_peak": (_i, [C.POINTER(C.c_double)]),
 }
 

@@ -1,0 +1,402 @@
+// Batched Householder QR and least squares for tall-skinny systems
+// (m >= n, n <= 64): the GPU form of nalgebra's `m.qr()`
+// (src/linalg/qr.rs:55-76, householder.rs:19-85, geometry/reflection.rs:70-83),
+// `q_tr_mul` (qr.rs:157-171) and the least-squares solve of nalgebra-lapack
+// (nalgebra-lapack/src/qr_util.rs:167-239: Q^T b, then the upper-triangular
+// solve with R[0:n, 0:n], dividing by |diag_i| as qr.rs:224-256 does).
+//
+// Sign convention.  nalgebra applies each reflection with a sign,
+// c <- s_i * (I - 2 v v^T) c with s_i = signum(diag_i) (householder.rs:75-82).
+// Writing D_i for the diagonal matrix that is s_i on rows >= i and 1 above,
+// nalgebra's transform is D_{n-1} H_{n-1} ... D_0 H_0, and every D_i commutes
+// with the later H_j (H_j touches rows >= j > i, where D_i is a scalar), so it
+// equals D H_{n-1} ... H_0 with D = diag(d_r), d_r = prod_{i <= min(r, n-1)} s_i.
+// The reflections themselves do not depend on the signs (a reflection axis is
+// defined up to sign).  So the kernel runs plain Householder QR in compact-WY
+// blocks, then one sign sweep gives nalgebra's stored factors exactly:
+//   diag_i  = P_i * diag_std_i   (P_i = prod_{j<i} s_j, s_i = signum(diag_i)),
+//   axis_i  = P_i * v_i          (the stored unit axis),
+//   R[r][c] = d_r * R_std[r][c]  (strict upper part), Q^T b rows likewise,
+// and the least-squares solution does not change at all (D cancels).
+//
+// Design (GB300): FP64-pipe bound like the other solvers.  One CTA (128
+// threads) per problem; problems are pulled from a work queue (largest first).
+// The matrix stays in global memory (L2-resident while the CTA works on it);
+// each 8-column panel is factored in shared memory, then the trailing columns
+// and the right-hand side take the block reflector I - V T^T V^T, one warp per
+// column: one pass computes V^T a (8 partial dots per lane, butterfly
+// reduce-scatter), one pass applies a -= V (T^T V^T a).
+#include "common.cuh"
+
+namespace nacu {
+namespace {
+
+constexpr int kQrThreads = 128;
+constexpr int kQrNB = 8;
+constexpr int kQrMaxN = 64;
+// s_t layout: T (NB x NB) | tau (NB) | V^T V partials (4 warps x 32)
+constexpr int kTOff = 0;
+constexpr int kTauOff = kQrNB * kQrNB;
+constexpr int kGOff = kTauOff + kQrNB;            // 4 warps x 32 partials
+constexpr int kGSumOff = kGOff + 4 * 32;           // 28 reduced pairs (i < j)
+constexpr int kSTSize = kGSumOff + 32;
+
+struct QrArgs {
+  int count;
+  int n;
+  int m_max;
+  const int32_t* ms;
+  const int64_t* aoff;
+  double* A;
+  const int64_t* boff;  // nullable: factor only
+  double* B;
+  double* X;      // n per problem, nullable
+  double* diag;   // n per problem
+  int32_t* info;
+  const int32_t* order;
+  int32_t* counter;
+};
+
+// Butterfly reduce-scatter of N (a power of two <= 32) per-lane values: lane L
+// ends with the warp-wide sum of value (L mod N) in v[0]; N-1 adds per lane
+// plus log2(32/N) more, instead of N separate 5-step warp reductions.
+template <int N>
+__device__ __forceinline__ void warp_reduce_scatter(double (&v)[N]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int half = N / 2; half >= 1; half >>= 1) {
+    const bool up = (lane & half) != 0;
+#pragma unroll
+    for (int t = 0; t < half; ++t) {
+      const double keep = up ? v[t + half] : v[t];
+      const double give = up ? v[t] : v[t + half];
+      v[t] = keep + __shfl_xor_sync(0xffffffffu, give, half);
+    }
+  }
+#pragma unroll
+  for (int off = N; off < 32; off <<= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
+}
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+#pragma unroll
+  for (int w = 0; w < kQrThreads / 32; ++w) s += red[w];
+  return s;
+}
+
+// One problem.  P: panel buffer (ldp x kQrNB), V^T V and T in s_t, per-column
+// standard diagonals in s_dstd, reductions in s_red.
+__device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, double* s_dstd,
+                       double* s_red, double* s_misc) {
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int n = g.n;
+  const int m = g.ms[s];
+  if (m < n || m > g.m_max) {
+    if (tid == 0 && g.info) g.info[s] = -1;
+    return;
+  }
+  double* a = g.A + g.aoff[s];
+  double* b = g.boff ? g.B + g.boff[s] : nullptr;
+  for (int J0 = 0; J0 < n; J0 += kQrNB) {
+    const int jb = min(kQrNB, n - J0);
+    const int rows = m - J0;
+    for (int e = tid; e < rows * jb; e += kQrThreads) {
+      const int c = e / rows, r = e - c * rows;
+      P[(size_t)c * ldp + r] = a[(size_t)(J0 + c) * m + J0 + r];
+    }
+    __syncthreads();
+    // ---- panel: jb Householder steps in shared memory ----
+    for (int j = 0; j < jb; ++j) {
+      double* pj = P + (size_t)j * ldp;
+      double part = 0.0;
+      for (int r = j + tid; r < rows; r += kQrThreads) part = fma(pj[r], pj[r], part);
+      const double sq = block_sum(part, s_red);
+      if (tid == 0) {
+        // householder.rs:19-53 (reflection_axis_mut) without the sign step
+        const double nrm = sqrt(sq);
+        const double x0 = pj[j];
+        const double mod = (x0 >= 0.0) ? x0 : -x0;
+        const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;  // simba to_exp
+        const double signed_norm = sgn * nrm;
+        const double factor = (sq + mod * nrm) * 2.0;
+        if (factor != 0.0) {
+          pj[j] = x0 + signed_norm;
+          s_misc[0] = rsqrt(factor);
+          s_misc[1] = 2.0;                // tau: v is unit length
+          s_dstd[J0 + j] = -signed_norm;  // R_std[j][j]
+        } else {
+          s_misc[0] = 0.0;
+          s_misc[1] = 0.0;  // no reflection (zero column)
+          s_dstd[J0 + j] = signed_norm;
+        }
+        s_t[kTauOff + j] = s_misc[1];
+      }
+      __syncthreads();
+      const double scale = s_misc[0], tau = s_misc[1];
+      // v = x * scale; dots of v with the remaining panel columns
+      double dots[kQrNB];
+#pragma unroll
+      for (int c = 0; c < kQrNB; ++c) dots[c] = 0.0;
+      for (int r = j + tid; r < rows; r += kQrThreads) {
+        const double v = pj[r] * scale;
+        pj[r] = v;
+#pragma unroll
+        for (int c = 0; c < kQrNB; ++c)
+          if (c > j && c < jb) dots[c] = fma(v, P[(size_t)c * ldp + r], dots[c]);
+      }
+      // reduce the dots (at most 7) across the CTA
+      warp_reduce_scatter<kQrNB>(dots);
+      if (lane < kQrNB) s_red[4 + warp * kQrNB + lane] = dots[0];
+      __syncthreads();
+      double coef[kQrNB];  // -tau * (v^T P_c), zero for columns outside j+1..jb-1
+#pragma unroll
+      for (int c = 0; c < kQrNB; ++c) {
+        double d = 0.0;
+#pragma unroll
+        for (int w = 0; w < kQrThreads / 32; ++w) d += s_red[4 + w * kQrNB + c];
+        coef[c] = (c > j && c < jb) ? -tau * d : 0.0;
+      }
+      for (int r = j + tid; r < rows; r += kQrThreads) {
+        const double v = pj[r];
+#pragma unroll
+        for (int c = 0; c < kQrNB; ++c)
+          if (c > j && c < jb) P[(size_t)c * ldp + r] = fma(coef[c], v, P[(size_t)c * ldp + r]);
+      }
+      __syncthreads();
+    }
+    // ---- T (forward, columnwise): T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] V^T v_j ----
+    // G = V^T V (strict upper part), V lower trapezoidal: v_j[r] = 0 for r < j.
+    {
+      double gpart[32];  // the 28 pairs i < j, padded to 32 for the butterfly
+#pragma unroll
+      for (int k = 0; k < 32; ++k) gpart[k] = 0.0;
+      for (int r = tid; r < rows; r += kQrThreads) {
+        double v[kQrNB];
+#pragma unroll
+        for (int c = 0; c < kQrNB; ++c) v[c] = (c < jb && r >= c) ? P[(size_t)c * ldp + r] : 0.0;
+#pragma unroll
+        for (int i = 0; i < kQrNB; ++i)
+#pragma unroll
+          for (int j = i + 1; j < kQrNB; ++j) {
+            const int k = i * kQrNB - i * (i + 1) / 2 + (j - i - 1);
+            gpart[k] = fma(v[i], v[j], gpart[k]);
+          }
+      }
+      warp_reduce_scatter<32>(gpart);
+      double* gsh = s_t + kGOff;  // 28 partials per warp
+      gsh[warp * 32 + lane] = gpart[0];
+      __syncthreads();
+      // Reduce the 4 warps' partials into G (strict upper part), then thread 0
+      // runs the small T recurrence in shared memory.
+      if (tid < kQrNB * (kQrNB - 1) / 2) {
+        double acc = 0.0;
+#pragma unroll
+        for (int w = 0; w < kQrThreads / 32; ++w) acc += gsh[w * 32 + tid];
+        s_t[kGSumOff + tid] = acc;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        for (int j = 0; j < kQrNB; ++j)
+          for (int i = 0; i < kQrNB; ++i) s_t[kTOff + i * kQrNB + j] = 0.0;
+        for (int j = 0; j < jb; ++j) {
+          const double tj = s_t[kTauOff + j];
+          s_t[kTOff + j * kQrNB + j] = tj;
+          for (int i = 0; i < j; ++i) {
+            double acc = 0.0;
+            for (int l = i; l < j; ++l)
+              acc = fma(s_t[kTOff + i * kQrNB + l], s_t[kGSumOff + l * kQrNB - l * (l + 1) / 2 + (j - l - 1)], acc);
+            s_t[kTOff + i * kQrNB + j] = -tj * acc;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // ---- trailing columns and the right-hand side: c <- c - V T^T V^T c ----
+    const int ntrail = n - J0 - jb;
+    const int ncol = ntrail + (b ? 1 : 0);
+    for (int t = warp; t < ncol; t += kQrThreads / 32) {
+      double* col = (t < ntrail) ? a + (size_t)(J0 + jb + t) * m + J0 : b + J0;
+      double w[kQrNB];
+#pragma unroll
+      for (int c = 0; c < kQrNB; ++c) w[c] = 0.0;
+      for (int r = lane; r < rows; r += 32) {
+        const double x = col[r];
+#pragma unroll
+        for (int c = 0; c < kQrNB; ++c) {
+          const double v = (c < jb && r >= c) ? P[(size_t)c * ldp + r] : 0.0;
+          w[c] = fma(v, x, w[c]);
+        }
+      }
+      // butterfly reduce-scatter: lane L ends with the full sum of w[L & 7]
+      warp_reduce_scatter<kQrNB>(w);
+      // w' = T^T w: lane k (k = lane & 7) forms w'_k, then every lane gathers all
+      const int k = lane & (kQrNB - 1);
+      double wk = 0.0;
+#pragma unroll
+      for (int j = 0; j < kQrNB; ++j) {
+        const double wj = __shfl_sync(0xffffffffu, w[0], j);
+        if (j <= k) wk = fma(s_t[kTOff + j * kQrNB + k], wj, wk);
+      }
+      double wp[kQrNB];
+#pragma unroll
+      for (int j = 0; j < kQrNB; ++j) wp[j] = __shfl_sync(0xffffffffu, wk, j);
+      for (int r = lane; r < rows; r += 32) {
+        double x = col[r];
+#pragma unroll
+        for (int c = 0; c < kQrNB; ++c) {
+          const double v = (c < jb && r >= c) ? P[(size_t)c * ldp + r] : 0.0;
+          x = fma(-v, wp[c], x);
+        }
+        col[r] = x;
+      }
+    }
+    __syncthreads();
+    // ---- write the factored panel back ----
+    for (int e = tid; e < rows * jb; e += kQrThreads) {
+      const int c = e / rows, r = e - c * rows;
+      a[(size_t)(J0 + c) * m + J0 + r] = P[(size_t)c * ldp + r];
+    }
+    __syncthreads();
+  }
+  // ---- sign sweep (nalgebra's reflect_with_sign convention) ----
+  // s_misc[2 + i] = P_i (axis sign), s_misc[2 + 64 + i] = d_i (row sign).
+  if (tid == 0) {
+    double pi = 1.0;
+    int inf = 0;
+    for (int i = 0; i < n; ++i) {
+      const double di = pi * s_dstd[i];
+      const double si = signbit(di) ? -1.0 : 1.0;  // Rust f64::signum (diag is never NaN here unless input is)
+      s_misc[2 + i] = pi;
+      pi *= si;
+      s_misc[2 + kQrMaxN + i] = pi;
+      s_dstd[i] = di;
+      if (di == 0.0 && inf == 0) inf = i + 1;
+    }
+    s_misc[1] = (double)inf;
+  }
+  __syncthreads();
+  const int inf = (int)s_misc[1];
+  // |diag_i|^-1 for the back substitution (computed in parallel, once).
+  for (int i = tid; i < n; i += kQrThreads) s_t[kGOff + i] = 1.0 / fabs(s_dstd[i]);
+  __syncthreads();
+  // The least-squares solution.  With R_nal = D R_std and (Q^T b)_nal = D (Q^T b)_std
+  // the signs cancel; the solve uses nalgebra's R (rows scaled by d_r, diagonal
+  // |diag_i|) exactly as qr.rs:224-256 restricted to the top n rows.
+  if (b && g.X && inf == 0 && warp == 0) {
+    double* x = g.X + (size_t)s * n;
+    double yv[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int r = lane + 32 * k;
+      yv[k] = (r < n) ? b[r] * s_misc[2 + kQrMaxN + r] : 0.0;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      const double yi = __shfl_sync(0xffffffffu, (i < 32) ? yv[0] : yv[1], i & 31);
+      const double xi = yi * s_t[kGOff + i];
+      if (lane == (i & 31)) {
+        if (i < 32) yv[0] = xi;
+        else yv[1] = xi;
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int r = lane + 32 * k;
+        if (r < i) yv[k] = fma(-xi, a[(size_t)i * m + r] * s_misc[2 + kQrMaxN + r], yv[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int r = lane + 32 * k;
+      if (r < n) x[r] = yv[k];
+    }
+  }
+  __syncthreads();
+  // Apply the signs (+-1: a sign-bit flip, no FP64 work) to the stored
+  // factors and to Q^T b.
+  for (int e = tid; e < m * n; e += kQrThreads) {
+    const int c = e / m, r = e - c * m;
+    double* p = a + (size_t)c * m + r;
+    const double f = (r >= c) ? s_misc[2 + c] : s_misc[2 + kQrMaxN + r];  // axis_c *= P_c, R[r][c] *= d_r
+    const unsigned long long mask = (unsigned long long)__double_as_longlong(f) & 0x8000000000000000ull;
+    *p = __longlong_as_double(__double_as_longlong(*p) ^ mask);
+  }
+  if (b)
+    for (int r = tid; r < m; r += kQrThreads) {
+      const double f = s_misc[2 + kQrMaxN + min(r, n - 1)];
+      const unsigned long long mask = (unsigned long long)__double_as_longlong(f) & 0x8000000000000000ull;
+      b[r] = __longlong_as_double(__double_as_longlong(b[r]) ^ mask);
+    }
+  for (int i = tid; i < n; i += kQrThreads) g.diag[(size_t)s * n + i] = s_dstd[i];
+  if (tid == 0 && g.info) g.info[s] = inf;
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kQrThreads, 4) qr_batched_kernel(QrArgs g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double s_t[kSTSize];
+  __shared__ double s_dstd[kQrMaxN];
+  __shared__ double s_red[4 + 4 * kQrNB];
+  __shared__ double s_misc[2 + 2 * kQrMaxN];
+  __shared__ int s_item;
+  const int ldp = g.m_max | 1;
+  double* P = reinterpret_cast<double*>(smem_raw);
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1);
+    __syncthreads();
+    const int idx = s_item;
+    __syncthreads();
+    if (idx >= g.count) break;
+    const int s = g.order ? g.order[idx] : idx;
+    qr_one(g, s, P, ldp, s_t, s_dstd, s_red, s_misc);
+  }
+}
+
+}  // namespace
+}  // namespace nacu
+
+extern "C" {
+
+size_t nacu_qr_workspace_bytes(int count) {
+  (void)count;
+  return 256;
+}
+
+int nacu_dgels_batched(int count, int n, int m_max, const int32_t* ms, const int64_t* a_offsets, double* A,
+                       const int64_t* b_offsets, double* B, double* X, double* diag, int32_t* info,
+                       const int32_t* order, void* workspace, size_t workspace_bytes, int flags,
+                       nacu_stream_t stream) {
+  using namespace nacu;
+  if (count < 0) return record_arg_error(-1, "dgels_batched: negative count");
+  if (n < 1 || n > kQrMaxN) return record_arg_error(-2, "dgels_batched: n out of range [1, 64]");
+  if (m_max < n || m_max > NACU_QR_MAX_M) return record_arg_error(-3, "dgels_batched: m_max out of range [n, 2048]");
+  if (count == 0) return NACU_SUCCESS;
+  if (!ms || !a_offsets || !A) return record_arg_error(-4, "dgels_batched: null ms, a_offsets or A");
+  if ((b_offsets == nullptr) != (B == nullptr)) return record_arg_error(-7, "dgels_batched: b_offsets and B must both be set or both null");
+  if (!diag) return record_arg_error(-10, "dgels_batched: null diag");
+  if (!workspace || workspace_bytes < nacu_qr_workspace_bytes(count))
+    return record_arg_error(-14, "dgels_batched: workspace too small");
+  if (flags & NACU_FLAG_EXACT) return record_arg_error(-15, "dgels_batched: NACU_FLAG_EXACT is not available for QR");
+  QrArgs g{count, n, m_max, ms, a_offsets, A, b_offsets, B, X, diag, info, order,
+           reinterpret_cast<int32_t*>(workspace)};
+  const size_t smem = (size_t)(m_max | 1) * kQrNB * sizeof(double);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaFuncSetAttribute(qr_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgels_batched");
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_batched_kernel, kQrThreads, smem);
+  if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgels_batched");
+  if (per_sm < 1) per_sm = 1;
+  int grid = sm_count() * per_sm;
+  if (grid > count) grid = count;
+  e = cudaMemsetAsync(workspace, 0, sizeof(int32_t), s);
+  if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgels_batched");
+  qr_batched_kernel<<<grid, kQrThreads, smem, s>>>(g);
+  return check_launch("nacu_dgels_batched");
+}
+
+}  // extern "C"

@@ -85,3 +85,17 @@ def ragged_spd_torch(count: int, n_lo: int, n_hi: int, nrhs: int = 4, seed: int 
             ar = torch.arange(n * n, device=device)
             a_flat[(dst[:, None] + ar[None, :]).reshape(-1)] = A.reshape(-1)
     return dict(ns=ns, a_offsets=aoff, a_flat=a_flat, b_offsets=boff, b_flat=b_flat, nrhs=nrhs)
+
+
+def ragged_ls(count: int, m_lo: int, m_hi: int, n: int = 64, seed: int = 0):
+    """Tall-skinny least-squares problems: m ~ U{m_lo..m_hi} rows, n columns,
+    A and b iid N(0,1), column-major.  Returns dict with ms, a_offsets, a_flat,
+    b_offsets, b_flat, n."""
+    rng = np.random.default_rng(seed)
+    ms = rng.integers(m_lo, m_hi + 1, size=count).astype(np.int32)
+    sizes = ms.astype(np.int64) * n
+    aoff = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    boff = np.concatenate([[0], np.cumsum(ms.astype(np.int64))[:-1]]).astype(np.int64)
+    a_flat = rng.standard_normal(int(sizes.sum()))
+    b_flat = rng.standard_normal(int(ms.astype(np.int64).sum()))
+    return dict(ms=ms, a_offsets=aoff, a_flat=a_flat, b_offsets=boff, b_flat=b_flat, n=n)

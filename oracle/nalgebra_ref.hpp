@@ -342,12 +342,15 @@ inline void qr_q_tr_mul(std::size_t m, std::size_t n, const T* qr, std::size_t l
 // |diag_i|, axpy with the strict upper part of R) restricted to the top n rows,
 // as nalgebra-lapack's qr_solve_mut_with_rank_unpermuted (qr_util.rs:167-239)
 // restricts dtrtrs to R[0:n, 0:n].  b (m x nrhs) is overwritten by Q^T b; x
-// (n x nrhs) receives the solution.  Returns 0, or i + 1 for the first (from the
-// bottom) zero |diag_i| (rank deficient, LAPACK trtrs info > 0).
+// (n x nrhs) receives the solution.  Returns 0, or i + 1 for the first zero
+// |diag_i| (rank deficient, LAPACK trtrs info > 0).
 template <class T>
 inline int qr_ls_solve(std::size_t m, std::size_t n, const T* qr, std::size_t lda, const T* diag,
                        T* b, std::size_t ldb, T* x, std::size_t ldx, std::size_t nrhs) {
   qr_q_tr_mul(m, n, qr, lda, diag, b, ldb, nrhs);
+  // LAPACK trtrs reports the first zero diagonal from the top (info > 0).
+  for (std::size_t i = 0; i < n; ++i)
+    if (std::fabs(diag[i]) == T(0)) return (int)i + 1;
   for (std::size_t c = 0; c < nrhs; ++c) {
     T* xc = x + c * ldx;
     for (std::size_t r = 0; r < n; ++r) xc[r] = b[r + c * ldb];
