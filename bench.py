@@ -255,6 +255,9 @@ def bench_ragged_ours(args, rank, world):
     plain_solves_per_s = plain_sample.size / (plain_ms * 1e-3)
     plain_flops = ragged_flops(ns[plain_sample], nrhs) / (plain_ms * 1e-3)
 
+    # precision form: FP32 factor + FP64 refinement, same inputs, one launch
+    mixed = bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host)
+
     peak = ctypes_probe(L)
     flops = ragged_flops(ns, nrhs)
     achieved = flops / (kern_ms * 1e-3)
@@ -282,6 +285,7 @@ def bench_ragged_ours(args, rank, world):
             "batched_persistent_fp64": {"solves_per_s": value / world, "gflops": achieved / 1e9},
             "plain_fp64_launch_per_matrix": {"solves_per_s": plain_solves_per_s, "gflops": plain_flops / 1e9,
                                              "sample": int(plain_sample.size)},
+            "batched_mixed_fp32_factor_fp64_refined": mixed,
         },
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
@@ -294,6 +298,49 @@ def bench_ragged_ours(args, rank, world):
         "clocks": clk.summary(),
     }
     return res, dict(ns=ns, aoff=aoff, boff=boff, a_host=a_host, b_host=b_host, nrhs=nrhs)
+
+
+def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host):
+    import torch
+
+    from nalgebra_gb300 import _lib
+
+    count = ns.size
+    sp = int(stream.cuda_stream)
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    dns, daoff, dboff = d(ns.astype(np.int32)), d(aoff), d(boff)
+    order = d(np.argsort(-ns, kind="stable").astype(np.int32))
+    X = torch.zeros_like(b0)
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    iters = torch.zeros(count, dtype=torch.int32, device="cuda")
+    total = int(a0.numel())
+    ws = torch.empty(L.nacu_mixed_workspace_bytes(total), dtype=torch.uint8, device="cuda")
+
+    def launch():
+        _lib.call("nacu_dposv_ragged_mixed", count, int(ns.max()), dns.data_ptr(), daoff.data_ptr(), a0.data_ptr(),
+                  nrhs, dboff.data_ptr(), b0.data_ptr(), X.data_ptr(), info.data_ptr(), iters.data_ptr(),
+                  order.data_ptr(), total, ws.data_ptr(), ws.numel(), 0.0, 0, 0.0, 0, sp)
+
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        launch()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+    it = iters.cpu().numpy()
+    if np.any(info.cpu().numpy() != 0):
+        raise RuntimeError("mixed form: systems reported not SPD")
+    rng = np.random.default_rng(2)
+    sample = rng.choice(count, size=min(48, count), replace=False)
+    berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, X.cpu().numpy(), nrhs, sample)
+    return {"solves_per_s": count / (ms * 1e-3), "ms_per_step": ms,
+            "gflops_fp64_equivalent": ragged_flops(ns, nrhs) / (ms * 1e-3) / 1e9,
+            "residuals_per_system_mean": float(np.mean(np.abs(it))), "fp64_fallbacks": int(np.sum(it < 0)),
+            "backward_error_max_over_sample_in_n_eps": berr}
 
 
 def ctypes_probe(L):

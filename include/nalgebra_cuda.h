@@ -62,6 +62,10 @@ typedef void* nacu_stream_t;
 /* Cholesky: replace a failing pivot by the `substitute` argument, as
  * Cholesky::new_with_substitute does (src/linalg/cholesky.rs:216-218). */
 #define NACU_FLAG_SUBSTITUTE 4
+/* Mixed precision: always confirm convergence with a final FP64 residual
+ * instead of accepting an iterate whose predicted error is far below the
+ * target. */
+#define NACU_FLAG_VERIFY 8
 
 #define NACU_LU_BATCHED_MAX_N 128
 #define NACU_LU_BATCHED_MAX_NRHS 16
@@ -140,6 +144,31 @@ int nacu_dpotrs_ragged(int count, int n_max, const int32_t* ns, const int64_t* a
  * `.ln_determinant()` for an n x n SPD matrix (n <= 512). */
 int nacu_dposv(int n, double* A, int nrhs, double* B, int32_t* info, double* logdet, double substitute,
                int flags, nacu_stream_t stream);
+
+/* ---- Cholesky, mixed precision (FP32 factor, FP64 refinement) ------------- */
+
+/* Workspace bytes of nacu_dposv_ragged_mixed: 256 + 8 * total_matrix_elements
+ * (room for an FP32 factor, or for the FP64 fallback factor, per matrix). */
+size_t nacu_mixed_workspace_bytes(int64_t total_matrix_elements);
+
+/* The precision form of nacu_dposv_ragged: same ragged layout, but A and B
+ * are read-only and the solutions go to X (X + b_offsets[s], ns[s] x nrhs,
+ * nrhs <= 4).  Each matrix is factored in FP32 and its solutions refined with
+ * FP64 residuals r = b - A x until the normwise backward error
+ * ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol_units * n * eps64
+ * (tol_units <= 0: 1.0), at most max_iter residuals (<= 0: 10).  A matrix that
+ * is not SPD in FP32 or whose refinement does not converge is refactored and
+ * solved in FP64 in the workspace.  info[s]: 0 ok, k = not SPD (as
+ * nacu_dposv_ragged); iters[s] (nullable): residuals computed, negative when
+ * the FP64 fallback was used.  total_matrix_elements = sum ns[s]^2 (the extent
+ * of A).  No reference counterpart: nalgebra has no mixed precision; it
+ * replaces `m.cholesky()` + `.solve(&b)` (src/linalg/cholesky.rs:221-272,
+ * 122-143) where FP64-accurate solutions, not the factor, are wanted. */
+int nacu_dposv_ragged_mixed(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, const double* A,
+                            int nrhs, const int64_t* b_offsets, const double* B, double* X, int32_t* info,
+                            int32_t* iters, const int32_t* order, int64_t total_matrix_elements, void* workspace,
+                            size_t workspace_bytes, double tol_units, int max_iter, double substitute, int flags,
+                            nacu_stream_t stream);
 
 /* ---- Householder QR and least squares (batched, tall-skinny) ------------- */
 

@@ -20,6 +20,7 @@ NACU_ERR_UNSUPPORTED = 2
 FLAG_EXACT = 1
 FLAG_NO_FACTORS = 2
 FLAG_SUBSTITUTE = 4
+FLAG_VERIFY = 8
 
 _vp = C.c_void_p
 _i = C.c_int
@@ -42,6 +43,9 @@ SIGNATURES = {
     "nacu_dpotrs_ragged": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_dposv": (_i, [_i, _vp, _i, _vp, _vp, _vp, _d, _i, _vp]),
     "nacu_dposv_ragged_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _d, _i, _vp]),
+    "nacu_mixed_workspace_bytes": (_sz, [_i64]),
+    "nacu_dposv_ragged_mixed": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _sz, _d, _i,
+                                     _d, _i, _vp]),
     "nacu_qr_workspace_bytes": (_sz, [_i]),
     "nacu_dgels_batched": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_probe_fp64_peak": (_i, [C.POINTER(C.c_double)]),

@@ -1,0 +1,328 @@
+// Device building blocks of the Cholesky kernels, shared by the FP64 ragged
+// kernel (chol_ragged.cu) and the FP32-factor / FP64-refinement kernel
+// (chol_mixed.cu): templated on the scalar type, see chol_ragged.cu for the
+// algorithm and the reference citations.
+#pragma once
+#include "common.cuh"
+
+namespace nacu {
+namespace {
+
+constexpr int kCholThreads = 128;
+constexpr int kNB = 16;        // panel width
+constexpr int kRhsChunk = 4;   // right-hand sides per register pass
+constexpr int kRowsPerPass = 256;  // rows of the panel update held in registers per pass
+
+// Pivot of column j (cholesky.rs:237-268): re <= 0 -> None, else try_sqrt
+// (x >= 0), NaN fails; the substitute is tried the same way.  EXACT computes the
+// correctly rounded sqrt and 1/sqrt as two operations; the FMA form derives
+// both from one reciprocal square root (one dependent FP64 chain instead of
+// two: on this part every dependent FP64 step costs tens of cycles).
+template <bool EXACT, typename T>
+__device__ __forceinline__ bool chol_pivot(T d, int has_subst, double subst, T* denom, T* rcp) {
+  T v;
+  if (!(d <= T(0)) && d >= T(0)) v = d;
+  else if (has_subst && !(subst <= 0.0) && subst >= 0.0) v = (T)subst;
+  else return false;
+  if constexpr (EXACT) {
+    *denom = sqrt(v);
+    *rcp = T(1) / *denom;
+  } else {
+    const T r = rsqrt(v);
+    *rcp = r;
+    *denom = v * r;
+  }
+  return true;
+}
+
+// Factor one n x n matrix (column-major, lda = n, global memory, in place).
+// Leaves info (0 ok, j+1 first failing pivot) in *s_info and, in the FMA form,
+// 1/L_ii in rdiag[i] for the solves.
+template <bool EXACT, typename T>
+__device__ void chol_factor_cta(int n, T* __restrict__ a, int ldp, T* __restrict__ P, T* rdiag,
+                                int* s_info, T* s_scal, int has_subst, double subst) {
+  const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int J0 = 0; J0 < n; J0 += kNB) {
+    const int jb = min(kNB, n - J0);
+    const int rows = n - J0;
+    // Phase 1+2: P = A[J0.., J0..J0+jb] - L[J0.., 0..J0] * L[J0..J0+jb, 0..J0]^T
+    // (lower part).  Warp w owns columns 4w..4w+3, lanes own rows lane + 32q;
+    // each element still takes its updates in order k = 0, 1, ..., J0-1.
+    for (int cg = warp * 4; cg < jb; cg += (nthr >> 5) * 4) {
+      for (int rb = 0; rb < rows; rb += kRowsPerPass) {
+        const int qmax = min(8, (rows - rb + 31) >> 5);
+        T acc[8][4];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int r = rb + lane + 32 * q, c = cg + j;
+            acc[q][j] = (q < qmax && r < rows && c < jb && r >= c) ? a[(size_t)(J0 + c) * n + J0 + r] : T(0);
+          }
+        const T* colk = a + J0;
+#pragma unroll 2
+        for (int k = 0; k < J0; ++k, colk += n) {
+          // L[c][k]; the negation is folded into the FMA operand (a select of
+          // -x would cost one FP64 instruction per load).
+          T lc[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) lc[j] = (cg + j < jb) ? colk[cg + j] : T(0);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            if (q < qmax) {
+              const int r = rb + lane + 32 * q;
+              const T lr = (r < rows) ? colk[r] : T(0);
+#pragma unroll
+              for (int j = 0; j < 4; ++j) acc[q][j] = axpy1<EXACT>(acc[q][j], -lc[j], lr);
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int r = rb + lane + 32 * q, c = cg + j;
+            if (q < qmax && r < rows && c < jb && r >= c) P[(size_t)c * ldp + r] = acc[q][j];
+          }
+      }
+    }
+    __syncthreads();
+    // Phase 3: factor the panel in shared memory, right-looking inside the panel
+    // (the same per-element update order).  Thread 0 owns every diagonal
+    // element of the trailing update (flattened index 0), so it computes the
+    // next pivot right after its own update: two barriers per column.
+    if (tid == 0) {
+      T denom, rcp;
+      if (chol_pivot<EXACT>(P[0], has_subst, subst, &denom, &rcp)) {
+        P[0] = denom;
+        s_scal[0] = denom;
+        s_scal[1] = rcp;
+        rdiag[J0] = rcp;
+      } else {
+        *s_info = J0 + 1;
+      }
+    }
+    __syncthreads();
+    for (int j = 0; j < jb; ++j) {
+      if (*s_info != 0) return;
+      T* pj = P + (size_t)j * ldp;
+      const T denom = s_scal[0], rcp = s_scal[1];
+      for (int r = j + 1 + tid; r < rows; r += nthr) {
+        if constexpr (EXACT) pj[r] = pj[r] / denom;  // cholesky.rs:261-262 (col /= denom)
+        else pj[r] = pj[r] * rcp;
+      }
+      __syncthreads();
+      const int m = rows - j - 1;  // rows j+1..rows-1
+      const int w = jb - j - 1;    // columns j+1..jb-1
+      if (w > 0) {
+        const int total = m * w;
+        int e = tid;
+        int cq = e / m, rr = e - cq * m;
+        const int dq = nthr / m, dr = nthr - dq * m;
+        for (; e < total; e += nthr) {
+          const int c = j + 1 + cq, r = j + 1 + rr;
+          if (r >= c) {
+            T* pc = P + (size_t)c * ldp;
+            pc[r] = axpy1<EXACT>(pc[r], -pj[c], pj[r]);
+          }
+          rr += dr;
+          cq += dq;
+          if (rr >= m) {
+            rr -= m;
+            ++cq;
+          }
+        }
+        if (tid == 0) {  // element (j+1, j+1) was this thread's first update
+          T* pn = P + (size_t)(j + 1) * ldp + (j + 1);
+          T dn, rn;
+          if (chol_pivot<EXACT>(*pn, has_subst, subst, &dn, &rn)) {
+            *pn = dn;
+            s_scal[0] = dn;
+            s_scal[1] = rn;
+            rdiag[J0 + j + 1] = rn;
+          } else {
+            *s_info = J0 + j + 2;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (*s_info != 0) return;
+    // Phase 4: write the finished panel back (lower part; the strict upper
+    // triangle of the diagonal block was never modified).
+    for (int e = tid; e < rows * jb; e += nthr) {
+      const int c = e / rows, r = e - c * rows;
+      if (r >= c) a[(size_t)(J0 + c) * n + J0 + r] = P[(size_t)c * ldp + r];
+    }
+    __syncthreads();
+  }
+}
+
+// Forward solve L y = b (axpy form) for up to kRhsChunk columns of X (shared,
+// column-major ldx), blocked by 32 rows.
+template <bool EXACT, typename T>
+__device__ void chol_forward_cta(int n, const T* __restrict__ a, T* X, int ldx, int nr, const T* rdiag) {
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int I0 = 0; I0 < n; I0 += 32) {
+    const int ib = min(32, n - I0);
+    if (warp == 0) {
+      T lrow[32];
+      T b[kRhsChunk];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) lrow[i] = (lane < ib && i <= lane) ? a[(size_t)(I0 + i) * n + I0 + lane] : T(0);
+#pragma unroll
+      for (int c = 0; c < kRhsChunk; ++c) b[c] = (lane < ib && c < nr) ? X[(size_t)c * ldx + I0 + lane] : T(0);
+      const T rd = (lane < ib) ? rdiag[I0 + lane] : T(0);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        if (i < ib) {
+#pragma unroll
+          for (int c = 0; c < kRhsChunk; ++c) {
+            if (lane == i) {
+              if constexpr (EXACT) b[c] = b[c] / lrow[i];  // solve.rs:509: b_i / L_ii
+              else b[c] = b[c] * rd;
+            }
+            const T y = __shfl_sync(0xffffffffu, b[c], i);
+            if (lane > i) b[c] = axpy1<EXACT>(b[c], -y, lrow[i]);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < kRhsChunk; ++c)
+        if (lane < ib && c < nr) X[(size_t)c * ldx + I0 + lane] = b[c];
+    }
+    __syncthreads();
+    // Rows below the block: b_r -= sum_i L[r][I0+i] y_i, one thread per row
+    // for all right-hand sides (one L load feeds kRhsChunk FMAs), i ascending.
+    for (int r = I0 + ib + tid; r < n; r += nthr) {
+      T v[kRhsChunk];
+#pragma unroll
+      for (int c = 0; c < kRhsChunk; ++c) v[c] = (c < nr) ? X[(size_t)c * ldx + r] : T(0);
+      const T* lp = a + (size_t)I0 * n + r;
+      for (int i = 0; i < ib; ++i, lp += n) {
+        const T l = *lp;
+#pragma unroll
+        for (int c = 0; c < kRhsChunk; ++c) v[c] = axpy1<EXACT>(v[c], -X[(size_t)c * ldx + I0 + i], l);
+      }
+#pragma unroll
+      for (int c = 0; c < kRhsChunk; ++c)
+        if (c < nr) X[(size_t)c * ldx + r] = v[c];
+    }
+    __syncthreads();
+  }
+}
+
+// Back solve L^T x = y, FMA form: blocked from the bottom, reductions over the
+// rows below each 32-row block, then a warp solve of the transposed block.
+template <typename T>
+__device__ void chol_backward_fast_cta(int n, const T* __restrict__ a, T* X, int ldx, int nr, const T* rdiag) {
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
+  const int nblocks = (n + 31) / 32;
+  for (int bI = nblocks - 1; bI >= 0; --bI) {
+    const int I0 = bI * 32;
+    const int ib = min(32, n - I0);
+    const int r0 = I0 + ib;
+    if (r0 < n) {
+      // y_i -= sum_{r >= r0} L[r][i] x_r for the block's columns i: warp w owns
+      // 4 columns at a time; each lane accumulates 4 columns x 4 rhs over rows
+      // r = r0+lane, r0+lane+32, ... (coalesced column loads), then a butterfly
+      // reduce-scatter leaves sum k = lane & 15 in lane `lane` (16 adds per lane
+      // instead of 16 separate 5-step warp reductions).
+      for (int cb = warp * 4; cb < ib; cb += nwarps * 4) {
+        T v[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = T(0);
+        for (int r = r0 + lane; r < n; r += 32) {
+          T xr[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) xr[c] = (c < nr) ? X[(size_t)c * ldx + r] : T(0);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const T l = (cb + j < ib) ? a[(size_t)(I0 + cb + j) * n + r] : T(0);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) v[j * 4 + c] = fma(l, xr[c], v[j * 4 + c]);
+          }
+        }
+#pragma unroll
+        for (int half = 8; half >= 1; half >>= 1) {
+          const bool up = (lane & half) != 0;
+#pragma unroll
+          for (int t = 0; t < half; ++t) {
+            const T keep = up ? v[t + half] : v[t];
+            const T give = up ? v[t] : v[t + half];
+            v[t] = keep + __shfl_xor_sync(0xffffffffu, give, half);
+          }
+        }
+        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 16);
+        const int j = (lane & 15) >> 2, c = lane & 3;
+        if (lane < 16 && cb + j < ib && c < nr) X[(size_t)c * ldx + I0 + cb + j] -= v[0];
+      }
+      __syncthreads();
+    }
+    if (warp == 0) {
+      T lcol[32];  // lane j holds column j of the diagonal block
+#pragma unroll
+      for (int i = 0; i < 32; ++i) lcol[i] = (lane < ib && i < ib && i >= lane) ? a[(size_t)(I0 + lane) * n + I0 + i] : T(0);
+      const T rd = (lane < ib) ? rdiag[I0 + lane] : T(0);
+      for (int c = 0; c < nr; ++c) {
+        T y = (lane < ib) ? X[(size_t)c * ldx + I0 + lane] : T(0);
+#pragma unroll
+        for (int i = 31; i >= 0; --i) {
+          if (i < ib) {
+            if (lane == i) y = y * rd;
+            const T xi = __shfl_sync(0xffffffffu, y, i);
+            if (lane < i) y = fma(-xi, lcol[i], y);
+          }
+        }
+        if (lane < ib) X[(size_t)c * ldx + I0 + lane] = y;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Back solve L^T x = y in nalgebra's exact order (solve.rs:732-755): for i from
+// n-1 down, x_i = (y_i - dot(L[i+1.., i], x[i+1..])) / L_ii with the
+// 8-accumulator dot of src/base/blas.rs:96-165.  One warp, 8 lanes per rhs.
+__device__ void chol_backward_exact_cta(int n, const double* __restrict__ a, double* X, int ldx, int nr) {
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    const int lane = tid, c = lane >> 3, k = lane & 7;
+    const unsigned grp = 0xffu << (c * 8);
+    double* xc = X + (size_t)(c < nr ? c : 0) * ldx;
+    for (int i = n - 1; i >= 0; --i) {
+      const int len = n - i - 1;
+      const double* li = a + (size_t)i * n + i + 1;
+      const double* xv = xc + i + 1;
+      const int nb = len >> 3;
+      double acc = 0.0;
+      for (int b = 0; b < nb; ++b) acc = __dadd_rn(acc, __dmul_rn(li[8 * b + k], xv[8 * b + k]));
+      // res += acc0 + acc4; res += acc1 + acc5; res += acc2 + acc6; res += acc3 + acc7
+      const double hi = __shfl_down_sync(0xffffffffu, acc, 4, 8);
+      double res = 0.0;
+      double pair = __dadd_rn(acc, hi);  // valid on k < 4
+      const double p0 = __shfl_sync(0xffffffffu, pair, 0, 8);
+      const double p1 = __shfl_sync(0xffffffffu, pair, 1, 8);
+      const double p2 = __shfl_sync(0xffffffffu, pair, 2, 8);
+      const double p3 = __shfl_sync(0xffffffffu, pair, 3, 8);
+      if (k == 0 && c < nr) {
+        res = __dadd_rn(res, p0);
+        res = __dadd_rn(res, p1);
+        res = __dadd_rn(res, p2);
+        res = __dadd_rn(res, p3);
+        for (int t = 8 * nb; t < len; ++t) res = __dadd_rn(res, __dmul_rn(li[t], xv[t]));
+        xc[i] = __ddiv_rn(__dsub_rn(xc[i], res), a[(size_t)i * n + i]);
+      }
+      (void)grp;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace
+}  // namespace nacu

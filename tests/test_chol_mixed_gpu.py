@@ -1,0 +1,93 @@
+"""GPU checks of the mixed-precision ragged SPD solve (FP32 factor, FP64
+refinement): every solution meets the FP64 backward-error target
+||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= n eps64, measured by the
+oracle's compensated residual; A and B are untouched; matrices that FP32
+cannot factor fall back to FP64 and are still solved; non-SPD matrices report
+nalgebra's None (info = failing column)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from nalgebra_gb300 import _lib
+from nalgebra_gb300 import workloads as W
+from tests.conftest import EPS64
+
+pytestmark = pytest.mark.gpu
+FLAG_VERIFY = 8
+
+
+def _mixed(cuda, ns, a_flat, b_flat, nrhs, flags=0, max_iter=0):
+    torch = cuda
+    ns = np.asarray(ns, dtype=np.int32)
+    count = ns.size
+    aoff = np.concatenate([[0], np.cumsum(ns.astype(np.int64) ** 2)[:-1]]).astype(np.int64)
+    boff = np.concatenate([[0], np.cumsum(ns.astype(np.int64) * nrhs)[:-1]]).astype(np.int64)
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    A, B = d(a_flat), d(b_flat)
+    X = torch.full_like(B, np.nan)
+    dns, daoff, dboff = d(ns), d(aoff), d(boff)
+    order = d(np.argsort(-ns, kind="stable").astype(np.int32))
+    info = torch.full((count,), -7, dtype=torch.int32, device="cuda")
+    iters = torch.zeros(count, dtype=torch.int32, device="cuda")
+    total = int(a_flat.size)
+    ws = torch.zeros(_lib.load().nacu_mixed_workspace_bytes(total), dtype=torch.uint8, device="cuda")
+    _lib.call("nacu_dposv_ragged_mixed", count, int(ns.max()), dns.data_ptr(), daoff.data_ptr(), A.data_ptr(), nrhs,
+              dboff.data_ptr(), B.data_ptr(), X.data_ptr(), info.data_ptr(), iters.data_ptr(), order.data_ptr(),
+              total, ws.data_ptr(), ws.numel(), 0.0, max_iter, 0.0, flags, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return (A.cpu().numpy(), B.cpu().numpy(), X.cpu().numpy(), info.cpu().numpy(), iters.cpu().numpy(), aoff, boff)
+
+
+@pytest.mark.parametrize("flags", [0, FLAG_VERIFY])
+def test_workload_slice_meets_fp64_backward_error(cuda, flags):
+    w = W.ragged_spd(400, 8, 256, nrhs=4, seed=3)
+    ns = w["ns"]
+    A, B, X, info, iters, aoff, boff = _mixed(cuda, ns, w["a_flat"], w["b_flat"], 4, flags)
+    assert np.array_equal(A, w["a_flat"]) and np.array_equal(B, w["b_flat"])
+    assert np.all(info == 0)
+    assert np.all(iters > 0), "no FP64 fallback expected on these well-conditioned SPD matrices"
+    _, xo, _, _ = O.posv_ragged(ns, w["a_offsets"], w["a_flat"], w["b_offsets"], w["b_flat"], 4)
+    worst = 0.0
+    for s in range(ns.size):
+        n = int(ns[s])
+        a = w["a_flat"][aoff[s]:aoff[s] + n * n].reshape(n, n).T
+        a = np.tril(a) + np.tril(a, -1).T
+        x = X[boff[s]:boff[s] + 4 * n].reshape(4, n).T
+        b = w["b_flat"][boff[s]:boff[s] + 4 * n].reshape(4, n).T
+        worst = max(worst, O.backward_error(a, x, b) / (n * EPS64))
+    assert worst <= 1.0, worst
+    assert np.allclose(X, xo, rtol=1e-12, atol=1e-14)  # forward error ~ cond * eps, cond <= 5 here
+    if flags == FLAG_VERIFY:
+        assert np.all(iters >= 2)
+
+
+def test_fp32_breakdown_falls_back_to_fp64(cuda):
+    eps = 1e-9
+    m_near = np.array([[1.0, 1.0 - eps], [1.0 - eps, 1.0]])     # SPD in FP64, singular in FP32
+    m_big = 1e200 * np.array([[4.0, 1.0], [1.0, 3.0]])          # overflows FP32
+    m_tiny = 1e-200 * np.array([[4.0, 1.0], [1.0, 3.0]])        # underflows FP32
+    m_bad = np.array([[1.0, 2.0], [2.0, 1.0]])                   # not SPD at all
+    rng = np.random.default_rng(0)
+    bm = rng.standard_normal((30, 30))
+    m_ok = bm @ bm.T + 30 * np.eye(30)
+    mats = [m_near, m_big, m_tiny, m_bad, m_ok]
+    ns = [m.shape[0] for m in mats]
+    a_flat = np.concatenate([m.ravel(order="F") for m in mats])
+    b_flat = rng.standard_normal(sum(ns))
+    A, B, X, info, iters, aoff, boff = _mixed(cuda, ns, a_flat, b_flat, 1)
+    assert list(info) == [0, 0, 0, 2, 0]
+    assert iters[0] < 0 and iters[1] < 0 and iters[2] < 0 and iters[4] > 0
+    for s in (0, 1, 2, 4):
+        n = ns[s]
+        a = mats[s]
+        x = X[boff[s]:boff[s] + n]
+        b = b_flat[boff[s]:boff[s] + n]
+        assert O.backward_error(a, x, b) <= n * EPS64, s
+
+
+def test_max_iter_one_forces_fallback_but_stays_correct(cuda):
+    w = W.ragged_spd(20, 8, 64, nrhs=2, seed=5)
+    A, B, X, info, iters, aoff, boff = _mixed(cuda, w["ns"], w["a_flat"], w["b_flat"], 2, 0, max_iter=1)
+    assert np.all(info == 0)
+    _, xo, _, _ = O.posv_ragged(w["ns"], w["a_offsets"], w["a_flat"], w["b_offsets"], w["b_flat"], 2)
+    assert np.allclose(X, xo, rtol=1e-12, atol=1e-14)
