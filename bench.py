@@ -193,7 +193,11 @@ def bench_ragged_ours(args, rank, world):
     times = [e0.elapsed_time(e1) for e0, e1 in ev]
     kern_ms = float(np.mean(times))
     if args.profile:
-        return {"workload": "ragged_cholesky", "count": count, "ms_per_step": kern_ms}, None
+        out = {"workload": "ragged_cholesky", "count": count, "ms_per_step": kern_ms}
+        if args.profile_mixed:
+            out["mixed"] = bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a0.cpu().numpy(),
+                                              b0.cpu().numpy())
+        return out, None
     info = chol.info.cpu().numpy()
     if np.any(info != 0):
         raise RuntimeError(f"{int(np.sum(info != 0))} systems failed to factor")
@@ -314,7 +318,7 @@ def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_
     info = torch.zeros(count, dtype=torch.int32, device="cuda")
     iters = torch.zeros(count, dtype=torch.int32, device="cuda")
     total = int(a0.numel())
-    ws = torch.empty(L.nacu_mixed_workspace_bytes(total), dtype=torch.uint8, device="cuda")
+    ws = torch.empty(L.nacu_mixed_workspace_bytes(count, total), dtype=torch.uint8, device="cuda")
 
     def launch():
         _lib.call("nacu_dposv_ragged_mixed", count, int(ns.max()), dns.data_ptr(), daoff.data_ptr(), a0.data_ptr(),
@@ -530,6 +534,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=0, help="ragged_cholesky: override the number of systems")
     ap.add_argument("--profile", action="store_true", help="timed kernel only (for ncu captures)")
+    ap.add_argument("--profile-mixed", action="store_true", help="with --profile: also run the mixed-precision form")
     args = ap.parse_args()
     rank, world, local = dist_env()
 

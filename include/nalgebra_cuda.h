@@ -147,9 +147,10 @@ int nacu_dposv(int n, double* A, int nrhs, double* B, int32_t* info, double* log
 
 /* ---- Cholesky, mixed precision (FP32 factor, FP64 refinement) ------------- */
 
-/* Workspace bytes of nacu_dposv_ragged_mixed: 256 + 8 * total_matrix_elements
- * (room for an FP32 factor, or for the FP64 fallback factor, per matrix). */
-size_t nacu_mixed_workspace_bytes(int64_t total_matrix_elements);
+/* Workspace bytes of nacu_dposv_ragged_mixed: queue heads and a fallback
+ * list (4 bytes per matrix), then 8 bytes per matrix element (room for the
+ * FP32 factor, or for the FP64 fallback factor). */
+size_t nacu_mixed_workspace_bytes(int count, int64_t total_matrix_elements);
 
 /* The precision form of nacu_dposv_ragged: same ragged layout, but A and B
  * are read-only and the solutions go to X (X + b_offsets[s], ns[s] x nrhs,

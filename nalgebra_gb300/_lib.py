@@ -43,7 +43,7 @@ SIGNATURES = {
     "nacu_dpotrs_ragged": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_dposv": (_i, [_i, _vp, _i, _vp, _vp, _vp, _d, _i, _vp]),
     "nacu_dposv_ragged_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _d, _i, _vp]),
-    "nacu_mixed_workspace_bytes": (_sz, [_i64]),
+    "nacu_mixed_workspace_bytes": (_sz, [_i, _i64]),
     "nacu_dposv_ragged_mixed": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _sz, _d, _i,
                                      _d, _i, _vp]),
     "nacu_qr_workspace_bytes": (_sz, [_i]),

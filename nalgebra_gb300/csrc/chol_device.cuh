@@ -202,10 +202,16 @@ __device__ void chol_forward_cta(int n, const T* __restrict__ a, T* X, int ldx, 
 #pragma unroll
       for (int c = 0; c < kRhsChunk; ++c) v[c] = (c < nr) ? X[(size_t)c * ldx + r] : T(0);
       const T* lp = a + (size_t)I0 * n + r;
-      for (int i = 0; i < ib; ++i, lp += n) {
-        const T l = *lp;
+      for (int i0 = 0; i0 < ib; i0 += 8) {  // 8 independent loads in flight
+        T l8[8];
 #pragma unroll
-        for (int c = 0; c < kRhsChunk; ++c) v[c] = axpy1<EXACT>(v[c], -X[(size_t)c * ldx + I0 + i], l);
+        for (int u = 0; u < 8; ++u) l8[u] = (i0 + u < ib) ? lp[(size_t)(i0 + u) * n] : T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (i0 + u < ib)
+#pragma unroll
+            for (int c = 0; c < kRhsChunk; ++c)
+              v[c] = axpy1<EXACT>(v[c], -X[(size_t)c * ldx + I0 + i0 + u], l8[u]);
       }
 #pragma unroll
       for (int c = 0; c < kRhsChunk; ++c)
@@ -236,15 +242,25 @@ __device__ void chol_backward_fast_cta(int n, const T* __restrict__ a, T* X, int
         T v[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) v[k] = T(0);
-        for (int r = r0 + lane; r < n; r += 32) {
-          T xr[4];
+        for (int r0l = r0 + lane; r0l < n; r0l += 64) {  // two rows per step: 8 loads in flight
+          T l2[2][4];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) xr[c] = (c < nr) ? X[(size_t)c * ldx + r] : T(0);
+          for (int h = 0; h < 2; ++h)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const T l = (cb + j < ib) ? a[(size_t)(I0 + cb + j) * n + r] : T(0);
+            for (int j = 0; j < 4; ++j) {
+              const int r = r0l + 32 * h;
+              l2[h][j] = (cb + j < ib && r < n) ? a[(size_t)(I0 + cb + j) * n + r] : T(0);
+            }
 #pragma unroll
-            for (int c = 0; c < 4; ++c) v[j * 4 + c] = fma(l, xr[c], v[j * 4 + c]);
+          for (int h = 0; h < 2; ++h) {
+            const int r = r0l + 32 * h;
+            T xr[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) xr[c] = (c < nr && r < n) ? X[(size_t)c * ldx + r] : T(0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+              for (int c = 0; c < 4; ++c) v[j * 4 + c] = fma(l2[h][j], xr[c], v[j * 4 + c]);
           }
         }
 #pragma unroll

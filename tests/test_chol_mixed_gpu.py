@@ -30,7 +30,7 @@ def _mixed(cuda, ns, a_flat, b_flat, nrhs, flags=0, max_iter=0):
     info = torch.full((count,), -7, dtype=torch.int32, device="cuda")
     iters = torch.zeros(count, dtype=torch.int32, device="cuda")
     total = int(a_flat.size)
-    ws = torch.zeros(_lib.load().nacu_mixed_workspace_bytes(total), dtype=torch.uint8, device="cuda")
+    ws = torch.zeros(_lib.load().nacu_mixed_workspace_bytes(count, total), dtype=torch.uint8, device="cuda")
     _lib.call("nacu_dposv_ragged_mixed", count, int(ns.max()), dns.data_ptr(), daoff.data_ptr(), A.data_ptr(), nrhs,
               dboff.data_ptr(), B.data_ptr(), X.data_ptr(), info.data_ptr(), iters.data_ptr(), order.data_ptr(),
               total, ws.data_ptr(), ws.numel(), 0.0, max_iter, 0.0, flags, torch.cuda.current_stream().cuda_stream)
