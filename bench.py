@@ -177,6 +177,14 @@ def bench_ragged_ours(args, rank, world):
         restore()
         launch()
     torch.cuda.synchronize()
+    # the batching form runs as a captured CUDA graph (memset + persistent launch)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        launch()
+    stream = torch.cuda.current_stream()
+    restore()
+    graph.replay()
+    torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if world > 1:
         torch.distributed.barrier()
@@ -185,7 +193,7 @@ def bench_ragged_ours(args, rank, world):
         for i in range(args.steps):
             restore()
             ev[i][0].record(stream)
-            launch()
+            graph.replay()
             ev[i][1].record(stream)
         torch.cuda.synchronize()
     if world > 1:
@@ -521,6 +529,68 @@ def bench_ls_ours(args, rank, world):
             "gpu_launches": args.steps, "clocks": clk.summary()}
 
 
+# ----------------------------------------------------------------------------- adjoint
+
+def bench_adjoint_ours(args, rank, world):
+    """2048 SPD systems of order 128 (f64 and f32): forward (factor + solve +
+    logdet) and backward (db, dA) of l = sum w^T x + logdet A, store vs
+    recompute."""
+    import torch
+
+    from nalgebra_gb300 import _lib
+    from nalgebra_gb300 import workloads as W
+
+    L = _lib.load()
+    count, n = args.count or 2048, 128
+    out = {}
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    for dtype, pre, tdt in ((np.float64, "d", torch.float64), (np.float32, "s", torch.float32)):
+        a, b, w = W.spd_uniform(count, n, seed=rank, dtype=dtype)
+        d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+        A, B, Wt = d(a), d(b), d(w)
+        X = torch.zeros((count, n), dtype=tdt, device="cuda")
+        Lf = torch.zeros_like(A)
+        logdet = torch.zeros(count, dtype=tdt, device="cuda")
+        info = torch.zeros(count, dtype=torch.int32, device="cuda")
+        dA = torch.zeros_like(A)
+        db = torch.zeros_like(X)
+        res = {}
+        for mode in ("store", "recompute"):
+            rec = mode == "recompute"
+
+            def fwd():
+                _lib.call(f"nacu_{pre}posv_logdet_forward", n, A.data_ptr(), n * n, B.data_ptr(), X.data_ptr(),
+                          0 if rec else Lf.data_ptr(), logdet.data_ptr(), info.data_ptr(), count, sp)
+
+            def bwd():
+                _lib.call(f"nacu_{pre}posv_logdet_backward", n, (A if rec else Lf).data_ptr(), n * n, 1 if rec else 0,
+                          X.data_ptr(), Wt.data_ptr(), dA.data_ptr(), db.data_ptr(), info.data_ptr(), count, sp)
+
+            for _ in range(args.warmup):
+                fwd(); bwd()
+            torch.cuda.synchronize()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record(stream)
+            for _ in range(args.steps):
+                fwd()
+            e[1].record(stream)
+            for _ in range(args.steps):
+                bwd()
+            e[2].record(stream)
+            torch.cuda.synchronize()
+            fms, bms = e[0].elapsed_time(e[1]) / args.steps, e[1].elapsed_time(e[2]) / args.steps
+            res[mode] = {"forward_ms": fms, "backward_ms": bms,
+                         "systems_per_s_fwd_bwd": count / ((fms + bms) * 1e-3),
+                         "stored_intermediate_bytes": 0 if rec else int(count * n * n * np.dtype(dtype).itemsize)}
+        out[pre + "_" + np.dtype(dtype).name] = res
+    return {"metric": "adjoint of batched Cholesky solve + logdet (2048 x 128, f64 and f32)",
+            "value": out["d_float64"]["store"]["systems_per_s_fwd_bwd"], "unit": "systems/s (forward+backward, f64)",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "adjoint", "count": count, "n": n}, "forms": out, "gpu_launches": 2 * args.steps}
+
+
 # ----------------------------------------------------------------------------- main
 
 def main():
@@ -529,7 +599,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr"])
+    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=0, help="ragged_cholesky: override the number of systems")
@@ -558,8 +628,9 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
-    if args.workload in ("lu_batched", "ls_qr"):
-        res = (bench_lu_ours if args.workload == "lu_batched" else bench_ls_ours)(args, rank, world)
+    if args.workload in ("lu_batched", "ls_qr", "adjoint"):
+        res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours}[args.workload](
+            args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

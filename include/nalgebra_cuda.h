@@ -171,6 +171,32 @@ int nacu_dposv_ragged_mixed(int count, int n_max, const int32_t* ns, const int64
                             size_t workspace_bytes, double tol_units, int max_iter, double substitute, int flags,
                             nacu_stream_t stream);
 
+/* ---- Adjoint of the Cholesky solve and log-determinant (batched, n <= 128) - */
+
+/* Forward: for `batch` SPD matrices A + s*strideA (lower triangle read),
+ * X[s*n..] = A^-1 B[s*n..] and logdet[s] = sum ln(L_ii^2)
+ * (src/linalg/cholesky.rs:221-272, 122-143, 172-185).  L (nullable) receives
+ * the factor (lower triangle, zeros above): the "store" form keeps it for the
+ * backward pass; pass NULL to keep nothing (the "recompute" form).  No
+ * reference counterpart for the adjoint itself: nalgebra has no autodiff. */
+int nacu_dposv_logdet_forward(int n, const double* A, int64_t strideA, const double* B, double* X, double* L,
+                              double* logdet, int32_t* info, int batch, nacu_stream_t stream);
+int nacu_sposv_logdet_forward(int n, const float* A, int64_t strideA, const float* B, float* X, float* L,
+                              float* logdet, int32_t* info, int batch, nacu_stream_t stream);
+
+/* Backward of l = sum_s w_s^T x_s + logdet A_s: db[s*n..] = A^-1 w and the
+ * gradient with respect to the lower-triangle entries of A in dA's lower
+ * triangle (dA_ii = -v_i x_i + (A^-1)_ii, dA_ij = -(v_i x_j + v_j x_i) +
+ * 2 (A^-1)_ij for i > j, v = A^-1 w; zeros above).  AL holds the stored factor
+ * L (recompute = 0) or the original A (recompute = 1: the factor is rebuilt,
+ * trading n^3/3 flops for n^2 stored values per matrix). */
+int nacu_dposv_logdet_backward(int n, const double* AL, int64_t strideA, int recompute, const double* X,
+                               const double* W, double* dA, double* db, int32_t* info, int batch,
+                               nacu_stream_t stream);
+int nacu_sposv_logdet_backward(int n, const float* AL, int64_t strideA, int recompute, const float* X,
+                               const float* W, float* dA, float* db, int32_t* info, int batch,
+                               nacu_stream_t stream);
+
 /* ---- Householder QR and least squares (batched, tall-skinny) ------------- */
 
 /* Bytes of device scratch nacu_dgels_batched needs (the work-queue head). */

@@ -350,6 +350,25 @@ class CholeskyBatch:
         self.solve_mut(res)
         return res
 
+    def capture(self, rhs: DeviceBatch):
+        """Capture the fused factor + solve + log-det of this batch into a CUDA
+        graph (torch.cuda.CUDAGraph); ``graph.replay()`` re-runs it on the
+        same device buffers (refill them between replays: the factorization is
+        in place).  The calls it captures neither synchronize nor allocate."""
+        torch = _torch()
+        g = torch.cuda.CUDAGraph()
+        stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(stream):
+            self.factored = False
+            self.solve_mut(rhs)  # warm-up launch outside the graph (first-use set-up)
+        torch.cuda.current_stream().wait_stream(stream)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g):
+            self.factored = False
+            self.solve_mut(rhs)
+        return g
+
     def ln_determinant(self) -> np.ndarray:
         self.factor()
         return self.logdet.cpu().numpy()

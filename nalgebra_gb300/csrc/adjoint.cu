@@ -1,0 +1,344 @@
+// Reverse-mode adjoint of the batched Cholesky solve and log-determinant, for
+// batches of equal-order SPD matrices (n <= 128), in FP64 and FP32.
+//
+// Forward (nalgebra's `m.cholesky()`, `.solve(&b)`, `.ln_determinant()`,
+// src/linalg/cholesky.rs:221-272, 122-143, 172-185): x = A^-1 b and
+// logdet A = sum ln(L_ii^2); the factor L is written out (the "store" form)
+// or discarded (the "recompute" form keeps only A).
+//
+// Backward, for the loss  l = sum_s w_s^T x_s + logdet A_s  (nalgebra has no
+// autodiff; this is the chosen differentiation form):
+//   v  = A^-1 w                       (dl/db)
+//   Abar = -v x^T + A^-1              (dl/dA for an unstructured A)
+// nalgebra reads only the lower triangle, so the parameters are the lower
+// entries theta_ij (i >= j) with A_ij = A_ji = theta_ij; the gradient
+// returned in dA's lower triangle is
+//   dA_ii = Abar_ii = -v_i x_i + (A^-1)_ii,
+//   dA_ij = Abar_ij + Abar_ji = -(v_i x_j + v_j x_i) + 2 (A^-1)_ij  (i > j),
+// which is what central differences on theta_ij measure.  (Giles 2008,
+// "Collected matrix derivative results for forward and reverse mode AD";
+// Murray 2016, "Differentiation of the Cholesky decomposition".)
+//
+// Design: one CTA (256 threads) per matrix with the whole n x n matrix in
+// shared memory (column-major, odd leading dimension), so the factorization,
+// the in-place triangular inverse L -> L^-1 and the product
+// A^-1 = L^-T L^-1 run out of shared memory.  Trailing updates use a
+// pair-folded index over the lower triangle (column c paired with column
+// m-1-c fills an (m+1) x ceil(m/2) rectangle), so no lane idles on the
+// triangle's empty half.
+#include "common.cuh"
+
+namespace nacu {
+namespace {
+
+constexpr int kAdjThreads = 256;
+constexpr int kAdjMaxN = 128;
+
+template <typename T>
+__device__ __forceinline__ T fma_t(T a, T b, T c) {
+  if constexpr (sizeof(T) == 8) return fma(a, b, c);
+  else return fmaf(a, b, c);
+}
+
+// Pair-folded enumeration of the lower triangle (rows >= column) of an m x m
+// block: rectangle index (k, q), k in [0, m+1), q in [0, ceil(m/2)).
+__device__ __forceinline__ bool fold(int m, int k, int q, int* r, int* c) {
+  const int len = m - q;  // column q holds rows q..m-1
+  if (k < len) {
+    *c = q;
+    *r = q + k;
+    return true;
+  }
+  const int c2 = m - 1 - q;
+  if (c2 <= q) return false;  // odd m: the middle column appears once
+  *c = c2;
+  *r = c2 + (k - len);
+  return *r < m;
+}
+
+// Right-looking Cholesky of the n x n matrix in S (lower triangle).
+// Returns info (0 ok, j+1 first failing pivot) in *s_info.
+template <typename T>
+__device__ void chol_smem(int n, T* S, int ld, int* s_info, T* s_sc) {
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  for (int j = 0; j < n; ++j) {
+    T* cj = S + (size_t)j * ld;
+    if (tid == 0) {
+      const T d = cj[j];
+      if (!(d <= T(0)) && d >= T(0)) {
+        const T den = sqrt(d);
+        cj[j] = den;
+        s_sc[0] = T(1) / den;
+      } else if (*s_info == 0) {
+        *s_info = j + 1;
+      }
+    }
+    __syncthreads();
+    if (*s_info != 0) return;
+    const T rcp = s_sc[0];
+    for (int r = j + 1 + tid; r < n; r += nthr) cj[r] *= rcp;
+    __syncthreads();
+    const int m = n - j - 1;
+    if (m > 0) {
+      const int qn = (m + 1) >> 1, total = (m + 1) * qn;
+      for (int e = tid; e < total; e += nthr) {
+        const int q = e / (m + 1), k = e - q * (m + 1);
+        int r, c;
+        if (fold(m, k, q, &r, &c)) {
+          r += j + 1;
+          c += j + 1;
+          S[(size_t)c * ld + r] = fma_t(-cj[r], cj[c], S[(size_t)c * ld + r]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// In place L -> L^-1 (lower), columns from right to left (LAPACK trti2 order):
+// L^-1[j+1.., j] = -(1/L_jj) * L^-1[j+1.., j+1..] * L[j+1.., j].
+// Thread t owns rows j+1+t and n-1-t so every thread walks n-j-1 terms.
+template <typename T>
+__device__ void trinv_smem(int n, T* S, int ld, T* tmp) {
+  const int tid = threadIdx.x;
+  for (int j = n - 1; j >= 0; --j) {
+    T* cj = S + (size_t)j * ld;
+    const T ajj = T(1) / cj[j];
+    const int m = n - j - 1;
+    const int half = (m + 1) >> 1;
+    for (int t = tid; t < half; t += blockDim.x) {
+      const int i1 = j + 1 + t, i2 = n - 1 - t;
+      const int len1 = i1 - j, len2 = (i2 != i1) ? (i2 - j) : 0;
+      T s1 = T(0), s2 = T(0);
+      for (int q = 0; q < len1 + len2; ++q) {  // one loop: no divergence
+        const bool first = q < len1;
+        const int i = first ? i1 : i2;
+        const int k = j + 1 + (first ? q : q - len1);
+        const T p = S[(size_t)k * ld + i] * cj[k];  // L^-1[i][k] * L[k][j]
+        if (first) s1 += p;
+        else s2 += p;
+      }
+      tmp[i1] = -ajj * s1;
+      if (len2) tmp[i2] = -ajj * s2;
+    }
+    __syncthreads();
+    for (int i = j + 1 + tid; i < n; i += blockDim.x) cj[i] = tmp[i];
+    if (tid == 0) cj[j] = ajj;
+    __syncthreads();
+  }
+}
+
+// In place L^-1 -> A^-1 = L^-T L^-1 (lower triangle), column by column:
+// (A^-1)_ij = sum_{k >= i} Linv_ki Linv_kj  (i >= j); column j needs only
+// columns >= j of L^-1, so it can be overwritten once computed.
+template <typename T>
+__device__ void inv_from_trinv_smem(int n, T* S, int ld, T* tmp) {
+  const int tid = threadIdx.x;
+  for (int j = 0; j < n; ++j) {
+    const T* cj = S + (size_t)j * ld;
+    const int m = n - j;
+    const int half = (m + 1) >> 1;
+    for (int t = tid; t < half; t += blockDim.x) {
+      // rows i1 = j+t (sum over k = i1..n-1: n-i1 terms) and i2 = n-1-t
+      const int i1 = j + t, i2 = n - 1 - t;
+      const int len1 = n - i1, len2 = (i2 != i1) ? (n - i2) : 0;
+      T s1 = T(0), s2 = T(0);
+      for (int q = 0; q < len1 + len2; ++q) {
+        const bool first = q < len1;
+        const int i = first ? i1 : i2;
+        const int k = (first ? i1 + q : i2 + (q - len1));
+        const T p = S[(size_t)i * ld + k] * cj[k];  // Linv[k][i] * Linv[k][j]
+        if (first) s1 += p;
+        else s2 += p;
+      }
+      tmp[i1] = s1;
+      if (len2) tmp[i2] = s2;
+    }
+    __syncthreads();
+    T* cw = S + (size_t)j * ld;
+    for (int i = j + tid; i < n; i += blockDim.x) cw[i] = tmp[i];
+    __syncthreads();
+  }
+}
+
+// Forward: S <- A (lower), factor, x = A^-1 b (forward + back substitution in
+// shared memory), logdet; write L (store form) or nothing.
+template <typename T>
+__global__ void __launch_bounds__(kAdjThreads) adj_forward_kernel(int n, const T* __restrict__ A, int64_t strideA,
+                                                                  const T* __restrict__ B, T* __restrict__ X,
+                                                                  T* __restrict__ Lout, T* __restrict__ logdet,
+                                                                  int32_t* __restrict__ info, int batch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_info;
+  __shared__ T s_sc[2];
+  const int ld = n | 1;
+  T* S = reinterpret_cast<T*>(smem_raw);
+  T* y = S + (size_t)ld * n;
+  const int tid = threadIdx.x;
+  for (int s = blockIdx.x; s < batch; s += gridDim.x) {
+    const T* a = A + (size_t)s * strideA;
+    for (int e = tid; e < n * n; e += blockDim.x) {
+      const int c = e / n, r = e - c * n;
+      if (r >= c) S[(size_t)c * ld + r] = a[e];
+    }
+    for (int i = tid; i < n; i += blockDim.x) y[i] = B[(size_t)s * n + i];
+    if (tid == 0) s_info = 0;
+    __syncthreads();
+    chol_smem<T>(n, S, ld, &s_info, s_sc);
+    const int inf = s_info;
+    if (inf == 0) {
+      // L y = b then L^T x = y; one warp (n <= 128: four rows per lane)
+      if (tid < 32) {
+        for (int i = 0; i < n; ++i) {
+          if (tid == 0) y[i] = y[i] / S[(size_t)i * ld + i];
+          __syncwarp();
+          const T yi = y[i];
+          for (int r = i + 1 + tid; r < n; r += 32) y[r] = fma_t(-yi, S[(size_t)i * ld + r], y[r]);
+          __syncwarp();
+        }
+        for (int i = n - 1; i >= 0; --i) {
+          T sacc = T(0);
+          for (int r = i + 1 + tid; r < n; r += 32) sacc = fma_t(S[(size_t)i * ld + r], y[r], sacc);
+          sacc = warp_sum(sacc);
+          if (tid == 0) y[i] = (y[i] - sacc) / S[(size_t)i * ld + i];
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+      for (int i = tid; i < n; i += blockDim.x) X[(size_t)s * n + i] = y[i];
+      if (tid == 0) {
+        T sum = T(0);
+        for (int i = 0; i < n; ++i) {
+          const T d = S[(size_t)i * ld + i];
+          sum += log(d * d);
+        }
+        logdet[s] = sum;
+      }
+      if (Lout)
+        for (int e = tid; e < n * n; e += blockDim.x) {
+          const int c = e / n, r = e - c * n;
+          Lout[(size_t)s * strideA + e] = (r >= c) ? S[(size_t)c * ld + r] : T(0);
+        }
+    }
+    if (tid == 0 && info) info[s] = inf;
+    __syncthreads();
+  }
+}
+
+// Backward: from L (store form) or A (recompute form) build A^-1 in shared
+// memory, then db = v = A^-1 w and the lower-triangle gradient dA.
+template <typename T>
+__global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const T* __restrict__ AL, int64_t strideA,
+                                                                   int recompute, const T* __restrict__ X,
+                                                                   const T* __restrict__ Wt, T* __restrict__ dA,
+                                                                   T* __restrict__ db, int32_t* __restrict__ info,
+                                                                   int batch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_info;
+  __shared__ T s_sc[2];
+  const int ld = n | 1;
+  T* S = reinterpret_cast<T*>(smem_raw);
+  T* tmp = S + (size_t)ld * n;
+  T* v = tmp + n;
+  T* xs = v + n;
+  T* ws = xs + n;
+  const int tid = threadIdx.x;
+  for (int s = blockIdx.x; s < batch; s += gridDim.x) {
+    const T* a = AL + (size_t)s * strideA;
+    for (int e = tid; e < n * n; e += blockDim.x) {
+      const int c = e / n, r = e - c * n;
+      if (r >= c) S[(size_t)c * ld + r] = a[e];
+    }
+    for (int i = tid; i < n; i += blockDim.x) {
+      xs[i] = X[(size_t)s * n + i];
+      ws[i] = Wt[(size_t)s * n + i];
+    }
+    if (tid == 0) s_info = 0;
+    __syncthreads();
+    if (recompute) chol_smem<T>(n, S, ld, &s_info, s_sc);  // refactor instead of storing L
+    const int inf = s_info;
+    if (inf == 0) {
+      trinv_smem<T>(n, S, ld, tmp);
+      inv_from_trinv_smem<T>(n, S, ld, tmp);
+      // v = A^-1 w from the lower triangle of the symmetric A^-1
+      for (int i = tid; i < n; i += blockDim.x) {
+        T acc = T(0);
+        for (int k = 0; k <= i; ++k) acc = fma_t(S[(size_t)k * ld + i], ws[k], acc);
+        for (int k = i + 1; k < n; ++k) acc = fma_t(S[(size_t)i * ld + k], ws[k], acc);
+        v[i] = acc;
+      }
+      __syncthreads();
+      for (int i = tid; i < n; i += blockDim.x) db[(size_t)s * n + i] = v[i];
+      T* g = dA + (size_t)s * strideA;
+      for (int e = tid; e < n * n; e += blockDim.x) {
+        const int c = e / n, r = e - c * n;
+        T val = T(0);
+        if (r == c) val = fma_t(-v[r], xs[r], S[(size_t)c * ld + r]);
+        else if (r > c) val = fma_t(-v[r], xs[c], fma_t(-v[c], xs[r], T(2) * S[(size_t)c * ld + r]));
+        g[e] = val;
+      }
+    }
+    if (tid == 0 && info) info[s] = inf;
+    __syncthreads();
+  }
+}
+
+template <typename T>
+int adj_launch_forward(int n, const T* A, int64_t strideA, const T* B, T* X, T* Lout, T* logdet, int32_t* info,
+                       int batch, cudaStream_t stream, const char* name) {
+  if (n < 1 || n > kAdjMaxN) return record_arg_error(-1, "posv_logdet_forward: n out of range [1, 128]");
+  if (batch < 0) return record_arg_error(-9, "posv_logdet_forward: negative batch");
+  if (batch == 0) return NACU_SUCCESS;
+  if (!A || !B || !X || !logdet) return record_arg_error(-2, "posv_logdet_forward: null A, B, X or logdet");
+  if (strideA < (int64_t)n * n) return record_arg_error(-3, "posv_logdet_forward: strideA < n*n");
+  const size_t smem = ((size_t)(n | 1) * n + n) * sizeof(T);
+  cudaError_t e = cudaFuncSetAttribute(adj_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  adj_forward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, A, strideA, B, X, Lout, logdet, info, batch);
+  return check_launch(name);
+}
+
+template <typename T>
+int adj_launch_backward(int n, const T* AL, int64_t strideA, int recompute, const T* X, const T* W, T* dA, T* db,
+                        int32_t* info, int batch, cudaStream_t stream, const char* name) {
+  if (n < 1 || n > kAdjMaxN) return record_arg_error(-1, "posv_logdet_backward: n out of range [1, 128]");
+  if (batch < 0) return record_arg_error(-10, "posv_logdet_backward: negative batch");
+  if (batch == 0) return NACU_SUCCESS;
+  if (!AL || !X || !W || !dA || !db) return record_arg_error(-2, "posv_logdet_backward: null argument");
+  if (strideA < (int64_t)n * n) return record_arg_error(-3, "posv_logdet_backward: strideA < n*n");
+  const size_t smem = ((size_t)(n | 1) * n + 4 * (size_t)n) * sizeof(T);
+  cudaError_t e = cudaFuncSetAttribute(adj_backward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  adj_backward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, AL, strideA, recompute, X, W, dA, db, info, batch);
+  return check_launch(name);
+}
+
+}  // namespace
+}  // namespace nacu
+
+extern "C" {
+
+int nacu_dposv_logdet_forward(int n, const double* A, int64_t strideA, const double* B, double* X, double* L,
+                              double* logdet, int32_t* info, int batch, nacu_stream_t stream) {
+  return nacu::adj_launch_forward<double>(n, A, strideA, B, X, L, logdet, info, batch, (cudaStream_t)stream,
+                                          "nacu_dposv_logdet_forward");
+}
+int nacu_sposv_logdet_forward(int n, const float* A, int64_t strideA, const float* B, float* X, float* L,
+                              float* logdet, int32_t* info, int batch, nacu_stream_t stream) {
+  return nacu::adj_launch_forward<float>(n, A, strideA, B, X, L, logdet, info, batch, (cudaStream_t)stream,
+                                         "nacu_sposv_logdet_forward");
+}
+int nacu_dposv_logdet_backward(int n, const double* AL, int64_t strideA, int recompute, const double* X,
+                               const double* W, double* dA, double* db, int32_t* info, int batch,
+                               nacu_stream_t stream) {
+  return nacu::adj_launch_backward<double>(n, AL, strideA, recompute, X, W, dA, db, info, batch,
+                                           (cudaStream_t)stream, "nacu_dposv_logdet_backward");
+}
+int nacu_sposv_logdet_backward(int n, const float* AL, int64_t strideA, int recompute, const float* X,
+                               const float* W, float* dA, float* db, int32_t* info, int batch,
+                               nacu_stream_t stream) {
+  return nacu::adj_launch_backward<float>(n, AL, strideA, recompute, X, W, dA, db, info, batch,
+                                          (cudaStream_t)stream, "nacu_sposv_logdet_backward");
+}
+
+}  // extern "C"

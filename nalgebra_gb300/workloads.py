@@ -99,3 +99,15 @@ def ragged_ls(count: int, m_lo: int, m_hi: int, n: int = 64, seed: int = 0):
     a_flat = rng.standard_normal(int(sizes.sum()))
     b_flat = rng.standard_normal(int(ms.astype(np.int64).sum()))
     return dict(ms=ms, a_offsets=aoff, a_flat=a_flat, b_offsets=boff, b_flat=b_flat, n=n)
+
+
+def spd_uniform(count: int, n: int, seed: int = 0, dtype=np.float64):
+    """Equal-order SPD batch for the adjoint workload: A = B B^T + n I with
+    B ~ N(0,1), right-hand sides b and loss weights w ~ N(0,1).  Returns
+    (A (count, n*n) column-major rows, b (count, n), w (count, n))."""
+    rng = np.random.default_rng(seed)
+    bm = rng.standard_normal((count, n, n))
+    a = bm @ np.transpose(bm, (0, 2, 1)) + n * np.eye(n)
+    b = rng.standard_normal((count, n))
+    w = rng.standard_normal((count, n))
+    return (np.ascontiguousarray(a.reshape(count, n * n)).astype(dtype), b.astype(dtype), w.astype(dtype))
