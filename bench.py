@@ -591,6 +591,91 @@ def bench_adjoint_ours(args, rank, world):
             "config": {"workload": "adjoint", "count": count, "n": n}, "forms": out, "gpu_launches": 2 * args.steps}
 
 
+# ----------------------------------------------------------------------------- GEMM
+
+def bench_gemm_ours(args, rank, world):
+    """Matrix::gemm on m = n = k (default 8192) f64, A = N(0,1) 2^k per row,
+    B = N(0,1) 2^k per column, k uniform in [-20, 20]: native FP64 (nacu_dgemm)
+    vs BF16-split / FP32-accumulate tensor-core form (nacu_dgemm_split_bf16);
+    error of both against a compensated FP64 oracle on sampled entries."""
+    import ctypes
+
+    import torch
+
+    from nalgebra_gb300 import _lib
+
+    L = _lib.load()
+    n = args.count or 8192
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1234 + rank)
+    A = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn((n, n), dtype=torch.float64, device="cuda", generator=g)
+    # column-major: A[i, k] stored at k*n + i -> use the transposed views as storage
+    rs = torch.pow(2.0, torch.randint(-20, 21, (n,), device="cuda", generator=g).double())
+    cs = torch.pow(2.0, torch.randint(-20, 21, (n,), device="cuda", generator=g).double())
+    Acm = (A * rs[:, None]).t().contiguous()  # memory = column-major A
+    Bcm = (B * cs[None, :]).t().contiguous()  # memory = column-major B
+    C64 = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    C16 = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+    wsb = L.nacu_gemm_split_workspace_bytes(n, n, n)
+    ws = torch.empty(wsb + 1024, dtype=torch.uint8, device="cuda")
+    wp = (ws.data_ptr() + 1023) // 1024 * 1024
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+
+    def fp64():
+        _lib.call("nacu_dgemm", n, n, n, 1.0, Acm.data_ptr(), n, Bcm.data_ptr(), n, 0.0, C64.data_ptr(), n, sp)
+
+    def split():
+        _lib.call("nacu_dgemm_split_bf16", n, n, n, 1.0, Acm.data_ptr(), n, Bcm.data_ptr(), n, 0.0, C16.data_ptr(), n,
+                  3, wp, wsb, sp)
+
+    res = {}
+    for name, fn, steps in (("split_bf16x3", split, args.steps), ("fp64", fp64, max(1, min(args.steps, 2)))):
+        for _ in range(max(1, min(args.warmup, 2) if name == "fp64" else args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        res[name] = {"ms": ms, "tflops_fp64_equivalent": 2.0 * n ** 3 / (ms * 1e-3) / 1e12, "clocks": clk.summary()}
+    flag = ctypes.c_int(0)
+    L.nacu_split_gemm_error(ctypes.byref(flag))
+    # error on sampled entries against the compensated oracle (64 x 64 sample)
+    import oracle as O
+    rng = np.random.default_rng(5)
+    ri = np.sort(rng.choice(n, 64, replace=False))
+    ci = np.sort(rng.choice(n, 64, replace=False))
+    a_rows = Acm.view(n, n).t()[ri, :].cpu().numpy()      # rows of A
+    b_cols = Bcm.view(n, n).t()[:, ci].cpu().numpy()      # columns of B
+    ref = O.gemm_dot2(1.0, a_rows, b_cols)
+    scale = np.abs(a_rows) @ np.abs(b_cols)
+    got64 = C64.view(n, n).t()[ri][:, ci].cpu().numpy()
+    got16 = C16.view(n, n).t()[ri][:, ci].cpu().numpy()
+    res["fp64"]["max_err_rel_to_absAabsB"] = float(np.max(np.abs(got64 - ref) / scale))
+    res["split_bf16x3"]["max_err_rel_to_absAabsB"] = float(np.max(np.abs(got16 - ref) / scale))
+    res["split_bf16x3"]["pipeline_error_flag"] = flag.value
+    peaks = read_peaks()
+    bf16_peak = peaks.get("bf16_tflops", 1917.6)
+    split_tensor_tflops = 6 * 2.0 * n ** 3 / (res["split_bf16x3"]["ms"] * 1e-3) / 1e12
+    return {"metric": "GEMM f64 8192^3 (N(0,1) 2^k scaled rows/columns): split BF16 x3 tensor-core vs native FP64",
+            "value": res["split_bf16x3"]["tflops_fp64_equivalent"], "unit": "TFLOP/s (FP64-equivalent)",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 -> f32 accumulate -> f64", "data": "synthetic",
+            "config": {"workload": "gemm", "m": n, "n": n, "k": n, "slices": 3},
+            "forms": res,
+            "roofline": {"bound": "tensor", "achieved": split_tensor_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": split_tensor_tflops / bf16_peak, "traffic": None,
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
+                         "note": "achieved = 6 BF16 slice products x 2 n^3 / time (includes the split pre-pass)"},
+            "gpu_launches": args.steps * 5}
+
+
 # ----------------------------------------------------------------------------- main
 
 def main():
@@ -599,7 +684,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint"])
+    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=0, help="ragged_cholesky: override the number of systems")
@@ -628,9 +713,9 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
-    if args.workload in ("lu_batched", "ls_qr", "adjoint"):
-        res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours}[args.workload](
-            args, rank, world)
+    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm"):
+        res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
+               "gemm": bench_gemm_ours}[args.workload](args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

@@ -238,6 +238,32 @@ int nacu_dposv_ragged_noalloc(int count, int n_max, const int32_t* ns, const int
                               int nrhs, const int64_t* b_offsets, double* B, int32_t* info, double* logdet,
                               double substitute, int flags, nacu_stream_t stream);
 
+/* ---- GEMM ------------------------------------------------------------------ */
+
+/* C = alpha * A * B + beta * C, FP64, column-major (A m x k, B k x n, C m x n),
+ * `Matrix::gemm` (src/base/blas.rs:729-746, blas_uninit.rs:187-333).
+ * beta == 0: C is never read. */
+int nacu_dgemm(int m, int n, int k, double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
+               double beta, double* C, int64_t ldc, nacu_stream_t stream);
+
+/* Workspace bytes of nacu_dgemm_split_bf16 (BF16 slices of A and B, padded to
+ * the 128 x 256 x 64 tiles, and the row / column exponents). */
+size_t nacu_gemm_split_workspace_bytes(int m, int n, int k);
+
+/* The precision form of nacu_dgemm on the tensor cores: rows of A and columns
+ * of B scaled by powers of two, split into `slices` (1..3) BF16 parts, the
+ * slice products p + q < slices accumulated in FP32 by tcgen05.mma, the result
+ * rescaled and combined with beta * C in FP64.  FP32-class accuracy (3 slices:
+ * ~1e-7 relative to |A||B|).  No reference counterpart (nalgebra's gemm is
+ * FP64 only).  workspace must be 1024-byte aligned. */
+int nacu_dgemm_split_bf16(int m, int n, int k, double alpha, const double* A, int64_t lda, const double* B,
+                          int64_t ldb, double beta, double* C, int64_t ldc, int slices, void* workspace,
+                          size_t workspace_bytes, nacu_stream_t stream);
+
+/* 1 when a split-GEMM kernel gave up waiting on a pipeline barrier (its
+ * results are then invalid), else 0; synchronous. */
+int nacu_split_gemm_error(int* flag_out);
+
 /* ---- measurement helpers ---------------------------------------------------- */
 
 /* FP64 FMA throughput probe: runs a fixed DFMA-chain kernel over the whole GPU
