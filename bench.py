@@ -164,10 +164,11 @@ def bench_ragged_ours(args, rank, world):
     sp = int(stream.cuda_stream)
     n_max = int(ns.max())
 
-    def launch():
+    def launch():  # the stream is read at call time: inside a capture it is the capture stream
         _lib.call("nacu_dposv_ragged", count, n_max, batch._d_rows.data_ptr(), batch._d_off.data_ptr(),
                   A.data_ptr(), nrhs, rhs._d_off.data_ptr(), B.data_ptr(), chol.info.data_ptr(),
-                  chol.logdet.data_ptr(), chol._order.data_ptr(), chol._ws.data_ptr(), chol._ws.numel(), 0.0, 0, sp)
+                  chol.logdet.data_ptr(), chol._order.data_ptr(), chol._ws.data_ptr(), chol._ws.numel(), 0.0, 0,
+                  int(torch.cuda.current_stream().cuda_stream))
 
     def restore():
         A.copy_(a0)
@@ -183,8 +184,11 @@ def bench_ragged_ours(args, rank, world):
         launch()
     stream = torch.cuda.current_stream()
     restore()
+    chol.info.fill_(-7)
     graph.replay()
     torch.cuda.synchronize()
+    if int((chol.info != 0).sum().item()) != 0:
+        raise RuntimeError("graph replay did not run the factorization")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if world > 1:
         torch.distributed.barrier()
@@ -217,8 +221,13 @@ def bench_ragged_ours(args, rank, world):
     x_host = B.cpu().numpy()
     berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample)
 
-    # e2e through the public API from pinned host buffers (H2D in, D2H of X,
-    # info and log-det out), inside the timed region.
+    # precision form: FP32 factor + FP64 refinement, same inputs, one launch
+    mixed = bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host)
+    mchol, mrhs, mout = mixed.pop("_objects")
+    use_mixed = mixed["backward_error_max_over_sample_in_n_eps"] <= 1.0 and mixed["ms_per_step"] < kern_ms
+
+    # e2e through the public API from pinned host buffers (H2D of A and B in,
+    # D2H of X, info and the per-matrix status out), inside the timed region.
     a_pin = torch.empty(a0.numel(), dtype=torch.float64, pin_memory=True)
     b_pin = torch.empty(b0.numel(), dtype=torch.float64, pin_memory=True)
     x_pin = torch.empty(b0.numel(), dtype=torch.float64, pin_memory=True)
@@ -229,13 +238,20 @@ def bench_ragged_ours(args, rank, world):
     e2e_steps = max(1, min(args.steps, 5))
 
     def e2e_step():
-        A.copy_(a_pin, non_blocking=True)
-        B.copy_(b_pin, non_blocking=True)
-        chol.factored = False
-        chol.solve_mut(rhs)
-        x_pin.copy_(B, non_blocking=True)
-        i_pin.copy_(chol.info, non_blocking=True)
-        l_pin.copy_(chol.logdet, non_blocking=True)
+        if use_mixed:  # the mixed form reads A and B in place (read-only) and writes X
+            mchol.batch.data.copy_(a_pin, non_blocking=True)
+            mrhs.data.copy_(b_pin, non_blocking=True)
+            mchol.solve_refined_into(mrhs, mout)
+            x_pin.copy_(mout.data, non_blocking=True)
+            i_pin.copy_(mchol.info[:count], non_blocking=True)
+        else:
+            A.copy_(a_pin, non_blocking=True)
+            B.copy_(b_pin, non_blocking=True)
+            chol.factored = False
+            chol.solve_mut(rhs)
+            x_pin.copy_(B, non_blocking=True)
+            i_pin.copy_(chol.info, non_blocking=True)
+            l_pin.copy_(chol.logdet, non_blocking=True)
 
     e2e_step()
     torch.cuda.synchronize()
@@ -248,7 +264,7 @@ def bench_ragged_ours(args, rank, world):
     torch.cuda.synchronize()
     e2e_ms = t0.elapsed_time(t1) / e2e_steps
     h2d = (a0.numel() + b0.numel()) * 8
-    d2h = b0.numel() * 8 + count * 12
+    d2h = b0.numel() * 8 + count * (4 if use_mixed else 12)
 
     # one plain FP64 launch per matrix (nacu_dposv), on a sample, one stream
     plain_sample = rng.choice(count, size=min(1000, count), replace=False)
@@ -267,15 +283,24 @@ def bench_ragged_ours(args, rank, world):
     plain_solves_per_s = plain_sample.size / (plain_ms * 1e-3)
     plain_flops = ragged_flops(ns[plain_sample], nrhs) / (plain_ms * 1e-3)
 
-    # precision form: FP32 factor + FP64 refinement, same inputs, one launch
-    mixed = bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host)
-
     peak = ctypes_probe(L)
     flops = ragged_flops(ns, nrhs)
     achieved = flops / (kern_ms * 1e-3)
-    value = count * world / (kern_ms * 1e-3)
+    fp64_form = {"solves_per_s": count / (kern_ms * 1e-3), "gflops": achieved / 1e9, "ms_per_step": kern_ms,
+                 "frac_of_fp64_peak": achieved / peak, "backward_error_max_over_sample_in_n_eps": berr}
+    mixed["frac_of_fp64_peak_executed"] = mixed["fp64_flops_executed_per_launch"] / (mixed["ms_per_step"] * 1e-3) / peak
+    head_ms = mixed["ms_per_step"] if use_mixed else kern_ms
+    value = count * world / (head_ms * 1e-3)
+    if use_mixed:
+        roof_achieved = mixed["fp64_flops_executed_per_launch"] / (head_ms * 1e-3)
+        roof_note = ("dominant kernel chol_mixed_kernel: FP64 residual work executed per launch / launch time; "
+                     "the FP32 factor and solves run on the FMA pipe and are latency-bound")
+    else:
+        roof_achieved = achieved
+        roof_note = "dominant kernel chol_ragged_kernel<false>: n^3/3 + 2 nrhs n^2 per system"
+    berr_head = mixed["backward_error_max_over_sample_in_n_eps"] if use_mixed else berr
     res = {
-        "metric": "solves/s at backward err <= n*eps64 (ragged batched Cholesky factor+solve+logdet)",
+        "metric": "solves/s at backward err <= n*eps64 (ragged batched SPD solve, chosen forms vs plain FP64)",
         "value": value,
         "unit": "solves/s",
         "n_gpus": world,
@@ -288,20 +313,23 @@ def bench_ragged_ours(args, rank, world):
         "dtype": "f64",
         "data": "synthetic (seeded; A = B B^T + n I, B ~ N(0,1); 4 RHS ~ N(0,1))",
         "config": {"workload": "ragged_cholesky", "count": count, "n_range": [cfg["n_lo"], cfg["n_hi"]],
-                   "nrhs": nrhs, "form": "batched persistent FP64 (one launch, largest-first work queue)",
+                   "nrhs": nrhs,
+                   "form": ("batched persistent mixed precision (FP32 factor, FP64 refinement), CUDA graph"
+                            if use_mixed else "batched persistent FP64 (one launch, largest-first work queue), CUDA graph"),
                    "l2": "inputs (3.4 GB) larger than L2; input restore outside the timed events",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "gflops": achieved / 1e9,
-        "backward_error_max_over_sample_in_n_eps": berr,
+        "gflops": flops / (head_ms * 1e-3) / 1e9,
+        "backward_error_max_over_sample_in_n_eps": berr_head,
         "forms": {
-            "batched_persistent_fp64": {"solves_per_s": value / world, "gflops": achieved / 1e9},
+            "batched_persistent_fp64": fp64_form,
             "plain_fp64_launch_per_matrix": {"solves_per_s": plain_solves_per_s, "gflops": plain_flops / 1e9,
                                              "sample": int(plain_sample.size)},
             "batched_mixed_fp32_factor_fp64_refined": mixed,
+            "speedup_mixed_vs_fp64_batched": kern_ms / mixed["ms_per_step"],
         },
-        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "peak_source": "FP64 DFMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+        "roofline": {"bound": "fp64", "achieved": roof_achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                     "frac": roof_achieved / peak, "traffic": None, "note": roof_note,
+                     "peak_source": fp64_peak_source(),
                      "algorithmic_bytes_per_launch": ragged_bytes(ns, nrhs),
                      "hbm_frac_of_measured": (ragged_bytes(ns, nrhs) / (kern_ms * 1e-3)) / (read_peaks().get("hbm_gbs", 6794.8) * 1e9)},
         "e2e": {"value": count / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": h2d,
@@ -313,56 +341,87 @@ def bench_ragged_ours(args, rank, world):
 
 
 def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host):
+    """The precision form on the same inputs (A and B read-only, X out), one
+    graph-replayed launch per step."""
     import torch
 
-    from nalgebra_gb300 import _lib
+    from nalgebra_gb300 import DeviceBatch
 
     count = ns.size
-    sp = int(stream.cuda_stream)
-    d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
-    dns, daoff, dboff = d(ns.astype(np.int32)), d(aoff), d(boff)
-    order = d(np.argsort(-ns, kind="stable").astype(np.int32))
-    X = torch.zeros_like(b0)
-    info = torch.zeros(count, dtype=torch.int32, device="cuda")
-    iters = torch.zeros(count, dtype=torch.int32, device="cuda")
-    total = int(a0.numel())
-    ws = torch.empty(L.nacu_mixed_workspace_bytes(count, total), dtype=torch.uint8, device="cuda")
-
-    def launch():
-        _lib.call("nacu_dposv_ragged_mixed", count, int(ns.max()), dns.data_ptr(), daoff.data_ptr(), a0.data_ptr(),
-                  nrhs, dboff.data_ptr(), b0.data_ptr(), X.data_ptr(), info.data_ptr(), iters.data_ptr(),
-                  order.data_ptr(), total, ws.data_ptr(), ws.numel(), 0.0, 0, 0.0, 0, sp)
-
+    batch = DeviceBatch(a0, ns, ns, aoff)
+    rhs = DeviceBatch(b0, ns, np.full(count, nrhs), boff)
+    out = DeviceBatch(torch.zeros_like(b0), ns, np.full(count, nrhs), boff)
+    chol = batch.cholesky()
     for _ in range(args.warmup):
-        launch()
+        chol.solve_refined_into(rhs, out)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        chol.solve_refined_into(rhs, out)
+    out.data.zero_()
+    graph.replay()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
         ev[i][0].record(stream)
-        launch()
+        graph.replay()
         ev[i][1].record(stream)
     torch.cuda.synchronize()
     ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
-    it = iters.cpu().numpy()
-    if np.any(info.cpu().numpy() != 0):
+    it = chol._iters.cpu().numpy()[:count]
+    if np.any(chol.info.cpu().numpy()[:count] != 0):
         raise RuntimeError("mixed form: systems reported not SPD")
     rng = np.random.default_rng(2)
     sample = rng.choice(count, size=min(48, count), replace=False)
-    berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, X.cpu().numpy(), nrhs, sample)
+    berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, out.data.cpu().numpy(), nrhs, sample)
+    n = ns.astype(np.float64)
+    fp64_flops = float(np.sum(np.abs(it) * 2.0 * nrhs * n * n))  # FP64 residual work actually executed
     return {"solves_per_s": count / (ms * 1e-3), "ms_per_step": ms,
             "gflops_fp64_equivalent": ragged_flops(ns, nrhs) / (ms * 1e-3) / 1e9,
+            "fp64_flops_executed_per_launch": fp64_flops,
             "residuals_per_system_mean": float(np.mean(np.abs(it))), "fp64_fallbacks": int(np.sum(it < 0)),
-            "backward_error_max_over_sample_in_n_eps": berr}
+            "backward_error_max_over_sample_in_n_eps": berr, "_objects": (chol, rhs, out)}
+
+
+_FP64_PEAK = {}
 
 
 def ctypes_probe(L):
+    """FP64 roofline denominator: the best of a cuBLAS DGEMM (torch.matmul on
+    float64, 8192^3, best of 2 -- the FP64 counterpart of the cuBLAS BF16 figure
+    in MEASURED_PEAKS.json) and the library's DFMA probe, both measured in this
+    run.  Cached per process."""
+    if "value" in _FP64_PEAK:
+        return _FP64_PEAK["value"]
     import ctypes
+
+    import torch
 
     v = ctypes.c_double(0.0)
     rc = L.nacu_probe_fp64_peak(ctypes.byref(v))
     if rc != 0:
         raise RuntimeError("FP64 probe failed")
-    return v.value
+    n = 8192
+    a = torch.randn((n, n), dtype=torch.float64, device="cuda")
+    b = torch.randn((n, n), dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3))
+    _FP64_PEAK.update(value=max(best, v.value), cublas_dgemm=best, dfma_probe=v.value)
+    return _FP64_PEAK["value"]
+
+
+def fp64_peak_source():
+    return ("FP64: max of cuBLAS DGEMM 8192^3 (%.3f TFLOP/s) and the DFMA probe (%.3f TFLOP/s), measured in this "
+            "run; MEASURED_PEAKS.json has no FP64 figure" % (_FP64_PEAK.get("cublas_dgemm", 0) / 1e12,
+                                                             _FP64_PEAK.get("dfma_probe", 0) / 1e12))
 
 
 def cpu_baseline_ragged(data, max_seconds=20.0):
@@ -409,7 +468,7 @@ def bench_ragged_reference(args, rank, world):
     value = k / dt
     return {
         "impl": "reference",
-        "metric": "solves/s at backward err <= n*eps64 (ragged batched Cholesky factor+solve+logdet)",
+        "metric": "solves/s at backward err <= n*eps64 (ragged batched SPD solve, chosen forms vs plain FP64)",
         "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded; A = B B^T + n I, B ~ N(0,1); 4 RHS ~ N(0,1))",
@@ -467,7 +526,8 @@ def bench_lu_ours(args, rank, world):
                                             "l2": "256 MB flush between steps"},
             "gflops": flops / (ms * 1e-3) / 1e9,
             "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak / 1e12,
-                         "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / peak, "traffic": None},
+                         "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / peak, "traffic": None,
+                         "peak_source": fp64_peak_source()},
             "gpu_launches": args.steps, "clocks": clk.summary()}
 
 
@@ -525,7 +585,8 @@ def bench_ls_ours(args, rank, world):
             "config": {"workload": "ls_qr", "count": count, "m_range": [128, 512], "n": n},
             "gflops": flops / (ms_step * 1e-3) / 1e9,
             "roofline": {"bound": "fp64", "achieved": flops / (ms_step * 1e-3) / 1e12, "peak": peak / 1e12,
-                         "unit": "TFLOP/s", "frac": flops / (ms_step * 1e-3) / peak, "traffic": None},
+                         "unit": "TFLOP/s", "frac": flops / (ms_step * 1e-3) / peak, "traffic": None,
+                         "peak_source": fp64_peak_source()},
             "gpu_launches": args.steps, "clocks": clk.summary()}
 
 

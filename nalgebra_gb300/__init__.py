@@ -373,6 +373,36 @@ class CholeskyBatch:
         self.factor()
         return self.logdet.cpu().numpy()
 
+    def solve_refined_into(self, rhs: DeviceBatch, out: DeviceBatch, tol_units: float = 1.0, max_iter: int = 0,
+                           verify: bool = False):
+        """The precision form (nacu_dposv_ragged_mixed): FP32 factor, FP64
+        iterative refinement to backward error <= tol_units * n * eps64, FP64
+        fallback per matrix.  The batch's matrices and ``rhs`` are left
+        unchanged; solutions go to ``out`` (same layout as ``rhs``).  Returns the
+        device per-matrix residual counts (negative: FP64 fallback used)."""
+        torch = _torch()
+        b = self.batch
+        nrhs = int(rhs.ncols[0]) if len(rhs) else 0
+        if not hasattr(self, "_mws"):
+            total = int(b.data.numel())
+            self._mws = torch.empty(_lib.load().nacu_mixed_workspace_bytes(len(b), total), dtype=torch.uint8,
+                                    device="cuda")
+            self._iters = torch.zeros(max(len(b), 1), dtype=torch.int32, device="cuda")
+        flags = self.flags & FLAG_SUBSTITUTE
+        if verify:
+            flags |= _lib.FLAG_VERIFY
+        _lib.call("nacu_dposv_ragged_mixed", len(b), self.n_max, b._d_rows.data_ptr(), b._d_off.data_ptr(),
+                  b.data.data_ptr(), nrhs, rhs._d_off.data_ptr(), rhs.data.data_ptr(), out.data.data_ptr(),
+                  self.info.data_ptr(), self._iters.data_ptr(), self._order.data_ptr(), int(b.data.numel()),
+                  self._mws.data_ptr(), self._mws.numel(), float(tol_units), int(max_iter), self.substitute, flags,
+                  _stream_ptr())
+        return self._iters
+
+    def solve_refined(self, rhs: DeviceBatch, **kw) -> DeviceBatch:
+        out = rhs.clone_owned()
+        self.solve_refined_into(rhs, out, **kw)
+        return out
+
     def is_ok(self) -> np.ndarray:
         """Per matrix: True where nalgebra's ``cholesky()`` returns Some."""
         self.factor()

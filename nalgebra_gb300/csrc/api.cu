@@ -24,23 +24,22 @@ namespace {
 
 __device__ double g_probe_sink;
 
-// Eight independent DFMA chains per thread; the result is stored only when it
-// equals an impossible value, so the chains are live but nothing is written.
-__global__ void fp64_probe_kernel(int iters, double s) {
-  double a0 = threadIdx.x * 1e-3, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
-  double a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+// Sixteen independent DFMA chains per thread, two warps per SM sub-partition
+// (the FP64 unit needs little latency hiding but every issue slot must carry a
+// DFMA); the result is stored only when it equals an impossible value, so the
+// chains are live but nothing is written.
+__global__ void __launch_bounds__(256) fp64_probe_kernel(int iters, double s) {
+  double a[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) a[i] = threadIdx.x * 1e-3 + i;
   const double m = 0.999999;
-  for (int i = 0; i < iters; ++i) {
-    a0 = fma(a0, m, s);
-    a1 = fma(a1, m, s);
-    a2 = fma(a2, m, s);
-    a3 = fma(a3, m, s);
-    a4 = fma(a4, m, s);
-    a5 = fma(a5, m, s);
-    a6 = fma(a6, m, s);
-    a7 = fma(a7, m, s);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) a[i] = fma(a[i], m, s);
   }
-  const double r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  double r = 0.0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) r += a[i];
   if (r == -12345.678) g_probe_sink = r;
 }
 
@@ -64,7 +63,7 @@ int nacu_device_arch(void) {
 int nacu_probe_fp64_peak(double* flops) {
   using namespace nacu;
   if (!flops) return record_arg_error(-1, "probe_fp64_peak: null output");
-  const int blocks = sm_count() * 8, threads = 256, iters = 4000;
+  const int blocks = sm_count() * 2, threads = 256, iters = 4000;
   cudaEvent_t e0, e1;
   cudaError_t e = cudaEventCreate(&e0);
   if (e != cudaSuccess) return record_cuda_error(e, "probe_fp64_peak");
@@ -82,7 +81,7 @@ int nacu_probe_fp64_peak(double* flops) {
     }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    const double f = 2.0 * 8.0 * (double)blocks * threads * iters / (ms * 1e-3);
+    const double f = 2.0 * 16.0 * (double)blocks * threads * iters / (ms * 1e-3);
     if (rep > 0 && f > best) best = f;
   }
   cudaEventDestroy(e0);
