@@ -238,6 +238,41 @@ int nacu_dposv_ragged_noalloc(int count, int n_max, const int32_t* ns, const int
                               int nrhs, const int64_t* b_offsets, double* B, int32_t* info, double* logdet,
                               double substitute, int flags, nacu_stream_t stream);
 
+/* ---- LU of one large matrix (blocked, multi-SM) ---------------------------- */
+
+/* Workspace bytes of nacu_dgetrf (panel pivot candidates). */
+size_t nacu_getrf_workspace_bytes(int n);
+
+/* LU with partial pivoting of one n x n matrix (column-major, lda), in place,
+ * nalgebra's packed L\U with per-step pivots ipiv[0..n) (src/linalg/lu.rs:93-122;
+ * icamax rule src/base/min_max.rs:221-240; a zero column is skipped,
+ * lu.rs:107-110).  *info (device) = 0, or the first skipped column + 1. */
+int nacu_dgetrf(int n, double* A, int64_t lda, int32_t* ipiv, int32_t* info, void* workspace, size_t workspace_bytes,
+                nacu_stream_t stream);
+
+/* Solve A x = b in place in b from nacu_dgetrf factors
+ * (src/linalg/lu.rs:242-260); *info = first zero U_kk + 1, or 0. */
+int nacu_dgetrs(int n, const double* LU, int64_t lda, const int32_t* ipiv, double* b, int32_t* info,
+                nacu_stream_t stream);
+
+/* Workspace bytes of nacu_dgesv_mixed_ir (FP32 copy of A, split-GEMM slices,
+ * vectors, and an FP64 copy of A for the fallback). */
+size_t nacu_gesv_mixed_workspace_bytes(int n);
+
+/* Mixed-precision solve of one large system A x = b (A, b read-only, FP64):
+ * FP32 LU with partial pivoting (BF16-split tensor-core trailing updates),
+ * then FP64 iterative refinement r = b - A x, x += (LU)^-1 r until the normwise
+ * backward error ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol_units * n *
+ * eps64 (tol_units <= 0: 1), at most max_iter steps (<= 0: 30); when FP32 cannot
+ * factor A or the refinement stagnates, A is refactored in FP64 (fallback).
+ * Synchronous: *iters_out, *berr_out, *fallback_out are host values.  No
+ * reference counterpart (nalgebra has no mixed precision); it replaces
+ * `m.lu().solve(&b)` (src/linalg/lu.rs:93-122, 221-260) when an FP64-accurate
+ * solution, not the factor, is wanted. */
+int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, double* x, double tol_units,
+                        int max_iter, int* iters_out, double* berr_out, int* fallback_out, void* workspace,
+                        size_t workspace_bytes, nacu_stream_t stream);
+
 /* ---- GEMM ------------------------------------------------------------------ */
 
 /* C = alpha * A * B + beta * C, FP64, column-major (A m x k, B k x n, C m x n),

@@ -52,6 +52,12 @@ SIGNATURES = {
     "nacu_sposv_logdet_backward": (_i, [_i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "nacu_qr_workspace_bytes": (_sz, [_i]),
     "nacu_dgels_batched": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
+    "nacu_getrf_workspace_bytes": (_sz, [_i]),
+    "nacu_dgetrf": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _sz, _vp]),
+    "nacu_dgetrs": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp]),
+    "nacu_gesv_mixed_workspace_bytes": (_sz, [_i]),
+    "nacu_dgesv_mixed_ir": (_i, [_i, _vp, _i64, _vp, _vp, _d, _i, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_int), _vp, _sz, _vp]),
     "nacu_dgemm": (_i, [_i, _i, _i, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64, _vp]),
     "nacu_gemm_split_workspace_bytes": (_sz, [_i, _i, _i]),
     "nacu_dgemm_split_bf16": (_i, [_i, _i, _i, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64, _i, _vp, _sz, _vp]),

@@ -7,6 +7,11 @@
 
 namespace nacu {
 
+// BF16-split tensor-core GEMM (gemm_split.cu): C = alpha A B + beta C.
+template <typename TI, typename TO>
+int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, const TI* B, int64_t ldb, double beta,
+                   TO* C, int64_t ldc, int slices, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
 // Records a CUDA error (from a launch or a runtime call) for nacu_last_error().
 int record_cuda_error(cudaError_t e, const char* where);
 // Records an argument error message; returns `code`.

@@ -116,25 +116,27 @@ __device__ __forceinline__ double pow2(int e) { return __longlong_as_double((lon
 __device__ __forceinline__ int scale_exp(int e) { return (e < -1100) ? 0 : max(min(e, 1000), -1000); }
 
 // Per-row max exponent of A (column-major m x k), atomicMax into rexp (init INT_MIN).
-__global__ void row_exp_kernel(int m, int k, const double* __restrict__ A, int64_t lda, int* __restrict__ rexp) {
+template <typename TI>
+__global__ void row_exp_kernel(int m, int k, const TI* __restrict__ A, int64_t lda, int* __restrict__ rexp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const int c0 = blockIdx.y * 256, c1 = min(k, c0 + 256);
   int e = INT_MIN;
   for (int c = c0; c < c1; ++c) {
-    const double v = A[(size_t)c * lda + i];
+    const double v = (double)A[(size_t)c * lda + i];
     if (v != 0.0) e = max(e, exp_of(v));
   }
   if (e != INT_MIN) atomicMax(&rexp[i], e);
 }
 // Per-column max exponent of B (column-major k x n): one warp per column.
-__global__ void col_exp_kernel(int k, int n, const double* __restrict__ B, int64_t ldb, int* __restrict__ cexp) {
+template <typename TI>
+__global__ void col_exp_kernel(int k, int n, const TI* __restrict__ B, int64_t ldb, int* __restrict__ cexp) {
   const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (j >= n) return;
   int e = INT_MIN;
   for (int r = lane; r < k; r += 32) {
-    const double v = B[(size_t)j * ldb + r];
+    const double v = (double)B[(size_t)j * ldb + r];
     if (v != 0.0) e = max(e, exp_of(v));
   }
 #pragma unroll
@@ -155,7 +157,8 @@ __device__ __forceinline__ void split3(double v, int slices, __nv_bfloat16* out)
 
 // A (m x k column-major) -> slices [s][mp][kp] (row-major: K contiguous),
 // zero padded; 32 x 32 tiles transposed through shared memory.
-__global__ void split_a_kernel(int m, int k, const double* __restrict__ A, int64_t lda, const int* __restrict__ rexp,
+template <typename TI>
+__global__ void split_a_kernel(int m, int k, const TI* __restrict__ A, int64_t lda, const int* __restrict__ rexp,
                                int mp, int kp, int slices, __nv_bfloat16* __restrict__ out) {
   __shared__ double t[32][33];
   const int i0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
@@ -163,7 +166,7 @@ __global__ void split_a_kernel(int m, int k, const double* __restrict__ A, int64
   for (int r = ty; r < 32; r += 8) {
     const int i = i0 + tx, c = c0 + r;
     double v = 0.0;
-    if (i < m && c < k) v = A[(size_t)c * lda + i] * pow2(-scale_exp(rexp[i]));
+    if (i < m && c < k) v = (double)A[(size_t)c * lda + i] * pow2(-scale_exp(rexp[i]));
     t[r][tx] = v;  // t[k][m]
   }
   __syncthreads();
@@ -175,12 +178,13 @@ __global__ void split_a_kernel(int m, int k, const double* __restrict__ A, int64
   }
 }
 // B (k x n column-major: column j contiguous over K) -> slices [s][np][kp].
-__global__ void split_b_kernel(int k, int n, const double* __restrict__ B, int64_t ldb, const int* __restrict__ cexp,
+template <typename TI>
+__global__ void split_b_kernel(int k, int n, const TI* __restrict__ B, int64_t ldb, const int* __restrict__ cexp,
                                int np, int kp, int slices, __nv_bfloat16* __restrict__ out) {
   const int j = blockIdx.y;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < kp; c += gridDim.x * blockDim.x) {
     double v = 0.0;
-    if (j < n && c < k) v = B[(size_t)j * ldb + c] * pow2(-scale_exp(cexp[j]));
+    if (j < n && c < k) v = (double)B[(size_t)j * ldb + c] * pow2(-scale_exp(cexp[j]));
     __nv_bfloat16 h[3];
     split3(v, slices, h);
     for (int s = 0; s < 3; ++s) out[((size_t)s * np + j) * kp + c] = h[s];
@@ -194,12 +198,13 @@ struct SplitArgs {
   int npairs;
   int pa[6], pb[6];  // slice pairs
   double alpha, beta;
-  double* C;
+  void* C;
   int64_t ldc;
   const int* rexp;
   const int* cexp;
 };
 
+template <typename TO>
 __global__ void __launch_bounds__(kSplitThreads, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                       const SplitArgs g) {
@@ -284,9 +289,14 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     for (int j = 0; j < 16; ++j) {
       const int col = n0 + c0 + j;
       if (col < g.n) {
-        const double val = (double)__uint_as_float(v[j]) * srow * pow2(scale_exp(g.cexp[col]));
-        double* cp = g.C + (size_t)col * g.ldc + row;
-        *cp = (g.beta == 0.0) ? g.alpha * val : fma(g.alpha, val, g.beta * *cp);
+        TO* cp = static_cast<TO*>(g.C) + (size_t)col * g.ldc + row;
+        if constexpr (sizeof(TO) == 8) {
+          const double val = (double)__uint_as_float(v[j]) * srow * pow2(scale_exp(g.cexp[col]));
+          *cp = (g.beta == 0.0) ? g.alpha * val : fma(g.alpha, val, g.beta * *cp);
+        } else {  // FP32 output: scale and combine in FP32 (no FP64 instructions)
+          const float val = __uint_as_float(v[j]) * (float)srow * (float)pow2(scale_exp(g.cexp[col]));
+          *cp = (g.beta == 0.0) ? (float)g.alpha * val : fmaf((float)g.alpha, val, (float)g.beta * *cp);
+        }
       }
     }
   }
@@ -359,10 +369,13 @@ int nacu_split_gemm_error(int* flag_out) {
   return NACU_SUCCESS;
 }
 
-int nacu_dgemm_split_bf16(int m, int n, int k, double alpha, const double* A, int64_t lda, const double* B,
-                          int64_t ldb, double beta, double* C, int64_t ldc, int slices, void* workspace,
-                          size_t workspace_bytes, nacu_stream_t stream) {
-  using namespace nacu;
+}  // extern "C"
+
+namespace nacu {
+
+template <typename TI, typename TO>
+int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, const TI* B, int64_t ldb, double beta,
+                   TO* C, int64_t ldc, int slices, void* workspace, size_t workspace_bytes, cudaStream_t stream) {
   if (m < 0) return record_arg_error(-1, "dgemm_split_bf16: m < 0");
   if (n < 0) return record_arg_error(-2, "dgemm_split_bf16: n < 0");
   if (k < 0) return record_arg_error(-3, "dgemm_split_bf16: k < 0");
@@ -375,7 +388,7 @@ int nacu_dgemm_split_bf16(int m, int n, int k, double alpha, const double* A, in
   if (!workspace || workspace_bytes < L.total) return record_arg_error(-13, "dgemm_split_bf16: workspace too small");
   if ((reinterpret_cast<uintptr_t>(workspace) & 1023) != 0)
     return record_arg_error(-13, "dgemm_split_bf16: workspace must be 1024-byte aligned");
-  cudaStream_t s = (cudaStream_t)stream;
+  cudaStream_t s = stream;
   unsigned char* ws = static_cast<unsigned char*>(workspace);
   __nv_bfloat16* as = reinterpret_cast<__nv_bfloat16*>(ws + L.a_off);
   __nv_bfloat16* bs = reinterpret_cast<__nv_bfloat16*>(ws + L.b_off);
@@ -387,10 +400,10 @@ int nacu_dgemm_split_bf16(int m, int n, int k, double alpha, const double* A, in
   if (e == cudaSuccess) e = cudaMemsetAsync(rexp, 0x80, (size_t)L.mp * 4, s);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgemm_split_bf16");
   if (k > 0) {
-    row_exp_kernel<<<dim3((m + 255) / 256, (k + 255) / 256), 256, 0, s>>>(m, k, A, lda, rexp);
-    col_exp_kernel<<<(n + 7) / 8, 256, 0, s>>>(k, n, B, ldb, cexp);
-    split_a_kernel<<<dim3((k + 31) / 32, (m + 31) / 32), 256, 0, s>>>(m, k, A, lda, rexp, L.mp, L.kp, slices, as);
-    split_b_kernel<<<dim3((L.kp + 255) / 256, n), 256, 0, s>>>(k, n, B, ldb, cexp, L.np, L.kp, slices, bs);
+    row_exp_kernel<TI><<<dim3((m + 255) / 256, (k + 255) / 256), 256, 0, s>>>(m, k, A, lda, rexp);
+    col_exp_kernel<TI><<<(n + 7) / 8, 256, 0, s>>>(k, n, B, ldb, cexp);
+    split_a_kernel<TI><<<dim3((k + 31) / 32, (m + 31) / 32), 256, 0, s>>>(m, k, A, lda, rexp, L.mp, L.kp, slices, as);
+    split_b_kernel<TI><<<dim3((L.kp + 255) / 256, n), 256, 0, s>>>(k, n, B, ldb, cexp, L.np, L.kp, slices, bs);
     int rc = check_launch("nacu_dgemm_split_bf16: split");
     if (rc != NACU_SUCCESS) return rc;
   } else {
@@ -424,13 +437,27 @@ int nacu_dgemm_split_bf16(int m, int n, int k, double alpha, const double* A, in
   g.rexp = rexp;
   g.cexp = cexp;
   const size_t smem = (size_t)kStages * kStageBytes + 1024;
-  e = cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = cudaFuncSetAttribute(split_gemm_kernel<TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgemm_split_bf16");
   dim3 grid(L.mp / kTM, L.np / kTN);
-  if (g.npairs == 0)  // k == 0: C = beta * C, the FP64 GEMM's k = 0 path
-    return nacu_dgemm(m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc, stream);
-  split_gemm_kernel<<<grid, kSplitThreads, smem, s>>>(mapA, mapB, g);
+  if (g.npairs == 0) {  // k == 0: C = beta * C
+    if constexpr (sizeof(TO) == 8)
+      return nacu_dgemm(m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc, stream);
+    else
+      return record_arg_error(-3, "split gemm: k == 0 is not supported for FP32 output");
+  }
+  split_gemm_kernel<TO><<<grid, kSplitThreads, smem, s>>>(mapA, mapB, g);
   return check_launch("nacu_dgemm_split_bf16");
 }
 
-}  // extern "C"
+
+template int split_gemm_run<float, float>(int, int, int, double, const float*, int64_t, const float*, int64_t,
+                                           double, float*, int64_t, int, void*, size_t, cudaStream_t);
+}  // namespace nacu
+
+extern "C" int nacu_dgemm_split_bf16(int m, int n, int k, double alpha, const double* A, int64_t lda, const double* B,
+                                     int64_t ldb, double beta, double* C, int64_t ldc, int slices, void* workspace,
+                                     size_t workspace_bytes, nacu_stream_t stream) {
+  return nacu::split_gemm_run<double, double>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, workspace,
+                                              workspace_bytes, (cudaStream_t)stream);
+}

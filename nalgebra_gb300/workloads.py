@@ -10,6 +10,9 @@ column-major (each one packed as nalgebra's VecStorage would hold it).
   ragged_spd    : SPD matrices with n ~ U{n_lo..n_hi}, A = B B^T + n I,
                   B ~ N(0,1), nrhs right-hand sides ~ N(0,1)
                   (20000 matrices, n in [8, 256], 4 RHS)
+  conditioned   : one dense system A = U diag(s) V^T, U, V orthogonal (QR of
+                  N(0,1)), s log-uniform between 1 and 1/cond (cond 1e2, 1e5,
+                  1e8; n = 4096, 8192), b ~ N(0,1)
 """
 from __future__ import annotations
 
@@ -111,3 +114,36 @@ def spd_uniform(count: int, n: int, seed: int = 0, dtype=np.float64):
     b = rng.standard_normal((count, n))
     w = rng.standard_normal((count, n))
     return (np.ascontiguousarray(a.reshape(count, n * n)).astype(dtype), b.astype(dtype), w.astype(dtype))
+
+
+def _sigma(n: int, cond: float, rng) -> np.ndarray:
+    u = rng.uniform(0.0, 1.0, n)
+    u[0], u[-1] = 0.0, 1.0  # the extremes pin the condition number exactly
+    return cond ** (-u)
+
+
+def conditioned(n: int, cond: float, seed: int = 0):
+    """(A column-major as an (n, n) Fortran array, b): A = U diag(s) V^T with
+    U, V the Q factors of N(0,1) matrices and s log-uniform in [1/cond, 1]."""
+    rng = np.random.default_rng(seed)
+    u, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    v, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = _sigma(n, cond, rng)
+    a = (u * s) @ v.T
+    b = rng.standard_normal(n)
+    return np.asfortranarray(a), b
+
+
+def conditioned_torch(n: int, cond: float, seed: int = 0, device="cuda"):
+    """The same distribution as `conditioned`, generated on the device (the
+    QR factorizations of an 8192 x 8192 matrix are minutes on the host).
+    Returns (A as a column-major flat FP64 device tensor, b device tensor)."""
+    import torch
+
+    g = torch.Generator(device=device).manual_seed(seed)
+    u, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device=device, generator=g))
+    v, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device=device, generator=g))
+    s = torch.from_numpy(_sigma(n, cond, np.random.default_rng(seed))).to(device)
+    a = (u * s) @ v.T
+    b = torch.randn(n, dtype=torch.float64, device=device, generator=g)
+    return a.t().contiguous().reshape(-1), b  # a.t() row-major == a column-major

@@ -1,0 +1,95 @@
+"""GPU checks of the mixed-precision large solve (FP32 LU with BF16-split
+tensor-core trailing updates, FP64 iterative refinement, FP64 fallback) on
+A = U diag(s) V^T systems of prescribed condition: backward error
+||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= n eps64 (recomputed
+on the host), forward error against the oracle's FP64 LU solve within
+cond * n * eps64, and the fallback taken where FP32 cannot converge
+(u32 * cond > 1) or cannot factor at all."""
+import numpy as np
+import pytest
+
+import oracle as O
+from nalgebra_gb300 import _lib, workloads
+from tests.conftest import EPS64
+
+pytestmark = pytest.mark.gpu
+
+
+def _berr(a, x, b):
+    r = b - a @ x
+    return np.abs(r).max() / (np.abs(a).sum(axis=1).max() * np.abs(x).max() + np.abs(b).max())
+
+
+def _solve(cuda, a, b, tol_units=1.0, max_iter=30):
+    import ctypes as C
+
+    torch = cuda
+    n = a.shape[0]
+    A = torch.from_numpy(np.asfortranarray(a).ravel(order="F")).cuda()
+    B = torch.from_numpy(np.ascontiguousarray(b)).cuda()
+    X = torch.full((n,), np.nan, dtype=torch.float64, device="cuda")
+    L = _lib.load()
+    ws = torch.empty(L.nacu_gesv_mixed_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    it, berr, fb = C.c_int(-1), C.c_double(-1.0), C.c_int(-1)
+    s = torch.cuda.current_stream().cuda_stream
+    _lib.call("nacu_dgesv_mixed_ir", n, A.data_ptr(), n, B.data_ptr(), X.data_ptr(), tol_units, max_iter,
+              C.byref(it), C.byref(berr), C.byref(fb), ws.data_ptr(), ws.numel(), s)
+    torch.cuda.synchronize()
+    assert np.array_equal(A.cpu().numpy(), np.asfortranarray(a).ravel(order="F")), "A must stay unchanged"
+    return X.cpu().numpy(), it.value, berr.value, fb.value
+
+
+@pytest.mark.parametrize("n,cond", [(256, 1e2), (640, 1e2), (1000, 1e5), (1536, 1e5), (777, 1e3)])
+def test_refined_solution_meets_backward_error(cuda, n, cond):
+    a, b = workloads.conditioned(n, cond, seed=n)
+    x, iters, berr, fb = _solve(cuda, a, b)
+    assert fb == 0, "FP32 refinement should converge at u32 * cond < 1"
+    assert 1 <= iters <= 10
+    host_berr = _berr(a, x, b)
+    assert host_berr <= n * EPS64
+    assert berr <= n * EPS64
+    lu_o, ipiv_o, _ = O.lu(a)
+    x_o = O.lu_solve(lu_o, ipiv_o, b)
+    assert np.abs(x - x_o).max() <= cond * n * EPS64 * np.abs(x_o).max()
+
+
+def test_ill_conditioned_falls_back_to_fp64(cuda):
+    n, cond = 512, 1e8
+    a, b = workloads.conditioned(n, cond, seed=5)
+    x, iters, berr, fb = _solve(cuda, a, b)
+    assert fb == 1
+    assert _berr(a, x, b) <= n * EPS64
+
+
+def test_fp32_singular_matrix_falls_back(cuda):
+    # entries below FP32's smallest subnormal in one column: FP32 sees a zero
+    # column (info > 0) while FP64 factors the matrix
+    n = 300
+    rng = np.random.default_rng(11)
+    a = rng.standard_normal((n, n))
+    a[:, 17] *= 1e-60
+    b = rng.standard_normal(n)
+    x, iters, berr, fb = _solve(cuda, a, b)
+    assert fb == 1 and iters == 0
+    assert _berr(a, x, b) <= n * EPS64
+
+
+def test_tolerance_and_iteration_cap(cuda):
+    n = 400
+    a, b = workloads.conditioned(n, 1e4, seed=3)
+    # one step cannot reach 1e-3 n eps: with max_iter = 1 the driver falls back
+    x, iters, berr, fb = _solve(cuda, a, b, tol_units=1e-3, max_iter=1)
+    assert iters == 1 and fb == 1
+    x2, iters2, berr2, fb2 = _solve(cuda, a, b, tol_units=100.0)
+    assert fb2 == 0 and berr2 <= 100 * n * EPS64
+
+
+def test_argument_errors(cuda):
+    L = _lib.load()
+    assert L.nacu_dgesv_mixed_ir(-1, None, 1, None, None, 1.0, 5, None, None, None, None, 0, None) == -1
+    torch = cuda
+    A = torch.zeros(16, dtype=torch.float64, device="cuda")
+    ws = torch.empty(16, dtype=torch.uint8, device="cuda")
+    rc = L.nacu_dgesv_mixed_ir(4, A.data_ptr(), 4, A.data_ptr(), A.data_ptr(), 1.0, 5, None, None, None,
+                               ws.data_ptr(), ws.numel(), None)
+    assert rc == -11
