@@ -737,6 +737,90 @@ def bench_gemm_ours(args, rank, world):
             "gpu_launches": args.steps * 5}
 
 
+# ----------------------------------------------------------------------------- mixed LU + refinement
+
+def bench_mixed_lu_ours(args, rank, world):
+    """One dense f64 system at n = 4096 and 8192 (or --count n), A = U diag(s) V^T
+    with cond 1e2, 1e5, 1e8, one RHS: plain FP64 blocked LU + solve
+    (nacu_dgetrf + nacu_dgetrs) vs the mixed form (nacu_dgesv_mixed_ir: FP32 LU
+    with BF16-split tensor-core trailing updates, FP64 refinement to backward
+    error <= n eps64, FP64 fallback).  Work is counted as the FP64-equivalent
+    2/3 n^3 + 2 n^2 per solve."""
+    import ctypes
+
+    import torch
+
+    from nalgebra_gb300 import _lib, workloads
+
+    L = _lib.load()
+    sizes = [args.count] if args.count else [4096, 8192]
+    conds = [1e2, 1e5, 1e8]
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    forms = {}
+    headline = None
+    for n in sizes:
+        wsm = torch.empty(L.nacu_gesv_mixed_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+        wsf = torch.empty(L.nacu_getrf_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+        work = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        x = torch.empty(n, dtype=torch.float64, device="cuda")
+        ipiv = torch.empty(n, dtype=torch.int32, device="cuda")
+        info = torch.empty(4, dtype=torch.int32, device="cuda")
+        flops = 2.0 / 3.0 * n ** 3 + 2.0 * n ** 2
+        for cond in conds:
+            A, b = workloads.conditioned_torch(n, cond, seed=int(np.log10(cond)) + n)
+            it, berr, fb = ctypes.c_int(0), ctypes.c_double(0.0), ctypes.c_int(0)
+
+            def mixed():
+                _lib.call("nacu_dgesv_mixed_ir", n, A.data_ptr(), n, b.data_ptr(), x.data_ptr(), 1.0, 30,
+                          ctypes.byref(it), ctypes.byref(berr), ctypes.byref(fb), wsm.data_ptr(), wsm.numel(), sp)
+
+            def plain():
+                _lib.call("nacu_dgetrf", n, work.data_ptr(), n, ipiv.data_ptr(), info.data_ptr(), wsf.data_ptr(),
+                          wsf.numel(), sp)
+                x.copy_(b)
+                _lib.call("nacu_dgetrs", n, work.data_ptr(), n, ipiv.data_ptr(), x.data_ptr(), info[1:].data_ptr(),
+                          wsf.data_ptr(), wsf.numel(), sp)
+
+            res = {}
+            steps = max(1, args.steps if n <= 4096 else min(args.steps, 3))
+            for name, fn in (("mixed_ir", mixed), ("fp64", plain)):
+                times = []
+                with ClockSampler(torch.cuda.current_device()) as clk:
+                    for i in range(max(1, min(args.warmup, 2)) + steps):
+                        work.copy_(A)  # the plain form factors in place; the mixed form reads A only
+                        torch.cuda.synchronize()
+                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        e0.record(stream)
+                        fn()
+                        e1.record(stream)
+                        torch.cuda.synchronize()
+                        if i >= max(1, min(args.warmup, 2)):
+                            times.append(e0.elapsed_time(e1))
+                ms = float(np.median(times))
+                xr = x.clone()
+                r = b - (A.view(n, n).t() @ xr)
+                be = float(r.abs().max() / (A.view(n, n).abs().sum(dim=0).max() * xr.abs().max() + b.abs().max()))
+                res[name] = {"ms": ms, "solves_per_s": 1e3 / ms, "gflops_fp64_equivalent": flops / (ms * 1e-3) / 1e9,
+                             "backward_error": be, "backward_error_over_n_eps": be / (n * 2.220446049250313e-16),
+                             "clocks": clk.summary()}
+                if name == "mixed_ir":
+                    res[name].update({"refinement_steps": it.value, "fp64_fallback": bool(fb.value)})
+            res["speedup_mixed_over_fp64"] = res["fp64"]["ms"] / res["mixed_ir"]["ms"]
+            forms[f"n{n}_cond{cond:.0e}"] = res
+            if headline is None or (n == max(sizes) and cond == 1e5):
+                headline = (n, cond, res)
+            del A, b
+    n, cond, res = headline
+    return {"metric": "mixed-precision LU + FP64 refinement (backward error <= n eps64) vs plain FP64 GPU LU",
+            "value": res["mixed_ir"]["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 factor (bf16x3 tensor-core updates) + f64 refinement", "data": "synthetic",
+            "config": {"workload": "mixed_lu", "n": n, "cond": cond, "nrhs": 1, "sizes": sizes,
+                       "conds": conds, "inputs": "A = U diag(s) V^T, U, V from QR of N(0,1), s log-uniform"},
+            "forms": forms, "gpu_launches": None}
+
+
 # ----------------------------------------------------------------------------- main
 
 def main():
@@ -745,7 +829,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm"])
+    ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
+                                                                  "mixed_lu"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=0, help="ragged_cholesky: override the number of systems")
@@ -774,9 +859,9 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
-    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm"):
+    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu"):
         res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
-               "gemm": bench_gemm_ours}[args.workload](args, rank, world)
+               "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours}[args.workload](args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

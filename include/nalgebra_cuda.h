@@ -240,7 +240,8 @@ int nacu_dposv_ragged_noalloc(int count, int n_max, const int32_t* ns, const int
 
 /* ---- LU of one large matrix (blocked, multi-SM) ---------------------------- */
 
-/* Workspace bytes of nacu_dgetrf (panel pivot candidates). */
+/* Workspace bytes of nacu_dgetrf and nacu_dgetrs (the panel's pivot exchange
+ * area; the triangular solves' block flags). */
 size_t nacu_getrf_workspace_bytes(int n);
 
 /* LU with partial pivoting of one n x n matrix (column-major, lda), in place,
@@ -251,9 +252,12 @@ int nacu_dgetrf(int n, double* A, int64_t lda, int32_t* ipiv, int32_t* info, voi
                 nacu_stream_t stream);
 
 /* Solve A x = b in place in b from nacu_dgetrf factors
- * (src/linalg/lu.rs:242-260); *info = first zero U_kk + 1, or 0. */
-int nacu_dgetrs(int n, const double* LU, int64_t lda, const int32_t* ipiv, double* b, int32_t* info,
-                nacu_stream_t stream);
+ * (src/linalg/lu.rs:242-260); *info = first zero U_kk + 1, or 0 (-1000: an
+ * internal wait between thread blocks ran out; the result is not valid).
+ * workspace: nacu_getrf_workspace_bytes(n) bytes, not shared with a call in
+ * flight on another stream. */
+int nacu_dgetrs(int n, const double* LU, int64_t lda, const int32_t* ipiv, double* b, int32_t* info, void* workspace,
+                size_t workspace_bytes, nacu_stream_t stream);
 
 /* Workspace bytes of nacu_dgesv_mixed_ir (FP32 copy of A, split-GEMM slices,
  * vectors, and an FP64 copy of A for the fallback). */

@@ -54,7 +54,7 @@ SIGNATURES = {
     "nacu_dgels_batched": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_getrf_workspace_bytes": (_sz, [_i]),
     "nacu_dgetrf": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _sz, _vp]),
-    "nacu_dgetrs": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp]),
+    "nacu_dgetrs": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
     "nacu_gesv_mixed_workspace_bytes": (_sz, [_i]),
     "nacu_dgesv_mixed_ir": (_i, [_i, _vp, _i64, _vp, _vp, _d, _i, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int), _vp, _sz, _vp]),

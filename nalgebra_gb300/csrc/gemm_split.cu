@@ -275,6 +275,8 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int row = m0 + warp * 32 + lane;
   const double srow = (row < g.m) ? pow2(scale_exp(g.rexp[row])) : 0.0;
+  const int erow = (row < g.m) ? scale_exp(g.rexp[row]) : 0;
+  const float falpha = (float)g.alpha, fbeta = (float)g.beta;
   for (int c0 = 0; c0 < kTN; c0 += 16) {
     uint32_t v[16];
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
@@ -293,9 +295,9 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
         if constexpr (sizeof(TO) == 8) {
           const double val = (double)__uint_as_float(v[j]) * srow * pow2(scale_exp(g.cexp[col]));
           *cp = (g.beta == 0.0) ? g.alpha * val : fma(g.alpha, val, g.beta * *cp);
-        } else {  // FP32 output: scale and combine in FP32 (no FP64 instructions)
-          const float val = __uint_as_float(v[j]) * (float)srow * (float)pow2(scale_exp(g.cexp[col]));
-          *cp = (g.beta == 0.0) ? (float)g.alpha * val : fmaf((float)g.alpha, val, (float)g.beta * *cp);
+        } else {  // FP32 output: integer exponent arithmetic and FP32 only
+          const float val = ldexpf(__uint_as_float(v[j]), erow + scale_exp(g.cexp[col]));
+          *cp = (fbeta == 0.f) ? falpha * val : fmaf(falpha, val, fbeta * *cp);
         }
       }
     }

@@ -19,6 +19,9 @@
 // per phase.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+#include <cmath>
+
 #include "common.cuh"
 
 namespace cg = cooperative_groups;
@@ -26,49 +29,82 @@ namespace cg = cooperative_groups;
 namespace nacu {
 
 // ---------------------------------------------------------------------------
-// panel factorization (cooperative)
+// panel factorization (cooperative, the panel resident in shared memory)
 // ---------------------------------------------------------------------------
+constexpr int kPanelThreads = 256;
+constexpr int kPanelMaxG = 256;          // CTAs of one panel launch
+constexpr int kPanelMaxNb = 128;         // panel width
+constexpr int kPanelRowsPerCta = 64;     // rows per CTA aimed for
+constexpr size_t kPanelMaxSmem = 200 * 1024;
+
+// What each column step publishes to the other CTAs, double-buffered by the
+// column's parity (a slot is rewritten two steps later, after every CTA has
+// passed the barrier between): each CTA's pivot candidate (|x| key, row) and
+// that row's panel values, and the current values of row c.
+template <typename T>
+struct PanelPub {
+  unsigned long long key[2][kPanelMaxG];
+  int idx[2][kPanelMaxG];
+  T row[2][kPanelMaxG][kPanelMaxNb];
+  T diag[2][kPanelMaxNb];
+  // the panel's swaps as one row mapping: row pdst[k] takes old row psrc[k]
+  int npairs;
+  int pdst[2 * kPanelMaxNb];
+  int psrc[2 * kPanelMaxNb];
+};
+
 template <typename T>
 struct PanelArgs {
   int n;        // matrix order
   T* A;         // column-major, lda
   int64_t lda;
   int j0, nb;   // panel columns [j0, j0 + nb)
-  int32_t* ipiv;        // global per-step pivots (0-based rows)
-  unsigned long long* cand;  // per-CTA candidate (key << 32 | ~row) for the current column
-  int32_t* info;        // first zero pivot (1-based), atomicMin
+  int chunk;    // rows per CTA (CTA b owns rows j0 + b*chunk ...)
+  int32_t* ipiv;   // per-step pivots (0-based rows)
+  int32_t* info;   // first zero pivot (1-based), atomicMin
+  PanelPub<T>* pub;
 };
 
-constexpr int kPanelThreads = 256;
-
+// One grid barrier per column: the candidates and the candidate rows are
+// published before it, so after it every CTA knows the pivot row's values
+// without a second exchange; row c and the pivot row are swapped by their
+// owners (nalgebra swaps whole rows, lu.rs:111-116; the columns outside the
+// panel are swapped afterwards by lu_swap_kernel).
 template <typename T>
-__global__ void __launch_bounds__(kPanelThreads) lu_panel_coop_kernel(PanelArgs<T> g) {
+__global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g) {
   cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* P = reinterpret_cast<T*>(smem_raw);  // P[t * ldp + r]: panel column t, my row r
   __shared__ uint64_t s_key[kPanelThreads / 32];
   __shared__ int s_idx[kPanelThreads / 32];
-  __shared__ T s_prow[256];
-  __shared__ int s_piv;
+  __shared__ T s_prow[kPanelMaxNb];
+  __shared__ T s_drow[kPanelMaxNb];
+  __shared__ int s_win, s_piv, s_wcta;
   __shared__ T s_inv;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int G = gridDim.x;
-  const int n = g.n;
+  const int G = gridDim.x, b = blockIdx.x;
+  const int nb = g.nb, ldp = g.chunk;
+  const int rb = g.j0 + b * g.chunk;
+  const int nr = max(0, min(g.n, rb + g.chunk) - rb);
   T* A = g.A;
   const int64_t lda = g.lda;
-  const int rows_total = n - g.j0;
-  const int chunk = (rows_total + G - 1) / G;
-  const int r_begin = g.j0 + blockIdx.x * chunk;
-  const int r_end = min(n, r_begin + chunk);
-  for (int j = 0; j < g.nb; ++j) {
-    const int c = g.j0 + j;
-    T* col = A + (size_t)c * lda;
-    // 1. local icamax over my rows >= c (key = |x| bits; NaN only wins at row c)
+  PanelPub<T>* pub = g.pub;
+  for (int e = tid; e < nb * nr; e += kPanelThreads) {
+    const int t = e / nr, r = e - t * nr;
+    P[t * ldp + r] = A[(size_t)(g.j0 + t) * lda + rb + r];
+  }
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    const int c = g.j0 + j, par = j & 1;
+    // 1. my candidate: the largest |x| of column j over my rows >= c
+    //    (icamax, src/base/min_max.rs:221-240: first index on ties)
     uint64_t key = 0;
     int idx = 0x7fffffff;
-    for (int r = max(r_begin, c) + tid; r < r_end; r += kPanelThreads) {
-      const uint64_t k = pivot_key(col[r], r == c);
+    for (int r = max(0, c - rb) + tid; r < nr; r += kPanelThreads) {
+      const uint64_t k = pivot_key(P[j * ldp + r], rb + r == c);
       if (idx == 0x7fffffff || k > key) {
         key = k;
-        idx = r;
+        idx = rb + r;
       }
     }
     warp_argmax(key, idx);
@@ -77,68 +113,149 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_coop_kernel(PanelArgs<
       s_idx[warp] = idx;
     }
     __syncthreads();
-    if (tid == 0) {
-      uint64_t bk = 0;
-      int bi = 0x7fffffff;
-      for (int w = 0; w < kPanelThreads / 32; ++w)
-        if (s_idx[w] != 0x7fffffff && (bi == 0x7fffffff || s_key[w] > bk || (s_key[w] == bk && s_idx[w] < bi))) {
-          bk = s_key[w];
-          bi = s_idx[w];
-        }
-      g.cand[blockIdx.x] = (bi == 0x7fffffff) ? 0ull : bk;  // |x| key (NaN at row c: all ones)
-      g.cand[G + blockIdx.x] = (unsigned long long)(long long)(bi == 0x7fffffff ? -1 : bi);
+    if (warp == 0) {
+      key = lane < kPanelThreads / 32 ? s_key[lane] : 0ull;
+      idx = lane < kPanelThreads / 32 ? s_idx[lane] : 0x7fffffff;
+      warp_argmax(key, idx);
+      if (lane == 0) {
+        s_win = idx;
+        pub->key[par][b] = key;
+        pub->idx[par][b] = (idx == 0x7fffffff) ? -1 : idx;
+      }
+    }
+    __syncthreads();
+    // 2. publish my candidate row and, if I own it, row c
+    {
+      const int w = s_win;
+      if (w != 0x7fffffff)
+        for (int t = tid; t < nb; t += kPanelThreads) pub->row[par][b][t] = P[t * ldp + (w - rb)];
+      if (c >= rb && c < rb + nr)
+        for (int t = tid; t < nb; t += kPanelThreads) pub->diag[par][t] = P[t * ldp + (c - rb)];
     }
     grid.sync();
-    // 2. every CTA reduces the G candidates the same way; CTA 0 swaps rows
-    if (tid == 0) {
+    // 3. the pivot: every CTA reduces the G candidates the same way
+    if (warp == 0) {
       uint64_t bk = 0;
-      int bi = -1;
-      for (int b = 0; b < G; ++b) {
-        const int ri = (int)(long long)g.cand[G + b];
+      int bi = 0x7fffffff, bw = 0;
+      for (int q = lane; q < G; q += 32) {
+        const int ri = pub->idx[par][q];
         if (ri < 0) continue;
-        const uint64_t kk = g.cand[b];
-        if (bi < 0 || kk > bk || (kk == bk && ri < bi)) {
+        const uint64_t kk = pub->key[par][q];
+        if (bi == 0x7fffffff || kk > bk || (kk == bk && ri < bi)) {
           bk = kk;
           bi = ri;
+          bw = q;
         }
       }
-      s_piv = (bi < 0 || bk == 0) ? -1 : bi;  // key 0: |pivot| == 0, the column is skipped
-    }
-    __syncthreads();
-    // decided from the candidates alone: no CTA reads the matrix while CTA 0 swaps
-    const bool skip = (s_piv < 0);  // lu.rs:107-110
-    const int piv = skip ? c : s_piv;
-    if (blockIdx.x == 0) {
-      if (!skip && piv != c)
-        for (int cc = g.j0 + tid; cc < g.j0 + g.nb; cc += kPanelThreads) {
-          T* p = A + (size_t)cc * lda;
-          const T t = p[c];
-          p[c] = p[piv];
-          p[piv] = t;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const uint64_t k2 = __shfl_xor_sync(0xffffffffu, bk, off);
+        const int i2 = __shfl_xor_sync(0xffffffffu, bi, off);
+        const int w2 = __shfl_xor_sync(0xffffffffu, bw, off);
+        if (k2 > bk || (k2 == bk && i2 < bi)) {
+          bk = k2;
+          bi = i2;
+          bw = w2;
         }
-      if (tid == 0) {
-        g.ipiv[c] = skip ? c : piv;
-        if (skip) atomicMin(g.info, c + 1);
+      }
+      if (lane == 0) {
+        const bool zero = (bi == 0x7fffffff || bk == 0);  // all |x| == 0: skipped, lu.rs:107-110
+        s_piv = zero ? -1 : bi;
+        s_wcta = bw;
+        if (b == 0) {
+          g.ipiv[c] = zero ? c : bi;
+          if (zero) atomicMin(g.info, c + 1);
+        }
       }
     }
-    grid.sync();
-    if (skip) continue;
-    // 3. scale my rows of column c and update my rows of the panel's
-    //    remaining columns with the pivot row
-    const int w = g.j0 + g.nb - c - 1;
-    for (int t = tid; t < w; t += kPanelThreads) s_prow[t] = A[(size_t)(c + 1 + t) * lda + c];
-    if (tid == 0) s_inv = T(1) / A[(size_t)c * lda + c];
     __syncthreads();
+    const int piv = s_piv;
+    if (piv < 0) continue;
+    // 4. swap rows c and piv (their owners), from the published copies
+    const bool own_c = (c >= rb && c < rb + nr), own_p = (piv >= rb && piv < rb + nr);
+    for (int t = tid; t < nb; t += kPanelThreads) {
+      s_prow[t] = pub->row[par][s_wcta][t];
+      if (own_p && piv != c) s_drow[t] = pub->diag[par][t];
+    }
+    if (tid == 0) s_inv = T(1) / pub->row[par][s_wcta][j];
+    __syncthreads();
+    if (piv != c) {
+      for (int t = tid; t < nb; t += kPanelThreads) {
+        if (own_c) P[t * ldp + (c - rb)] = s_prow[t];
+        if (own_p) P[t * ldp + (piv - rb)] = s_drow[t];
+      }
+      __syncthreads();
+    }
+    // 5. multipliers of column j below row c; their elimination from the
+    //    panel's remaining columns (gauss_step, lu.rs:340-357)
+    const int r0 = max(0, c + 1 - rb);
     const T inv = s_inv;
-    for (int r = max(r_begin, c + 1) + tid; r < r_end; r += kPanelThreads) {
-      const T l = col[r] * inv;
-      col[r] = l;
-      for (int t = 0; t < w; ++t) {
-        T* p = A + (size_t)(c + 1 + t) * lda + r;
-        *p = axpy1<false>(*p, -s_prow[t], l);
+    for (int r = r0 + tid; r < nr; r += kPanelThreads) P[j * ldp + r] *= inv;
+    __syncthreads();
+    if (j + 1 < nb && r0 < nr) {
+      const int tr = tid & 63, tc = tid >> 6;  // rows r0 + tr + 64 i, columns j + 1 + tc + 4 k
+      for (int r = r0 + tr; r < nr; r += 64) {
+        const T l = P[j * ldp + r];
+        int t = j + 1 + tc;
+        for (; t + 12 < nb; t += 16) {
+          const T p0 = P[t * ldp + r], p1 = P[(t + 4) * ldp + r], p2 = P[(t + 8) * ldp + r],
+                  p3 = P[(t + 12) * ldp + r];
+          const T q0 = s_prow[t], q1 = s_prow[t + 4], q2 = s_prow[t + 8], q3 = s_prow[t + 12];
+          P[t * ldp + r] = axpy1<false>(p0, -q0, l);
+          P[(t + 4) * ldp + r] = axpy1<false>(p1, -q1, l);
+          P[(t + 8) * ldp + r] = axpy1<false>(p2, -q2, l);
+          P[(t + 12) * ldp + r] = axpy1<false>(p3, -q3, l);
+        }
+        for (; t < nb; t += 4) P[t * ldp + r] = axpy1<false>(P[t * ldp + r], -s_prow[t], l);
       }
     }
     __syncthreads();
+  }
+  for (int e = tid; e < nb * nr; e += kPanelThreads) {
+    const int t = e / nr, r = e - t * nr;
+    A[(size_t)(g.j0 + t) * lda + rb + r] = P[t * ldp + r];
+  }
+  if (b == 0) {
+    // compose the panel's swaps into one mapping for the columns outside it:
+    // slots 0..nb-1 are rows j0.., slot nb + i the first swap partner ipiv[j0+i]
+    // below the panel (ipiv was written by this CTA's thread 0)
+    __shared__ int s_slot[kPanelMaxNb];
+    __shared__ int s_row[2 * kPanelMaxNb];
+    __shared__ int s_src[2 * kPanelMaxNb];
+    for (int i = tid; i < nb; i += kPanelThreads) {
+      const int p = g.ipiv[g.j0 + i];
+      int slot = p - g.j0;
+      if (p >= g.j0 + nb) {
+        int f = i;
+        for (int q = 0; q < i; ++q)
+          if (g.ipiv[g.j0 + q] == p) {
+            f = q;
+            break;
+          }
+        slot = nb + f;
+      }
+      s_slot[i] = slot;
+      s_row[i] = g.j0 + i;
+      s_row[nb + i] = p;
+    }
+    for (int sl = tid; sl < 2 * nb; sl += kPanelThreads) s_src[sl] = sl;
+    __syncthreads();
+    if (tid == 0) {
+      for (int i = 0; i < nb; ++i) {
+        const int o = s_slot[i];
+        const int t = s_src[i];
+        s_src[i] = s_src[o];
+        s_src[o] = t;
+      }
+      int k = 0;
+      for (int sl = 0; sl < 2 * nb; ++sl)
+        if (s_src[sl] != sl) {
+          pub->pdst[k] = s_row[sl];
+          pub->psrc[k] = s_row[s_src[sl]];
+          ++k;
+        }
+      pub->npairs = k;
+    }
   }
 }
 
@@ -146,24 +263,91 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_coop_kernel(PanelArgs<
 // row swaps of the panel applied to the other columns; unit-lower TRSM
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void lu_swap_kernel(int n, T* A, int64_t lda, const int32_t* ipiv, int j0, int nb) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n || (c >= j0 && c < j0 + nb)) return;
+__global__ void __launch_bounds__(256) lu_swap_kernel(int n, T* A, int64_t lda, const PanelPub<T>* __restrict__ pub,
+                                                      int j0, int nb) {
+  __shared__ int s_dst[2 * kPanelMaxNb], s_src[2 * kPanelMaxNb];
+  const int np = pub->npairs;
+  for (int k = threadIdx.x; k < np; k += blockDim.x) {
+    s_dst[k] = pub->pdst[k];
+    s_src[k] = pub->psrc[k];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int c = blockIdx.x * 8 + warp;  // a warp per column outside the panel
+  if (c >= j0) c += nb;
+  if (np == 0 || c >= n) return;
   T* col = A + (size_t)c * lda;
-  for (int i = j0; i < j0 + nb; ++i) {
-    const int p = ipiv[i];
-    if (p != i) {
-      const T t = col[i];
-      col[i] = col[p];
-      col[p] = t;
-    }
+  constexpr int U = 2 * kPanelMaxNb / 32;
+  T v[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int k = lane + 32 * u;
+    if (k < np) v[u] = col[s_src[k]];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int k = lane + 32 * u;
+    if (k < np) col[s_dst[k]] = v[u];
   }
 }
 
-// U12 = L11^-1 A12 for columns j0+nb..n-1: L11 (nb x nb, unit lower) in
-// shared memory, one thread per column, the column kept in shared memory.
+// U12 = L11^-1 A12 (unit lower L11, NB x NB, in shared memory) for the columns
+// right of the panel: a warp owns kTrsmCols columns, lane l holding rows
+// l, l + 32, ... of each in registers; row k's final value is broadcast by a
+// shuffle and eliminated from the rows below (solve_lower_triangular_with_diag,
+// src/linalg/solve.rs:106-133, column-oriented).
+constexpr int kTrsmCols = 4;
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) lu_trsm_kernel(int n, T* A, int64_t lda, int j0) {
+  constexpr int M = NB / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* L = reinterpret_cast<T*>(smem_raw);  // L[k * NB + i] = A[j0 + i][j0 + k]
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+    const int k = e / NB, i = e - k * NB;
+    L[e] = A[(size_t)(j0 + k) * lda + j0 + i];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cbase = j0 + NB + (blockIdx.x * 8 + warp) * kTrsmCols;
+  if (cbase >= n) return;
+  T v[kTrsmCols][M];
+#pragma unroll
+  for (int c = 0; c < kTrsmCols; ++c) {
+    const int col = min(cbase + c, n - 1);
+#pragma unroll
+    for (int m = 0; m < M; ++m) v[c][m] = A[(size_t)col * lda + j0 + m * 32 + lane];
+  }
+#pragma unroll
+  for (int mb = 0; mb < M; ++mb) {
+#pragma unroll 4
+    for (int kk = 0; kk < 32; ++kk) {
+      const int k = mb * 32 + kk;
+      T lk[M];
+#pragma unroll
+      for (int m = mb; m < M; ++m) lk[m] = L[k * NB + m * 32 + lane];
+#pragma unroll
+      for (int c = 0; c < kTrsmCols; ++c) {
+        const T xk = __shfl_sync(0xffffffffu, v[c][mb], kk);
+#pragma unroll
+        for (int m = mb; m < M; ++m)
+          if (m > mb || lane > kk) v[c][m] = axpy1<false>(v[c][m], -lk[m], xk);
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < kTrsmCols; ++c) {
+    const int col = cbase + c;
+    if (col < n)
+#pragma unroll
+      for (int m = 0; m < M; ++m) A[(size_t)col * lda + j0 + m * 32 + lane] = v[c][m];
+  }
+}
+
+// The same for a panel width without a register-tiled instance: L11 in shared
+// memory, one thread per column, the column kept in shared memory.
 template <typename T>
-__global__ void __launch_bounds__(64) lu_trsm_kernel(int n, T* A, int64_t lda, int j0, int nb) {
+__global__ void __launch_bounds__(64) lu_trsm_generic_kernel(int n, T* A, int64_t lda, int j0, int nb) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* L = reinterpret_cast<T*>(smem_raw);  // nb x nb
   T* X = L + (size_t)nb * nb;             // nb x 64 (column-major per thread)
@@ -186,62 +370,165 @@ __global__ void __launch_bounds__(64) lu_trsm_kernel(int n, T* A, int64_t lda, i
     for (int i = 0; i < nb; ++i) col[i] = X[(size_t)i * 64 + tid];
 }
 
-// ---------------------------------------------------------------------------
-// triangular solves for one right-hand side (cooperative)
-// ---------------------------------------------------------------------------
-constexpr int kTrsvBlock = 128;
-constexpr int kTrsvThreads = 256;
+template <typename T, int NB>
+cudaError_t launch_trsm_tiled(int n, T* A, int64_t lda, int j0, int rest, cudaStream_t s) {
+  const size_t smem = (size_t)NB * NB * sizeof(T);
+  cudaError_t e = cudaFuncSetAttribute(lu_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int per_cta = 8 * kTrsmCols;
+  lu_trsm_kernel<T, NB><<<(rest + per_cta - 1) / per_cta, 256, smem, s>>>(n, A, lda, j0);
+  return cudaGetLastError();
+}
 
-// lower = true: x <- L^-1 x (unit diagonal); lower = false: x <- U^-1 x.
 template <typename T>
-__global__ void __launch_bounds__(kTrsvThreads) trsv_coop_kernel(int n, const T* __restrict__ A, int64_t lda, T* x,
-                                                                 int lower, int32_t* info) {
-  cg::grid_group grid = cg::this_grid();
-  __shared__ T xs[kTrsvBlock];
-  const int tid = threadIdx.x;
-  const int nblk = (n + kTrsvBlock - 1) / kTrsvBlock;
-  for (int s = 0; s < nblk; ++s) {
-    const int b = lower ? s : nblk - 1 - s;
-    const int r0 = b * kTrsvBlock, r1 = min(n, r0 + kTrsvBlock), bs = r1 - r0;
-    if (blockIdx.x == 0) {
-      // diagonal block: one warp, sequential over the block's rows
-      if (tid < 32) {
-        if (lower) {
-          for (int i = 0; i < bs; ++i) {
-            const T xi = x[r0 + i];
-            __syncwarp();
-            for (int r = i + 1 + tid; r < bs; r += 32)
-              x[r0 + r] = axpy1<false>(x[r0 + r], -xi, A[(size_t)(r0 + i) * lda + r0 + r]);
-            __syncwarp();
-          }
-        } else {
-          for (int i = bs - 1; i >= 0; --i) {
-            if (tid == 0) {
-              const T d = A[(size_t)(r0 + i) * lda + r0 + i];
-              if (d == T(0)) atomicMin(info, r0 + i + 1);
-              x[r0 + i] = x[r0 + i] / d;
-            }
-            __syncwarp();
-            const T xi = x[r0 + i];
-            for (int r = tid; r < i; r += 32)
-              x[r0 + r] = axpy1<false>(x[r0 + r], -xi, A[(size_t)(r0 + i) * lda + r0 + r]);
-            __syncwarp();
-          }
+cudaError_t launch_trsm(int n, T* A, int64_t lda, int j0, int jb, int rest, cudaStream_t s) {
+  if (jb == 64) return launch_trsm_tiled<T, 64>(n, A, lda, j0, rest, s);
+  if (jb == 128) return launch_trsm_tiled<T, 128>(n, A, lda, j0, rest, s);
+  const size_t smem = (size_t)jb * jb * sizeof(T) + (size_t)jb * 64 * sizeof(T);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(lu_trsm_generic_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  lu_trsm_generic_kernel<T><<<(rest + 63) / 64, 64, smem, s>>>(n, A, lda, j0, jb);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// triangular solves for one right-hand side (one CTA per row block, ready flags)
+// ---------------------------------------------------------------------------
+constexpr int kTrsvThreads = 256;
+constexpr int kTrsvInfoTimeout = -1000;  // info value when a wait ran out
+template <typename T>
+struct TrsvTile {
+  static constexpr int BS = sizeof(T) == 4 ? 128 : 64;  // rows per block
+  static constexpr int NC = kTrsvThreads / BS;          // column parts per row
+  static constexpr int CW = BS / NC;                    // columns per part
+};
+
+template <typename T>
+struct TrsvArgs {
+  int n;
+  const T* A;
+  int64_t lda;
+  T* x;
+  int lower;
+  int32_t* info;
+  int* sync;  // [0] ticket, [1] timeout flag, [2 + b] block b solved (zeroed before the launch)
+};
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// lower = 1: x <- L^-1 x (unit diagonal, blocks top-down); lower = 0:
+// x <- U^-1 x (bottom-up; a zero U_ii is reported in info, as
+// solve_upper_triangular_mut returns false, src/linalg/solve.rs:137-182).
+// CTAs take row blocks in ticket order, so a CTA only ever waits for blocks
+// whose CTAs have started: for each solved block it prefetches its tile of the
+// triangle into registers, waits for the block's flag (bounded), and applies
+// it; then it solves its diagonal block in shared memory, stores it and raises
+// its own flag.  Every wait gives up after a fixed number of polls, sets the
+// timeout flag and info = kTrsvInfoTimeout, and the CTA returns.
+template <typename T>
+__global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
+  constexpr int BS = TrsvTile<T>::BS, NC = TrsvTile<T>::NC, CW = TrsvTile<T>::CW, LD = BS + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Ts = reinterpret_cast<T*>(smem_raw);  // Ts[k * LD + i] = A[r0 + i][r0 + k]
+  __shared__ T xs[BS];
+  __shared__ T rd[BS];
+  __shared__ T part[NC][BS];
+  __shared__ int s_ticket, s_abort;
+  const int tid = threadIdx.x, tr = tid % BS, tc = tid / BS;
+  const int n = g.n, lower = g.lower;
+  const int nblk = (n + BS - 1) / BS;
+  if (tid == 0) {
+    s_ticket = atomicAdd(&g.sync[0], 1);
+    s_abort = 0;
+  }
+  __syncthreads();
+  const int t = s_ticket;
+  if (t >= nblk) return;
+  const int kb = lower ? t : nblk - 1 - t;
+  const int r0 = kb * BS, bs = min(BS, n - r0);
+  const T* A = g.A;
+  const int64_t lda = g.lda;
+  for (int e = tid; e < bs * bs; e += kTrsvThreads) {
+    const int k = e / bs, i = e - k * bs;
+    if (lower ? (i > k) : (i < k)) Ts[k * LD + i] = A[(size_t)(r0 + k) * lda + r0 + i];
+  }
+  if (!lower)
+    for (int i = tid; i < bs; i += kTrsvThreads) {
+      const T d = A[(size_t)(r0 + i) * lda + r0 + i];
+      if (d == T(0)) atomicMin(g.info, r0 + i + 1);
+      rd[i] = T(1) / d;
+    }
+  T acc = (tc == 0 && tr < bs) ? g.x[r0 + tr] : T(0);
+  for (int q = 0; q < t; ++q) {
+    const int jb = lower ? q : nblk - 1 - q;
+    const int c0 = jb * BS, cs = min(BS, n - c0);
+    T a[CW];
+#pragma unroll
+    for (int u = 0; u < CW; ++u) {
+      const int col = tc * CW + u;
+      a[u] = (tr < bs && col < cs) ? A[(size_t)(c0 + col) * lda + r0 + tr] : T(0);
+    }
+    if (tid == 0) {
+      int polls = 0;
+      while (ld_acquire(&g.sync[2 + jb]) == 0) {
+        if (++polls > (1 << 22)) {
+          s_abort = 1;
+          atomicExch(&g.sync[1], 1);
+          atomicMin(g.info, kTrsvInfoTimeout);
+          break;
         }
+        __nanosleep(64);
       }
     }
-    grid.sync();
-    // apply the solved block to the remaining rows: x[rest] -= A[rest, blk] x[blk]
-    for (int i = tid; i < bs; i += kTrsvThreads) xs[i] = x[r0 + i];
     __syncthreads();
-    const int rest0 = lower ? r1 : 0, rest1 = lower ? n : r0;
-    for (int r = rest0 + blockIdx.x * kTrsvThreads + tid; r < rest1; r += gridDim.x * kTrsvThreads) {
-      T acc = x[r];
-      for (int i = 0; i < bs; ++i) acc = axpy1<false>(acc, -xs[i], A[(size_t)(r0 + i) * lda + r]);
-      x[r] = acc;
-    }
-    grid.sync();
+    if (s_abort) return;
+    if (tid < cs) xs[tid] = __ldcg(&g.x[c0 + tid]);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < CW; ++u) acc = axpy1<false>(acc, -xs[tc * CW + u], a[u]);
+    __syncthreads();
   }
+  part[tc][tr] = acc;
+  __syncthreads();
+  if (tid < bs) {
+    T y = part[0][tid];
+#pragma unroll
+    for (int c = 1; c < NC; ++c) y += part[c][tid];
+    xs[tid] = y;
+  }
+  __syncthreads();
+  if (tid < 32) {
+    if (lower) {
+      for (int k = 0; k < bs; ++k) {
+        const T xk = xs[k];
+        for (int i = k + 1 + tid; i < bs; i += 32) xs[i] = axpy1<false>(xs[i], -Ts[k * LD + i], xk);
+        __syncwarp();
+      }
+    } else {
+      for (int k = bs - 1; k >= 0; --k) {
+        const T xk = xs[k] * rd[k];
+        for (int i = tid; i < k; i += 32) xs[i] = axpy1<false>(xs[i], -Ts[k * LD + i], xk);
+        __syncwarp();
+        if (tid == 0) xs[k] = xk;
+        __syncwarp();
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < bs) g.x[r0 + tid] = xs[tid];
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) st_release(&g.sync[2 + kb], 1);
 }
 
 // info holds a large sentinel until some pivot fails; 0 afterwards means "ok".
@@ -250,17 +537,66 @@ __global__ void info_finalize_kernel(int32_t* info) {
   if (*info == 0x7fffffff) *info = 0;
 }
 
+// x <- P x: nalgebra's row swaps in order (PermutationSequence::permute_rows,
+// src/linalg/permutation_sequence.rs), one thread, the vector and the swap
+// list staged in shared memory when they fit.
 template <typename T>
-__global__ void apply_pivots_kernel(int n, const int32_t* ipiv, T* x) {
-  if (blockIdx.x == 0 && threadIdx.x == 0)
+__global__ void apply_pivots_kernel(int n, const int32_t* __restrict__ ipiv, T* x, int staged) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* xs = reinterpret_cast<T*>(smem_raw);
+  int32_t* ps = reinterpret_cast<int32_t*>(xs + (staged ? n : 0));
+  if (!staged) {
+    if (threadIdx.x == 0)
+      for (int i = 0; i < n; ++i) {
+        const int p = ipiv[i];
+        if (p != i) {
+          const T t = x[i];
+          x[i] = x[p];
+          x[p] = t;
+        }
+      }
+    return;
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    xs[i] = x[i];
+    ps[i] = ipiv[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
     for (int i = 0; i < n; ++i) {
-      const int p = ipiv[i];
+      const int p = ps[i];
       if (p != i) {
-        const T t = x[i];
-        x[i] = x[p];
-        x[p] = t;
+        const T t = xs[i];
+        xs[i] = xs[p];
+        xs[p] = t;
       }
     }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xs[i];
+}
+
+// perm[i] = the source row of row i after the swaps (gathers replace them).
+__global__ void pivots_to_perm_kernel(int n, const int32_t* __restrict__ ipiv, int32_t* perm, int staged) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int32_t* pm = staged ? reinterpret_cast<int32_t*>(smem_raw) : perm;
+  int32_t* ps = staged ? pm + n : nullptr;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    pm[i] = i;
+    if (staged) ps[i] = ipiv[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 0; i < n; ++i) {
+      const int p = staged ? ps[i] : ipiv[i];
+      if (p != i) {
+        const int32_t t = pm[i];
+        pm[i] = pm[p];
+        pm[p] = t;
+      }
+    }
+  __syncthreads();
+  if (staged)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = pm[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -273,8 +609,8 @@ int coop_grid(const void* kern, int threads, size_t smem) {
   return sm_count() * per_sm;
 }
 
-// Workspace for the panel candidates: 2 * G + 1 words, G <= 4 * SMs.
-size_t getrf_ws_bytes() { return ((size_t)2 * 4 * 1024 + 16) * sizeof(unsigned long long); }
+// The panel's exchange area (sized for FP64 and the widest panel).
+size_t getrf_ws_bytes() { return (sizeof(PanelPub<double>) + 255) & ~(size_t)255; }
 
 typedef int (*UpdateFn)(int m, int n, int k, const void* L21, const void* U12, void* A22, int64_t lda, void* ctx,
                         cudaStream_t s);
@@ -282,31 +618,30 @@ typedef int (*UpdateFn)(int m, int n, int k, const void* L21, const void* U12, v
 template <typename T>
 int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* ws, int nb, UpdateFn update,
                   void* ctx, cudaStream_t s, const char* name) {
-  unsigned long long* cand = reinterpret_cast<unsigned long long*>(ws);
   cudaError_t e;
+  if (nb > kPanelMaxNb) nb = kPanelMaxNb;
+  const void* pk = reinterpret_cast<const void*>(lu_panel_kernel<T>);
+  e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelMaxSmem);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  const int gmax = std::min(kPanelMaxG, sm_count());
   info_init_kernel<<<1, 1, 0, s>>>(info);
-  const void* pk = reinterpret_cast<const void*>(lu_panel_coop_kernel<T>);
-  int G = coop_grid(pk, kPanelThreads, 0);
-  if (G > 1024) G = 1024;
   for (int j0 = 0; j0 < n; j0 += nb) {
-    const int jb = min(nb, n - j0);
-    PanelArgs<T> pa{n, A, lda, j0, jb, ipiv, cand, info};
-    // enough CTAs to cover the rows, at most the co-resident grid
+    const int jb = std::min(nb, n - j0);
     const int rows = n - j0;
-    int g = min(G, (rows + kPanelThreads - 1) / kPanelThreads);
-    if (g < 1) g = 1;
+    const int max_rows = (int)(kPanelMaxSmem / ((size_t)jb * sizeof(T)));
+    int G = std::max((rows + kPanelRowsPerCta - 1) / kPanelRowsPerCta, (rows + max_rows - 1) / max_rows);
+    G = std::max(1, std::min(G, gmax));
+    const int chunk = (rows + G - 1) / G;
+    if (chunk > max_rows) return record_arg_error(-1, "getrf: n too large for the shared-memory panel");
+    PanelArgs<T> pa{n, A, lda, j0, jb, chunk, ipiv, info, reinterpret_cast<PanelPub<T>*>(ws)};
     void* args[] = {&pa};
-    e = cudaLaunchCooperativeKernel(pk, g, kPanelThreads, args, 0, s);
+    e = cudaLaunchCooperativeKernel(pk, G, kPanelThreads, args, (size_t)chunk * jb * sizeof(T), s);
     if (e != cudaSuccess) return record_cuda_error(e, name);
-    lu_swap_kernel<T><<<(n + 255) / 256, 256, 0, s>>>(n, A, lda, ipiv, j0, jb);
+    if (n > jb) lu_swap_kernel<T><<<(n - jb + 7) / 8, 256, 0, s>>>(n, A, lda, pa.pub, j0, jb);
     const int rest = n - j0 - jb;
     if (rest > 0) {
-      const size_t smem = (size_t)jb * jb * sizeof(T) + (size_t)jb * 64 * sizeof(T);
-      if (smem > 48 * 1024) {
-        e = cudaFuncSetAttribute(lu_trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return record_cuda_error(e, name);
-      }
-      lu_trsm_kernel<T><<<(rest + 63) / 64, 64, smem, s>>>(n, A, lda, j0, jb);
+      e = launch_trsm<T>(n, A, lda, j0, jb, rest, s);
+      if (e != cudaSuccess) return record_cuda_error(e, name);
       int rc = update(rest, rest, jb, A + (size_t)j0 * lda + j0 + jb, A + (size_t)(j0 + jb) * lda + j0,
                       A + (size_t)(j0 + jb) * lda + j0 + jb, lda, ctx, s);
       if (rc != NACU_SUCCESS) return rc;
@@ -318,24 +653,42 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
   return check_launch(name);
 }
 
+// x <- U^-1 L^-1 x (the permutation already applied); sync: 2 + n/64 + 1 ints.
+size_t trsv_sync_bytes(int n) { return ((size_t)n / 64 + 4) * sizeof(int); }
+
 template <typename T>
-int getrs_one(int n, const T* LU, int64_t lda, const int32_t* ipiv, T* x, int32_t* info, cudaStream_t s,
+int trsv_pair(int n, const T* LU, int64_t lda, T* x, int32_t* info, int* sync, cudaStream_t s, const char* name) {
+  const void* tk = reinterpret_cast<const void*>(trsv_kernel<T>);
+  constexpr int BS = TrsvTile<T>::BS;
+  const size_t smem = (size_t)BS * (BS + 1) * sizeof(T);
+  cudaError_t e = cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  const int nblk = (n + BS - 1) / BS;
+  for (int lower = 1; lower >= 0; --lower) {
+    e = cudaMemsetAsync(sync, 0, (size_t)(nblk + 2) * sizeof(int), s);
+    if (e != cudaSuccess) return record_cuda_error(e, name);
+    TrsvArgs<T> ta{n, LU, lda, x, lower, info, sync};
+    trsv_kernel<T><<<nblk, kTrsvThreads, smem, s>>>(ta);
+  }
+  return check_launch(name);
+}
+
+constexpr size_t kStageLimit = 160 * 1024;
+
+template <typename T>
+int getrs_one(int n, const T* LU, int64_t lda, const int32_t* ipiv, T* x, int32_t* info, int* sync, cudaStream_t s,
               const char* name) {
   info_init_kernel<<<1, 1, 0, s>>>(info);
-  apply_pivots_kernel<T><<<1, 32, 0, s>>>(n, ipiv, x);
-  const void* tk = reinterpret_cast<const void*>(trsv_coop_kernel<T>);
-  int G = coop_grid(tk, kTrsvThreads, 0);
-  const int want = (n + kTrsvThreads - 1) / kTrsvThreads;
-  int g = min(G, max(1, want));
-  for (int lower = 1; lower >= 0; --lower) {
-    int nn = n;
-    const T* a = LU;
-    int64_t ld = lda;
-    int lw = lower;
-    void* args[] = {&nn, &a, &ld, &x, &lw, &info};
-    cudaError_t e = cudaLaunchCooperativeKernel(tk, g, kTrsvThreads, args, 0, s);
+  const size_t stage = (size_t)n * (sizeof(T) + sizeof(int32_t));
+  const int staged = stage <= kStageLimit;
+  if (staged && stage > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(apply_pivots_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kStageLimit);
     if (e != cudaSuccess) return record_cuda_error(e, name);
   }
+  apply_pivots_kernel<T><<<1, 256, staged ? stage : 0, s>>>(n, ipiv, x, staged);
+  int rc = trsv_pair<T>(n, LU, lda, x, info, sync, s, name);
+  if (rc != NACU_SUCCESS) return rc;
   info_finalize_kernel<<<1, 1, 0, s>>>(info);
   return check_launch(name);
 }
@@ -422,10 +775,11 @@ __global__ void residual_finish_kernel(int n, const double* __restrict__ b, cons
   }
 }
 
-// d32 = (float)(src * 2^-e)
-__global__ void scale_to_fp32_kernel(int n, const double* __restrict__ src, int e, float* __restrict__ d32) {
+// d32 = (float)(P src * 2^-e): the row permutation of the factor fused as a gather
+__global__ void scale_to_fp32_kernel(int n, const double* __restrict__ src, const int32_t* __restrict__ perm, int e,
+                                     float* __restrict__ d32) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) d32[i] = (float)(src[i] * __longlong_as_double((long long)(1023 - e) << 52));
+  if (i < n) d32[i] = (float)(src[perm[i]] * __longlong_as_double((long long)(1023 - e) << 52));
 }
 // x += (double)d32 * 2^e; max |d| into nrm[3]
 __global__ void accumulate_kernel(int n, const float* __restrict__ d32, int e, double* __restrict__ x,
@@ -443,7 +797,7 @@ __global__ void accumulate_kernel(int n, const float* __restrict__ d32, int e, d
 }
 
 struct MixedLuLayout {
-  size_t a32, ipiv, info, cand, split, r, d32, part, nrm, a64, total;
+  size_t a32, ipiv, perm, info, cand, split, r, d32, part, nrm, a64, total;
 };
 inline size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 MixedLuLayout mixed_lu_layout(int n, int nb) {
@@ -451,6 +805,7 @@ MixedLuLayout mixed_lu_layout(int n, int nb) {
   size_t o = 0;
   L.a32 = o;   o = up256(o + (size_t)n * n * 4);
   L.ipiv = o;  o = up256(o + (size_t)n * 4);
+  L.perm = o;  o = up256(o + (size_t)n * 4);
   L.info = o;  o = up256(o + 16);
   L.cand = o;  o = up256(o + getrf_ws_bytes());
   o = (o + 1023) & ~(size_t)1023;
@@ -492,6 +847,7 @@ int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, do
   unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)workspace + 1023) & ~(uintptr_t)1023);
   float* A32 = reinterpret_cast<float*>(base + L.a32);
   int32_t* ipiv = reinterpret_cast<int32_t*>(base + L.ipiv);
+  int32_t* perm = reinterpret_cast<int32_t*>(base + L.perm);
   int32_t* info = reinterpret_cast<int32_t*>(base + L.info);
   void* cand = base + L.cand;
   void* split_ws = base + L.split;
@@ -526,6 +882,12 @@ int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, do
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgesv_mixed_ir");
   bool converged = false;
   if (hinfo == 0) {
+    const int staged = (size_t)n * 8 <= kStageLimit;
+    if (staged && (size_t)n * 8 > 48 * 1024) {
+      e = cudaFuncSetAttribute(pivots_to_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageLimit);
+      if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgesv_mixed_ir");
+    }
+    pivots_to_perm_kernel<<<1, 256, staged ? (size_t)n * 8 : 0, s>>>(n, ipiv, perm, staged);
     // refinement: x0 = 0, r0 = b
     cudaMemsetAsync(x, 0, (size_t)n * 8, s);
     cudaMemcpyAsync(r, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, s);
@@ -537,8 +899,8 @@ int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, do
         const double m = rnorm;
         er = (m > 0.0 && std::isfinite(m)) ? exp_of_bits(__builtin_bit_cast(unsigned long long, m)) : 0;
       }
-      scale_to_fp32_kernel<<<nblk, 256, 0, s>>>(n, r, er, d32);
-      rc = getrs_one<float>(n, A32, n, ipiv, d32, info + 1, s, "nacu_dgesv_mixed_ir");
+      scale_to_fp32_kernel<<<nblk, 256, 0, s>>>(n, r, perm, er, d32);
+      rc = trsv_pair<float>(n, A32, n, d32, info + 1, reinterpret_cast<int*>(cand), s, "nacu_dgesv_mixed_ir");
       if (rc != NACU_SUCCESS) return rc;
       cudaMemsetAsync(nrm, 0, 64, s);
       accumulate_kernel<<<nblk, 256, 0, s>>>(n, d32, er, x, nrm);
@@ -567,7 +929,7 @@ int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, do
     rc = nacu_dgetrf(n, A64, n, ipiv, info, cand, getrf_ws_bytes(), stream);
     if (rc != NACU_SUCCESS) return rc;
     cudaMemcpyAsync(x, b, (size_t)n * 8, cudaMemcpyDeviceToDevice, s);
-    rc = nacu_dgetrs(n, A64, n, ipiv, x, info + 1, stream);
+    rc = nacu_dgetrs(n, A64, n, ipiv, x, info + 1, cand, getrf_ws_bytes(), stream);
     if (rc != NACU_SUCCESS) return rc;
     cudaMemsetAsync(nrm, 0, 64, s);
     gemv_partial_kernel<<<dim3(nblk, kGemvChunks), 256, 0, s>>>(n, A, lda, x, part, 0);
@@ -584,8 +946,7 @@ int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, do
 }
 
 size_t nacu_getrf_workspace_bytes(int n) {
-  (void)n;
-  return nacu::getrf_ws_bytes();
+  return std::max(nacu::getrf_ws_bytes(), nacu::trsv_sync_bytes(n < 0 ? 0 : n));
 }
 
 int nacu_dgetrf(int n, double* A, int64_t lda, int32_t* ipiv, int32_t* info, void* workspace, size_t workspace_bytes,
@@ -596,19 +957,23 @@ int nacu_dgetrf(int n, double* A, int64_t lda, int32_t* ipiv, int32_t* info, voi
   if (!A) return record_arg_error(-2, "dgetrf: null A");
   if (lda < n) return record_arg_error(-3, "dgetrf: lda < n");
   if (!ipiv || !info) return record_arg_error(-4, "dgetrf: null ipiv or info");
-  if (!workspace || workspace_bytes < getrf_ws_bytes()) return record_arg_error(-6, "dgetrf: workspace too small");
+  if (!workspace || workspace_bytes < nacu_getrf_workspace_bytes(n))
+    return record_arg_error(-6, "dgetrf: workspace too small");
   return getrf_blocked<double>(n, A, lda, ipiv, info, workspace, 64, update_fp64, nullptr, (cudaStream_t)stream,
                                "nacu_dgetrf");
 }
 
-int nacu_dgetrs(int n, const double* LU, int64_t lda, const int32_t* ipiv, double* b, int32_t* info,
-                nacu_stream_t stream) {
+int nacu_dgetrs(int n, const double* LU, int64_t lda, const int32_t* ipiv, double* b, int32_t* info, void* workspace,
+                size_t workspace_bytes, nacu_stream_t stream) {
   using namespace nacu;
   if (n < 0) return record_arg_error(-1, "dgetrs: n < 0");
   if (n == 0) return NACU_SUCCESS;
   if (!LU || !ipiv || !b || !info) return record_arg_error(-2, "dgetrs: null argument");
   if (lda < n) return record_arg_error(-3, "dgetrs: lda < n");
-  return getrs_one<double>(n, LU, lda, ipiv, b, info, (cudaStream_t)stream, "nacu_dgetrs");
+  if (!workspace || workspace_bytes < nacu::trsv_sync_bytes(n))
+    return record_arg_error(-7, "dgetrs: workspace too small");
+  return getrs_one<double>(n, LU, lda, ipiv, b, info, static_cast<int*>(workspace), (cudaStream_t)stream,
+                           "nacu_dgetrs");
 }
 
 }  // extern "C"

@@ -28,7 +28,8 @@ def _getrf(cuda, a, b=None):
     if b is not None:
         X = torch.from_numpy(np.ascontiguousarray(b)).cuda()
         i2 = torch.full((1,), -7, dtype=torch.int32, device="cuda")
-        _lib.call("nacu_dgetrs", n, A.data_ptr(), n, ipiv.data_ptr(), X.data_ptr(), i2.data_ptr(), s)
+        _lib.call("nacu_dgetrs", n, A.data_ptr(), n, ipiv.data_ptr(), X.data_ptr(), i2.data_ptr(), ws.data_ptr(),
+                  ws.numel(), s)
         torch.cuda.synchronize()
         x = X.cpu().numpy()
         info2 = int(i2.item())
