@@ -163,12 +163,16 @@ def bench_ragged_ours(args, rank, world):
     stream = torch.cuda.current_stream()
     sp = int(stream.cuda_stream)
     n_max = int(ns.max())
+    from nalgebra_gb300 import tuning
+
+    tune_res = tuning.autotune(save=False) if args.autotune else None
+    tiles_table = tuning.current(L)
 
     def launch():  # the stream is read at call time: inside a capture it is the capture stream
         _lib.call("nacu_dposv_ragged", count, n_max, batch._d_rows.data_ptr(), batch._d_off.data_ptr(),
                   A.data_ptr(), nrhs, rhs._d_off.data_ptr(), B.data_ptr(), chol.info.data_ptr(),
-                  chol.logdet.data_ptr(), chol._order.data_ptr(), chol._ws.data_ptr(), chol._ws.numel(), 0.0, 0,
-                  int(torch.cuda.current_stream().cuda_stream))
+                  chol.logdet.data_ptr(), chol._order.data_ptr() if args.single_launch else None,
+                  chol._ws.data_ptr(), chol._ws.numel(), 0.0, 0, int(torch.cuda.current_stream().cuda_stream))
 
     def restore():
         A.copy_(a0)
@@ -315,7 +319,10 @@ def bench_ragged_ours(args, rank, world):
         "config": {"workload": "ragged_cholesky", "count": count, "n_range": [cfg["n_lo"], cfg["n_hi"]],
                    "nrhs": nrhs,
                    "form": ("batched persistent mixed precision (FP32 factor, FP64 refinement), CUDA graph"
-                            if use_mixed else "batched persistent FP64 (one launch, largest-first work queue), CUDA graph"),
+                            if use_mixed else "batched persistent FP64, CUDA graph"),
+                   "fp64_launch": ("one launch, host largest-first order, default tile" if args.single_launch else
+                                   "size-bucketed persistent launches, autotuned tile per bucket"),
+                   "tile_table": tiles_table, "autotuned_now": tune_res,
                    "l2": "inputs (3.4 GB) larger than L2; input restore outside the timed events",
                    "parallelism": "replicas" if world > 1 else "single"},
         "gflops": flops / (head_ms * 1e-3) / 1e9,
@@ -832,6 +839,11 @@ def main():
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
                                                                   "mixed_lu"])
     ap.add_argument("--exact", action="store_true")
+    ap.add_argument("--single-launch", action="store_true",
+                    help="ragged_cholesky: one launch over a host-sorted order with the default tile "
+                         "(instead of the size-bucketed launches with the tuned tiles)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="ragged_cholesky: re-run the tile autotuner before timing (not saved)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=0, help="ragged_cholesky: override the number of systems")
     ap.add_argument("--profile", action="store_true", help="timed kernel only (for ncu captures)")

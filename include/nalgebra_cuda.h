@@ -107,6 +107,34 @@ int nacu_dgesv_batched(int n, int nrhs, double* A, int64_t strideA, int32_t* ipi
 int nacu_sgesv_batched(int n, int nrhs, float* A, int64_t strideA, int32_t* ipiv, float* B,
                        int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
 
+/* ---- autotuned tiles of the ragged Cholesky launch --------------------------
+ * When nacu_dposv_ragged / nacu_dpotrf_ragged / nacu_dpotrs_ragged get no
+ * processing order (order == NULL), the library sorts the batch by order into
+ * NACU_RAGGED_BUCKETS size buckets (upper orders 32, 64, 96, 128, 192, 256,
+ * 384, 512) and runs one persistent launch per bucket, largest first, each
+ * with the bucket's tile (threads per matrix, panel width) from the tuning
+ * table and shared memory sized for the bucket.  No reference counterpart
+ * (nalgebra factors one matrix per call). */
+#define NACU_RAGGED_BUCKETS 8
+#define NACU_RAGGED_TILES 4
+
+/* The bucket bounds (NACU_RAGGED_BUCKETS ints) and the tiles (threads per
+ * matrix and panel width, NACU_RAGGED_TILES ints each); any pointer may be NULL. */
+int nacu_ragged_tuning_layout(int32_t* bucket_hi, int32_t* tile_threads, int32_t* tile_nb);
+
+/* Installs / reads the process-wide tuning table (a tile index per bucket). */
+int nacu_ragged_set_tuning(const int32_t* table, int nbuckets);
+int nacu_ragged_get_tuning(int32_t* table, int nbuckets);
+
+/* Times every tile on every bucket (per_bucket synthetic diagonally dominant
+ * SPD systems with orders uniform in the bucket, nrhs right-hand sides; CUDA
+ * events, best of three after a warm-up), installs the fastest tile per
+ * bucket and returns the table and the times (ms_out: NACU_RAGGED_BUCKETS x
+ * NACU_RAGGED_TILES, may be NULL).  Allocates and frees its own test batch;
+ * synchronizes the stream. */
+int nacu_ragged_autotune(int per_bucket, int nrhs, int flags, int32_t* table_out, double* ms_out,
+                         nacu_stream_t stream);
+
 /* ---- Cholesky (ragged batch, one persistent launch) ------------------------ */
 
 /* Bytes of device scratch nacu_dposv_ragged needs (the work-queue head). */

@@ -297,8 +297,10 @@ class LUBatch:
 
 
 class CholeskyBatch:
-    """Ragged batched Cholesky (orders up to 512) in one persistent launch.
-    Lazy: ``solve`` runs factor + solve + log-determinant in one kernel."""
+    """Ragged batched Cholesky (orders up to 512): persistent launches over the
+    library's size-bucketed order, each bucket with its autotuned tile
+    (``nalgebra_gb300.tuning``).  Lazy: ``solve`` runs factor + solve +
+    log-determinant in one pass over the batch."""
 
     def __init__(self, batch: DeviceBatch, flags: int = 0, substitute: float | None = None):
         torch = _torch()
@@ -320,7 +322,7 @@ class CholeskyBatch:
         if not self.factored:
             b = self.batch
             _lib.call("nacu_dpotrf_ragged", len(b), self.n_max, b._d_rows.data_ptr(), b._d_off.data_ptr(),
-                      b.data.data_ptr(), self.info.data_ptr(), self.logdet.data_ptr(), self._order.data_ptr(),
+                      b.data.data_ptr(), self.info.data_ptr(), self.logdet.data_ptr(), None,
                       self._ws.data_ptr(), self._ws.numel(), self.substitute, self.flags, _stream_ptr())
             self.factored = True
         return self
@@ -335,12 +337,12 @@ class CholeskyBatch:
             raise ValueError("every right-hand side block needs the same nrhs")
         if self.factored:
             _lib.call("nacu_dpotrs_ragged", len(b), self.n_max, b._d_rows.data_ptr(), b._d_off.data_ptr(),
-                      b.data.data_ptr(), nrhs, rhs._d_off.data_ptr(), rhs.data.data_ptr(), self._order.data_ptr(),
+                      b.data.data_ptr(), nrhs, rhs._d_off.data_ptr(), rhs.data.data_ptr(), None,
                       self._ws.data_ptr(), self._ws.numel(), self.flags, _stream_ptr())
         else:
             _lib.call("nacu_dposv_ragged", len(b), self.n_max, b._d_rows.data_ptr(), b._d_off.data_ptr(),
                       b.data.data_ptr(), nrhs, rhs._d_off.data_ptr(), rhs.data.data_ptr(), self.info.data_ptr(),
-                      self.logdet.data_ptr(), self._order.data_ptr(), self._ws.data_ptr(), self._ws.numel(),
+                      self.logdet.data_ptr(), None, self._ws.data_ptr(), self._ws.numel(),
                       self.substitute, self.flags, _stream_ptr())
             self.factored = True
         return self.info

@@ -55,6 +55,10 @@ SIGNATURES = {
     "nacu_getrf_workspace_bytes": (_sz, [_i]),
     "nacu_dgetrf": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _sz, _vp]),
     "nacu_dgetrs": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "nacu_ragged_tuning_layout": (_i, [_vp, _vp, _vp]),
+    "nacu_ragged_set_tuning": (_i, [_vp, _i]),
+    "nacu_ragged_get_tuning": (_i, [_vp, _i]),
+    "nacu_ragged_autotune": (_i, [_i, _i, _i, _vp, _vp, _vp]),
     "nacu_gesv_mixed_workspace_bytes": (_sz, [_i]),
     "nacu_dgesv_mixed_ir": (_i, [_i, _vp, _i64, _vp, _vp, _d, _i, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int), _vp, _sz, _vp]),
@@ -96,6 +100,9 @@ def load(path: str | None = None):
         f.argtypes = args
     if path is None:
         _lib = L
+        from . import tuning
+
+        tuning.apply(L)  # the measured per-bucket tiles, when a table was saved
     return L
 
 

@@ -38,14 +38,14 @@ __device__ __forceinline__ bool chol_pivot(T d, int has_subst, double subst, T* 
 // Factor one n x n matrix (column-major, lda = n, global memory, in place).
 // Leaves info (0 ok, j+1 first failing pivot) in *s_info and, in the FMA form,
 // 1/L_ii in rdiag[i] for the solves.
-template <bool EXACT, typename T>
+template <bool EXACT, typename T, int NB = kNB>
 __device__ void chol_factor_cta(int n, T* __restrict__ a, int ldp, T* __restrict__ P, T* rdiag,
                                 int* s_info, T* s_scal, int has_subst, double subst) {
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31;
-  for (int J0 = 0; J0 < n; J0 += kNB) {
-    const int jb = min(kNB, n - J0);
+  for (int J0 = 0; J0 < n; J0 += NB) {
+    const int jb = min(NB, n - J0);
     const int rows = n - J0;
     // Phase 1+2: P = A[J0.., J0..J0+jb] - L[J0.., 0..J0] * L[J0..J0+jb, 0..J0]^T
     // (lower part).  Warp w owns columns 4w..4w+3, lanes own rows lane + 32q;

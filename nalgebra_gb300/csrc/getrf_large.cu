@@ -446,6 +446,7 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
   __shared__ int s_ticket, s_abort;
   const int tid = threadIdx.x, tr = tid % BS, tc = tid / BS;
   const int n = g.n, lower = g.lower;
+  static_assert(kTrsvThreads % 32 == 0, "warps");
   const int nblk = (n + BS - 1) / BS;
   if (tid == 0) {
     s_ticket = atomicAdd(&g.sync[0], 1);
@@ -507,24 +508,42 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
     xs[tid] = y;
   }
   __syncthreads();
-  if (tid < 32) {
-    if (lower) {
-      for (int k = 0; k < bs; ++k) {
-        const T xk = xs[k];
-        for (int i = k + 1 + tid; i < bs; i += 32) xs[i] = axpy1<false>(xs[i], -Ts[k * LD + i], xk);
-        __syncwarp();
+  // the diagonal block, 32 rows at a time: one warp solves the 32 x 32
+  // diagonal piece with shuffles, then all threads apply it to the block's
+  // remaining rows
+  const int warp = tid >> 5, lane = tid & 31;
+  const int nsub = (bs + 31) / 32;
+  for (int q = 0; q < nsub; ++q) {
+    const int sb = lower ? q * 32 : (nsub - 1 - q) * 32;
+    const int sw = min(32, bs - sb);
+    if (warp == 0) {
+      T v = lane < sw ? xs[sb + lane] : T(0);
+      if (lower) {
+#pragma unroll
+        for (int kk = 0; kk < 32; ++kk) {
+          const T xk = __shfl_sync(0xffffffffu, v, kk);
+          if (lane > kk && lane < sw) v = axpy1<false>(v, -Ts[(sb + kk) * LD + sb + lane], xk);
+        }
+      } else {
+#pragma unroll
+        for (int kk = 31; kk >= 0; --kk) {
+          if (lane == kk && kk < sw) v *= rd[sb + kk];
+          const T xk = __shfl_sync(0xffffffffu, v, kk);
+          if (lane < kk && kk < sw) v = axpy1<false>(v, -Ts[(sb + kk) * LD + sb + lane], xk);
+        }
       }
-    } else {
-      for (int k = bs - 1; k >= 0; --k) {
-        const T xk = xs[k] * rd[k];
-        for (int i = tid; i < k; i += 32) xs[i] = axpy1<false>(xs[i], -Ts[k * LD + i], xk);
-        __syncwarp();
-        if (tid == 0) xs[k] = xk;
-        __syncwarp();
-      }
+      if (lane < sw) xs[sb + lane] = v;
     }
+    __syncthreads();
+    const int i0 = lower ? sb + sw : 0, i1 = lower ? bs : sb;
+    for (int i = i0 + tid; i < i1; i += kTrsvThreads) {
+      T acc = xs[i];
+#pragma unroll 8
+      for (int k = 0; k < sw; ++k) acc = axpy1<false>(acc, -Ts[(sb + k) * LD + i], xs[sb + k]);
+      xs[i] = acc;
+    }
+    __syncthreads();
   }
-  __syncthreads();
   if (tid < bs) g.x[r0 + tid] = xs[tid];
   __threadfence();
   __syncthreads();
