@@ -33,7 +33,7 @@ from . import _lib
 from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 
 __all__ = [
-    "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch",
+    "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch", "solve_refined", "gemm",
     "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE",
 ]
 
@@ -93,7 +93,8 @@ class DeviceMatrix:
 
     # -- factorizations (consume self: the buffer is factored in place) --------
     def lu(self, flags: int = 0) -> "LU":
-        """Matrix::lu (src/linalg/decomposition.rs:48-54)."""
+        """Matrix::lu (src/linalg/decomposition.rs:48-54).  flags apply to the
+        batched kernel (n <= 128)."""
         if not self.is_square():
             raise NotImplementedError("rectangular LU is not on the GPU path")
         return LU(self, flags)
@@ -106,8 +107,9 @@ class DeviceMatrix:
 
 
 class LU:
-    """LU with partial pivoting of one square matrix (n <= 128), packed L\\U in
-    the matrix buffer, per-step pivots on the device."""
+    """LU with partial pivoting of one square matrix, packed L\\U in the matrix
+    buffer, per-step pivots on the device.  n <= 128: the shared-memory batched
+    kernel (batch of one); larger n: the blocked multi-SM factorization."""
 
     def __init__(self, m: DeviceMatrix, flags: int = 0):
         torch = _torch()
@@ -115,15 +117,30 @@ class LU:
         n = m.nrows
         self.flags = flags
         self.ipiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
-        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
-        _lib.call("nacu_dgetrf_batched", n, m.data.data_ptr(), n * n, self.ipiv.data_ptr(),
-                  self.info.data_ptr(), 1, flags, _stream_ptr())
+        self.info = torch.zeros(2, dtype=torch.int32, device="cuda")
+        self.large = n > 128
+        if self.large:
+            self._ws = torch.empty(_lib.load().nacu_getrf_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+            _lib.call("nacu_dgetrf", n, m.data.data_ptr(), n, self.ipiv.data_ptr(), self.info.data_ptr(),
+                      self._ws.data_ptr(), self._ws.numel(), _stream_ptr())
+        else:
+            _lib.call("nacu_dgetrf_batched", n, m.data.data_ptr(), n * n, self.ipiv.data_ptr(),
+                      self.info.data_ptr(), 1, flags, _stream_ptr())
 
     def solve_mut(self, b: DeviceMatrix) -> bool:
         """LU::solve_mut (src/linalg/lu.rs:242-260)."""
         n = self.lu.nrows
         assert b.nrows == n, "LU solve matrix dimension mismatch."
-        info = _torch().zeros(1, dtype=_torch().int32, device="cuda")
+        torch = _torch()
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        if self.large:
+            ok = True
+            for c in range(b.ncols):
+                _lib.call("nacu_dgetrs", n, self.lu.data.data_ptr(), n, self.ipiv.data_ptr(),
+                          b.data.data_ptr() + c * n * 8, info.data_ptr(), self._ws.data_ptr(), self._ws.numel(),
+                          _stream_ptr())
+                ok = ok and int(info.item()) == 0
+            return ok
         _lib.call("nacu_dgetrs_batched", n, b.ncols, self.lu.data.data_ptr(), n * n, self.ipiv.data_ptr(),
                   b.data.data_ptr(), n * b.ncols, info.data_ptr(), 1, self.flags, _stream_ptr())
         return int(info.item()) == 0
@@ -147,7 +164,7 @@ class LU:
         return d * (1.0 if len(self.p()) % 2 == 0 else -1.0)
 
     def is_invertible(self) -> bool:
-        return int(self.info.item()) == 0
+        return int(self.info[0].item()) == 0
 
     def l(self) -> np.ndarray:
         lu = self.lu.to_numpy()
@@ -155,6 +172,45 @@ class LU:
 
     def u(self) -> np.ndarray:
         return np.triu(self.lu.to_numpy())
+
+
+def solve_refined(a: DeviceMatrix, b: DeviceMatrix, tol_units: float = 1.0, max_iter: int = 0):
+    """The precision form for one large system (no nalgebra counterpart): FP32
+    LU with BF16-split tensor-core trailing updates, FP64 iterative refinement
+    to backward error <= tol_units * n * eps64, FP64 fallback.  ``a`` and ``b``
+    are left unchanged.  Returns (x, info) with info = dict(iters, berr,
+    fallback)."""
+    import ctypes as C
+
+    torch = _torch()
+    n = a.nrows
+    assert a.is_square() and b.nrows == n and b.ncols == 1, "one n x n system with one right-hand side"
+    x = DeviceMatrix(torch.empty(n, dtype=torch.float64, device="cuda"), n, 1)
+    ws = torch.empty(_lib.load().nacu_gesv_mixed_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    it, berr, fb = C.c_int(0), C.c_double(0.0), C.c_int(0)
+    _lib.call("nacu_dgesv_mixed_ir", n, a.data.data_ptr(), n, b.data.data_ptr(), x.data.data_ptr(),
+              float(tol_units), int(max_iter), C.byref(it), C.byref(berr), C.byref(fb), ws.data_ptr(), ws.numel(),
+              _stream_ptr())
+    return x, {"iters": it.value, "berr": berr.value, "fallback": bool(fb.value)}
+
+
+def gemm(c: DeviceMatrix, alpha: float, a: DeviceMatrix, b: DeviceMatrix, beta: float, split_slices: int = 0):
+    """Matrix::gemm (src/base/blas.rs:729-746): c = alpha a b + beta c, in
+    place.  split_slices = 1..3 selects the BF16-split tensor-core form."""
+    torch = _torch()
+    m, k = a.shape
+    k2, n = b.shape
+    assert k == k2 and c.shape == (m, n), "gemm dimension mismatch"
+    if split_slices:
+        wsb = _lib.load().nacu_gemm_split_workspace_bytes(m, n, k)
+        ws = torch.empty(wsb + 1024, dtype=torch.uint8, device="cuda")
+        wp = (ws.data_ptr() + 1023) // 1024 * 1024
+        _lib.call("nacu_dgemm_split_bf16", m, n, k, float(alpha), a.data.data_ptr(), max(m, 1), b.data.data_ptr(),
+                  max(k, 1), float(beta), c.data.data_ptr(), max(m, 1), int(split_slices), wp, wsb, _stream_ptr())
+    else:
+        _lib.call("nacu_dgemm", m, n, k, float(alpha), a.data.data_ptr(), max(m, 1), b.data.data_ptr(), max(k, 1),
+                  float(beta), c.data.data_ptr(), max(m, 1), _stream_ptr())
+    return c
 
 
 class Cholesky:

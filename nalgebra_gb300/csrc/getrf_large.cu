@@ -65,16 +65,35 @@ struct PanelArgs {
   PanelPub<T>* pub;
 };
 
-// One grid barrier per column: the candidates and the candidate rows are
-// published before it, so after it every CTA knows the pivot row's values
-// without a second exchange; row c and the pivot row are swapped by their
-// owners (nalgebra swaps whole rows, lu.rs:111-116; the columns outside the
-// panel are swapped afterwards by lu_swap_kernel).
+// The cluster form keeps each CTA's publication slots in its own shared
+// memory; the other CTAs of the cluster read them through distributed shared
+// memory.
 template <typename T>
+struct ClusterPub {
+  unsigned long long key[2];
+  int idx[2];
+  T row[2][kPanelMaxNb];
+  T diag[2][kPanelMaxNb];
+};
+template <typename T>
+__host__ __device__ constexpr size_t cluster_pub_bytes() {
+  return (sizeof(ClusterPub<T>) + 15) & ~(size_t)15;
+}
+constexpr int kClusterMaxCtas = 16;
+
+// One barrier per column: the candidates and the candidate rows are published
+// before it, so after it every CTA knows the pivot row's values without a
+// second exchange; row c and the pivot row are swapped by their owners
+// (nalgebra swaps whole rows, lu.rs:111-116; the columns outside the panel are
+// swapped afterwards by lu_swap_kernel).  CLUSTER = false: a cooperative grid,
+// the exchange through global memory and a grid barrier; CLUSTER = true: one
+// thread-block cluster, the exchange through distributed shared memory and a
+// cluster barrier (about a quarter of the grid barrier's latency).
+template <typename T, bool CLUSTER>
 __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g) {
-  cg::grid_group grid = cg::this_grid();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* P = reinterpret_cast<T*>(smem_raw);  // P[t * ldp + r]: panel column t, my row r
+  ClusterPub<T>* cpub = reinterpret_cast<ClusterPub<T>*>(smem_raw);  // cluster form only
+  T* P = reinterpret_cast<T*>(smem_raw + (CLUSTER ? cluster_pub_bytes<T>() : 0));  // P[t * ldp + r]
   __shared__ uint64_t s_key[kPanelThreads / 32];
   __shared__ int s_idx[kPanelThreads / 32];
   __shared__ T s_prow[kPanelMaxNb];
@@ -82,7 +101,14 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
   __shared__ int s_win, s_piv, s_wcta;
   __shared__ T s_inv;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int G = gridDim.x, b = blockIdx.x;
+  int G, b;
+  if constexpr (CLUSTER) {
+    G = (int)cg::this_cluster().num_blocks();
+    b = (int)cg::this_cluster().block_rank();
+  } else {
+    G = gridDim.x;
+    b = blockIdx.x;
+  }
   const int nb = g.nb, ldp = g.chunk;
   const int rb = g.j0 + b * g.chunk;
   const int nr = max(0, min(g.n, rb + g.chunk) - rb);
@@ -119,28 +145,44 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
       warp_argmax(key, idx);
       if (lane == 0) {
         s_win = idx;
-        pub->key[par][b] = key;
-        pub->idx[par][b] = (idx == 0x7fffffff) ? -1 : idx;
+        if constexpr (CLUSTER) {
+          cpub->key[par] = key;
+          cpub->idx[par] = (idx == 0x7fffffff) ? -1 : idx;
+        } else {
+          pub->key[par][b] = key;
+          pub->idx[par][b] = (idx == 0x7fffffff) ? -1 : idx;
+        }
       }
     }
     __syncthreads();
     // 2. publish my candidate row and, if I own it, row c
     {
       const int w = s_win;
+      T* prow_out = CLUSTER ? cpub->row[par] : pub->row[par][b];
+      T* diag_out = CLUSTER ? cpub->diag[par] : pub->diag[par];
       if (w != 0x7fffffff)
-        for (int t = tid; t < nb; t += kPanelThreads) pub->row[par][b][t] = P[t * ldp + (w - rb)];
+        for (int t = tid; t < nb; t += kPanelThreads) prow_out[t] = P[t * ldp + (w - rb)];
       if (c >= rb && c < rb + nr)
-        for (int t = tid; t < nb; t += kPanelThreads) pub->diag[par][t] = P[t * ldp + (c - rb)];
+        for (int t = tid; t < nb; t += kPanelThreads) diag_out[t] = P[t * ldp + (c - rb)];
     }
-    grid.sync();
+    if constexpr (CLUSTER) cg::this_cluster().sync();
+    else cg::this_grid().sync();
     // 3. the pivot: every CTA reduces the G candidates the same way
     if (warp == 0) {
       uint64_t bk = 0;
       int bi = 0x7fffffff, bw = 0;
       for (int q = lane; q < G; q += 32) {
-        const int ri = pub->idx[par][q];
+        int ri;
+        uint64_t kk;
+        if constexpr (CLUSTER) {
+          const ClusterPub<T>* rp = cg::this_cluster().map_shared_rank(cpub, q);
+          ri = rp->idx[par];
+          kk = rp->key[par];
+        } else {
+          ri = pub->idx[par][q];
+          kk = pub->key[par][q];
+        }
         if (ri < 0) continue;
-        const uint64_t kk = pub->key[par][q];
         if (bi == 0x7fffffff || kk > bk || (kk == bk && ri < bi)) {
           bk = kk;
           bi = ri;
@@ -173,11 +215,20 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
     if (piv < 0) continue;
     // 4. swap rows c and piv (their owners), from the published copies
     const bool own_c = (c >= rb && c < rb + nr), own_p = (piv >= rb && piv < rb + nr);
-    for (int t = tid; t < nb; t += kPanelThreads) {
-      s_prow[t] = pub->row[par][s_wcta][t];
-      if (own_p && piv != c) s_drow[t] = pub->diag[par][t];
+    const T* win_row;
+    const T* c_row;
+    if constexpr (CLUSTER) {
+      win_row = cg::this_cluster().map_shared_rank(cpub, s_wcta)->row[par];
+      c_row = cg::this_cluster().map_shared_rank(cpub, (c - g.j0) / g.chunk)->diag[par];
+    } else {
+      win_row = pub->row[par][s_wcta];
+      c_row = pub->diag[par];
     }
-    if (tid == 0) s_inv = T(1) / pub->row[par][s_wcta][j];
+    for (int t = tid; t < nb; t += kPanelThreads) {
+      s_prow[t] = win_row[t];
+      if (own_p && piv != c) s_drow[t] = c_row[t];
+    }
+    if (tid == 0) s_inv = T(1) / win_row[j];
     __syncthreads();
     if (piv != c) {
       for (int t = tid; t < nb; t += kPanelThreads) {
@@ -257,6 +308,7 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
       pub->npairs = k;
     }
   }
+  if constexpr (CLUSTER) cg::this_cluster().sync();  // no CTA leaves while others may read its slots
 }
 
 // ---------------------------------------------------------------------------
@@ -634,28 +686,86 @@ size_t getrf_ws_bytes() { return (sizeof(PanelPub<double>) + 255) & ~(size_t)255
 typedef int (*UpdateFn)(int m, int n, int k, const void* L21, const void* U12, void* A22, int64_t lda, void* ctx,
                         cudaStream_t s);
 
+// CTAs per cluster for the cluster-form panel (16, else 8, else 0 = grid
+// form only), from the occupancy API with the largest panel's shared memory;
+// queried once per scalar type.
+template <typename T>
+int panel_cluster_ctas() {
+  static int ctas = -1;
+  if (ctas >= 0) return ctas;
+  ctas = 0;
+  auto kern = lu_panel_kernel<T, true>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelMaxSmem) != cudaSuccess ||
+      cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return ctas;
+  }
+  for (int c = kClusterMaxCtas; c >= 8; c /= 2) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(kPanelThreads);
+    cfg.dynamicSmemBytes = kPanelMaxSmem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters >= 1) {
+      ctas = c;
+      break;
+    }
+    cudaGetLastError();
+  }
+  return ctas;
+}
+
 template <typename T>
 int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* ws, int nb, UpdateFn update,
                   void* ctx, cudaStream_t s, const char* name) {
   cudaError_t e;
   if (nb > kPanelMaxNb) nb = kPanelMaxNb;
-  const void* pk = reinterpret_cast<const void*>(lu_panel_kernel<T>);
+  const void* pk = reinterpret_cast<const void*>(lu_panel_kernel<T, false>);
   e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelMaxSmem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
+  const int cluster = panel_cluster_ctas<T>();
   const int gmax = std::min(kPanelMaxG, sm_count());
   info_init_kernel<<<1, 1, 0, s>>>(info);
   for (int j0 = 0; j0 < n; j0 += nb) {
     const int jb = std::min(nb, n - j0);
     const int rows = n - j0;
-    const int max_rows = (int)(kPanelMaxSmem / ((size_t)jb * sizeof(T)));
-    int G = std::max((rows + kPanelRowsPerCta - 1) / kPanelRowsPerCta, (rows + max_rows - 1) / max_rows);
-    G = std::max(1, std::min(G, gmax));
-    const int chunk = (rows + G - 1) / G;
-    if (chunk > max_rows) return record_arg_error(-1, "getrf: n too large for the shared-memory panel");
-    PanelArgs<T> pa{n, A, lda, j0, jb, chunk, ipiv, info, reinterpret_cast<PanelPub<T>*>(ws)};
-    void* args[] = {&pa};
-    e = cudaLaunchCooperativeKernel(pk, G, kPanelThreads, args, (size_t)chunk * jb * sizeof(T), s);
-    if (e != cudaSuccess) return record_cuda_error(e, name);
+    PanelArgs<T> pa{n, A, lda, j0, jb, 0, ipiv, info, reinterpret_cast<PanelPub<T>*>(ws)};
+    const int cchunk = cluster ? (rows + cluster - 1) / cluster : 0;
+    const size_t csmem = cluster_pub_bytes<T>() + (size_t)cchunk * jb * sizeof(T);
+    if (cluster && csmem <= kPanelMaxSmem) {
+      pa.chunk = cchunk;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cluster);
+      cfg.blockDim = dim3(kPanelThreads);
+      cfg.dynamicSmemBytes = csmem;
+      cfg.stream = s;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = cluster;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      e = cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, true>, pa);
+      if (e != cudaSuccess) return record_cuda_error(e, name);
+    } else {
+      const int max_rows = (int)(kPanelMaxSmem / ((size_t)jb * sizeof(T)));
+      int G = std::max((rows + kPanelRowsPerCta - 1) / kPanelRowsPerCta, (rows + max_rows - 1) / max_rows);
+      G = std::max(1, std::min(G, gmax));
+      const int chunk = (rows + G - 1) / G;
+      if (chunk > max_rows) return record_arg_error(-1, "getrf: n too large for the shared-memory panel");
+      pa.chunk = chunk;
+      void* args[] = {&pa};
+      e = cudaLaunchCooperativeKernel(pk, G, kPanelThreads, args, (size_t)chunk * jb * sizeof(T), s);
+      if (e != cudaSuccess) return record_cuda_error(e, name);
+    }
     if (n > jb) lu_swap_kernel<T><<<(n - jb + 7) / 8, 256, 0, s>>>(n, A, lda, pa.pub, j0, jb);
     const int rest = n - j0 - jb;
     if (rest > 0) {

@@ -27,89 +27,111 @@ namespace {
 
 constexpr int kLuThreads = 128;
 
+// Pivot of column c (icamax over rows c..n-1, one warp): s_piv[c] (c itself
+// for an all-zero column, which is skipped: lu.rs:107-110), and in s_rcp:
+// [0] = 1/pivot, [n+1] = the pivot, [n+2] = the old diagonal a[c][c].  Each
+// lane scans the rows it updated itself (r = c + lane + 32k), so the scan
+// needs no barrier after that update.
+template <typename T>
+__device__ __forceinline__ void lu_find_pivot(int n, int c, const T* colc, int* s_piv, T* s_rcp, int lane) {
+  uint64_t key = 0;
+  int idx = 0x7fffffff;
+  for (int r = c + lane; r < n; r += 32) {
+    const uint64_t k = pivot_key(colc[r], r == c);
+    if (idx == 0x7fffffff || k > key) {
+      key = k;
+      idx = r;
+    }
+  }
+  warp_argmax(key, idx);
+  __syncwarp();
+  if (lane == 0) {
+    const T d = colc[idx];
+    s_piv[c] = (d == T(0)) ? c : idx;
+    s_rcp[0] = (d == T(0)) ? T(0) : T(1) / d;  // one division per step, not per thread
+    s_rcp[n + 1] = d;
+    s_rcp[n + 2] = colc[c];
+  }
+}
+
 template <typename T, bool EXACT>
 __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_info, T* s_rcp, bool factor) {
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
   const int ncols = n + nrhs;
+  const int warp = tid >> 5, lane = tid & 31;
   if (factor) {
+    // Two barriers per step.  Phase A swaps rows i and piv in every column but
+    // i and writes column i as [pivot; multipliers].  Phase B is the rank-1
+    // update: warp 0 updates column i+1 and at once finds its pivot for the
+    // next step (look-ahead), the other warps update columns i+2.. (the
+    // right-hand sides included).  Every element still receives nalgebra's
+    // operations in nalgebra's order.
+    if (warp == 0 && n > 0) lu_find_pivot<T>(n, 0, sa, s_piv, s_rcp, lane);
+    __syncthreads();
     for (int i = 0; i < n; ++i) {
       T* coli = sa + (size_t)i * ld;
-      // icamax over rows i..n-1 of column i (one warp).
-      if (tid < 32) {
-        uint64_t key = 0;
-        int idx = 0x7fffffff;
-        for (int r = i + tid; r < n; r += 32) {
-          uint64_t k = pivot_key(coli[r], r == i);
-          if (idx == 0x7fffffff || k > key) {
-            key = k;
-            idx = r;
-          }
-        }
-        warp_argmax(key, idx);
-        if (tid == 0) {
-          s_piv[i] = idx;
-          const T d = coli[idx];
-          s_rcp[0] = (d == T(0)) ? T(0) : T(1) / d;  // one division per step, not per thread
-        }
-      }
-      __syncthreads();
       const int piv = s_piv[i];
-      const T diag = coli[piv];
-      if (diag == T(0)) {  // lu.rs:107-110: all-zero column, skipped
-        if (tid == 0) s_piv[i] = i;
-        __syncthreads();
-        continue;
-      }
+      const T diag = s_rcp[n + 1];
       const T inv_diag = s_rcp[0];
-      // Swap rows i and piv in every column but i (L part, U part and the
-      // right-hand sides), and rewrite column i as [diag; coeffs * inv_diag].
-      if (piv != i) {
-        for (int c = tid; c < ncols; c += nthr) {
-          if (c == i) continue;
-          T* col = sa + (size_t)c * ld;
-          T t = col[i];
-          col[i] = col[piv];
-          col[piv] = t;
-        }
-      }
-      const T old_ii = coli[i];
-      __syncthreads();
-      for (int r = i + 1 + tid; r < n; r += nthr) {
-        T v = (r == piv) ? old_ii : coli[r];
-        if constexpr (EXACT) {
-          coli[r] = (sizeof(T) == 8) ? (T)__dmul_rn((double)v, (double)inv_diag)
-                                     : (T)__fmul_rn((float)v, (float)inv_diag);
-        } else {
-          coli[r] = v * inv_diag;
-        }
-      }
-      if (tid == 0) coli[i] = diag;
-      __syncthreads();
-      // Rank-1 update of the trailing block (rows i+1..n-1, columns i+1..ncols-1):
-      // a[r][c] += (-a[i][c]) * l[r], one flattened index per element.
-      const int m = n - 1 - i;
-      const int w = ncols - 1 - i;
-      const int total = m * w;
-      if (m > 0) {
-        int e = tid;
-        int cq = e / m;
-        int rr = e - cq * m;
-        const int dq = nthr / m;
-        const int dr = nthr - dq * m;
-        T* base = sa + (size_t)(i + 1) * ld;
-        const T* lcol = coli + i + 1;
-        for (; e < total; e += nthr) {
-          T* col = base + (size_t)cq * ld;
-          const T u = col[i];
-          col[i + 1 + rr] = axpy1<EXACT>(col[i + 1 + rr], -u, lcol[rr]);
-          rr += dr;
-          cq += dq;
-          if (rr >= m) {
-            rr -= m;
-            ++cq;
+      const T old_ii = s_rcp[n + 2];
+      const bool skip = (diag == T(0));  // lu.rs:107-110: all-zero column, no elimination
+      if (!skip) {
+        if (piv != i) {
+          for (int c = tid; c < ncols; c += nthr) {
+            if (c == i) continue;
+            T* col = sa + (size_t)c * ld;
+            const T t = col[i];
+            col[i] = col[piv];
+            col[piv] = t;
           }
         }
+        for (int r = i + 1 + tid; r < n; r += nthr) {
+          const T v = (r == piv) ? old_ii : coli[r];
+          if constexpr (EXACT) {
+            coli[r] = (sizeof(T) == 8) ? (T)__dmul_rn((double)v, (double)inv_diag)
+                                       : (T)__fmul_rn((float)v, (float)inv_diag);
+          } else {
+            coli[r] = v * inv_diag;
+          }
+        }
+        if (tid == 0) coli[i] = diag;
+      }
+      __syncthreads();
+      const int m = n - 1 - i;
+      if (m > 0) {
+        T* coln = sa + (size_t)(i + 1) * ld;
+        if (!skip) {
+          const T* lcol = coli + i + 1;
+          if (warp == 0) {
+            const T u = coln[i];
+            for (int r = lane; r < m; r += 32) coln[i + 1 + r] = axpy1<EXACT>(coln[i + 1 + r], -u, lcol[r]);
+          } else {
+            // a[r][c] += (-a[i][c]) * l[r] for columns i+2.., one flattened
+            // index per element over warps 1..
+            const int w = ncols - 2 - i;
+            const int total = m * w;
+            const int nt = nthr - 32;
+            int e = tid - 32;
+            int cq = e / m;
+            int rr = e - cq * m;
+            const int dq = nt / m;
+            const int dr = nt - dq * m;
+            T* base = sa + (size_t)(i + 2) * ld;
+            for (; e < total; e += nt) {
+              T* col = base + (size_t)cq * ld;
+              const T u = col[i];
+              col[i + 1 + rr] = axpy1<EXACT>(col[i + 1 + rr], -u, lcol[rr]);
+              rr += dr;
+              cq += dq;
+              if (rr >= m) {
+                rr -= m;
+                ++cq;
+              }
+            }
+          }
+        }
+        if (warp == 0) lu_find_pivot<T>(n, i + 1, coln, s_piv, s_rcp, lane);
       }
       __syncthreads();
     }
@@ -158,7 +180,6 @@ __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_inf
     for (int i = tid; i < n; i += nthr) s_rcp[1 + i] = T(1) / sa[(size_t)i * ld + i];
     __syncthreads();
   }
-  const int warp = tid >> 5, lane = tid & 31;
   for (int c = warp; c < nrhs; c += (nthr >> 5)) {
     T* bcol = sa + (size_t)(n + c) * ld;
     for (int i = n - 1; i >= 0; --i) {
@@ -188,8 +209,8 @@ __global__ void __launch_bounds__(kLuThreads) lu_batched_kernel(int n, int nrhs,
   const int ld = n | 1;
   const int ncols = n + nrhs;
   T* sa = reinterpret_cast<T*>(smem_raw);
-  T* s_rcp = sa + (size_t)ld * ncols;  // [0]: 1/pivot of the current step; [1+i]: 1/U_ii
-  int* s_piv = reinterpret_cast<int*>(s_rcp + n + 1);
+  T* s_rcp = sa + (size_t)ld * ncols;  // [0]: 1/pivot, [n+1], [n+2]: the step's scalars; [1+i]: 1/U_ii
+  int* s_piv = reinterpret_cast<int*>(s_rcp + n + 3);
   int* s_info = s_piv + n;
   const int tid = threadIdx.x;
   for (int s = blockIdx.x; s < batch; s += gridDim.x) {
@@ -234,7 +255,7 @@ __global__ void __launch_bounds__(kLuThreads) lu_batched_kernel(int n, int nrhs,
 template <typename T>
 size_t lu_smem_bytes(int n, int nrhs) {
   const int ld = n | 1;
-  return (size_t)ld * (n + nrhs) * sizeof(T) + (size_t)(n + 1) * sizeof(T) + (size_t)(n + 1) * sizeof(int);
+  return (size_t)ld * (n + nrhs) * sizeof(T) + (size_t)(n + 3) * sizeof(T) + (size_t)(n + 1) * sizeof(int);
 }
 
 template <typename T>

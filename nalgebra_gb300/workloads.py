@@ -141,8 +141,14 @@ def conditioned_torch(n: int, cond: float, seed: int = 0, device="cuda"):
     import torch
 
     g = torch.Generator(device=device).manual_seed(seed)
-    u, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device=device, generator=g))
-    v, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device=device, generator=g))
+    gu = torch.randn(n, n, dtype=torch.float64, device=device, generator=g)
+    gv = torch.randn(n, n, dtype=torch.float64, device=device, generator=g)
+    try:
+        u, _ = torch.linalg.qr(gu)
+        v, _ = torch.linalg.qr(gv)
+    except RuntimeError:  # torch's linalg library unavailable (e.g. under a profiler): QR on the host
+        u = torch.from_numpy(np.linalg.qr(gu.cpu().numpy())[0]).to(device)
+        v = torch.from_numpy(np.linalg.qr(gv.cpu().numpy())[0]).to(device)
     s = torch.from_numpy(_sigma(n, cond, np.random.default_rng(seed))).to(device)
     a = (u * s) @ v.T
     b = torch.randn(n, dtype=torch.float64, device=device, generator=g)

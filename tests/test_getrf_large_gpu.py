@@ -73,3 +73,22 @@ def test_zero_column_and_singular(cuda):
     assert info == 71
     assert np.array_equal(ipiv, ipiv_o)
     assert info2 == 71  # U_70,70 == 0: the solve reports it
+
+
+def test_grid_form_panels_large_n(cuda):
+    """n = 6600: the first panels (rows above what a 16-CTA cluster holds in
+    shared memory) take the grid-barrier form, the rest the cluster form.
+    Pivots against LAPACK's partial pivoting (same rule: largest |x|, first
+    on ties) and the backward error."""
+    sla = pytest.importorskip("scipy.linalg")
+    n = 6600
+    rng = np.random.default_rng(66)
+    a = rng.standard_normal((n, n))
+    b = rng.standard_normal(n)
+    lu, ipiv, info, x, info2 = _getrf(cuda, a, b)
+    assert info == 0 and info2 == 0
+    _, piv_ref = sla.lu_factor(a, check_finite=False)
+    assert np.array_equal(ipiv, piv_ref)
+    r = b - a @ x
+    berr = np.abs(r).max() / (np.abs(a).sum(axis=1).max() * np.abs(x).max() + np.abs(b).max())
+    assert berr <= 10 * n * EPS64

@@ -93,3 +93,22 @@ def test_argument_errors(cuda):
     rc = L.nacu_dgesv_mixed_ir(4, A.data_ptr(), 4, A.data_ptr(), A.data_ptr(), 1.0, 5, None, None, None,
                                ws.data_ptr(), ws.numel(), None)
     assert rc == -11
+
+
+def test_mirror_large_lu_and_refined_solve(cuda):
+    from nalgebra_gb300 import DeviceMatrix, gemm, solve_refined
+
+    n = 300
+    a, b = workloads.conditioned(n, 1e3, seed=21)
+    lu = DeviceMatrix.from_numpy(a).lu()
+    assert lu.large and lu.is_invertible()
+    lu_o, ipiv_o, _ = O.lu(a)
+    assert [p for p in lu.p()] == [(i, int(p)) for i, p in enumerate(ipiv_o) if p != i]
+    x = lu.solve(DeviceMatrix.from_numpy(b.reshape(-1, 1))).to_numpy().ravel()
+    assert _berr(a, x, b) <= 10 * n * EPS64
+    xr, st = solve_refined(DeviceMatrix.from_numpy(a), DeviceMatrix.from_numpy(b.reshape(-1, 1)))
+    assert not st["fallback"] and st["berr"] <= n * EPS64
+    assert _berr(a, xr.to_numpy().ravel(), b) <= n * EPS64
+    c = DeviceMatrix.from_numpy(np.zeros((n, 1)))
+    gemm(c, 1.0, DeviceMatrix.from_numpy(a), xr, 0.0)
+    assert np.allclose(c.to_numpy().ravel(), b, rtol=0, atol=1e-10 * np.abs(b).max())
