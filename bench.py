@@ -112,6 +112,13 @@ def dist_env():
 RAGGED = dict(count=20000, n_lo=8, n_hi=256, nrhs=4, seed=0)
 
 
+def active_buckets(n_max):
+    """Size buckets of the ragged launch that can hold an order <= n_max (bucket b
+    holds orders above the previous bound; bucket 0 is always launched)."""
+    bounds = (32, 64, 96, 128, 192, 256, 384, 512)
+    return 1 + sum(1 for b in range(1, len(bounds)) if bounds[b - 1] < n_max)
+
+
 def ragged_flops(ns, nrhs):
     ns = ns.astype(np.float64)
     return float(np.sum(ns ** 3 / 3.0 + nrhs * 2.0 * ns ** 2))
@@ -342,9 +349,15 @@ def bench_ragged_ours(args, rank, world):
                      "hbm_frac_of_measured": (ragged_bytes(ns, nrhs) / (kern_ms * 1e-3)) / (read_peaks().get("hbm_gbs", 6794.8) * 1e9)},
         "e2e": {"value": count / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "gpu_launches": args.steps,
+        # per step: the mixed form launches chol_mixed_kernel + chol_mixed_fallback_kernel; the FP64
+        # form three sort kernels and one persistent launch per size bucket that can hold this batch
+        "gpu_launches": args.steps * (2 if use_mixed else (1 if args.single_launch else 3 + active_buckets(n_max))),
         "clocks": clk.summary(),
     }
+    traffic = PROFILED_TRAFFIC.get("chol_mixed_kernel" if use_mixed else "chol_ragged_kernel")
+    if traffic is not None and count == RAGGED["count"]:
+        res["roofline"]["traffic"] = traffic[0]
+        res["roofline"]["traffic_source"] = traffic[1]
     return res, dict(ns=ns, aoff=aoff, boff=boff, a_host=a_host, b_host=b_host, nrhs=nrhs)
 
 
@@ -392,6 +405,16 @@ def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_
 
 
 _FP64_PEAK = {}
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# dominant kernel, from one ncu capture of a smaller case of the same workload,
+# scaled to a full launch by the systems processed (traffic grows with them).
+PROFILED_TRAFFIC = {
+    # 1.342 GB read + 0.245 GB written for a 2000-system slice of the same size
+    # distribution (profiles/chol_mixed_kernel__ragged_spd_2000.md), x 10 systems
+    "chol_mixed_kernel": (15.87e9, "ncu capture of 2000 systems, scaled x10 by systems processed "
+                                   "(profiles/chol_mixed_kernel__ragged_spd_2000.md)"),
+}
 
 
 def ctypes_probe(L):

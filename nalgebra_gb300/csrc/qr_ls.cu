@@ -103,6 +103,7 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
   }
   double* a = g.A + g.aoff[s];
   double* b = g.boff ? g.B + g.boff[s] : nullptr;
+  double* s_coef = s_red + 4 + 4 * kQrNB;
   for (int J0 = 0; J0 < n; J0 += kQrNB) {
     const int jb = min(kQrNB, n - J0);
     const int rows = m - J0;
@@ -154,14 +155,19 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
       warp_reduce_scatter<kQrNB>(dots);
       if (lane < kQrNB) s_red[4 + warp * kQrNB + lane] = dots[0];
       __syncthreads();
-      double coef[kQrNB];  // -tau * (v^T P_c), zero for columns outside j+1..jb-1
-#pragma unroll
-      for (int c = 0; c < kQrNB; ++c) {
+      // coef_c = -tau * (v^T P_c), formed once per column by kQrNB threads
+      // (every thread forming all of them cost more FP64 issue slots than the
+      // panel update itself); zero outside columns j+1..jb-1
+      if (tid < kQrNB) {
         double d = 0.0;
 #pragma unroll
-        for (int w = 0; w < kQrThreads / 32; ++w) d += s_red[4 + w * kQrNB + c];
-        coef[c] = (c > j && c < jb) ? -tau * d : 0.0;
+        for (int w = 0; w < kQrThreads / 32; ++w) d += s_red[4 + w * kQrNB + tid];
+        s_coef[tid] = (tid > j && tid < jb) ? -tau * d : 0.0;
       }
+      __syncthreads();
+      double coef[kQrNB];
+#pragma unroll
+      for (int c = 0; c < kQrNB; ++c) coef[c] = s_coef[c];
       for (int r = j + tid; r < rows; r += kQrThreads) {
         const double v = pj[r];
 #pragma unroll
@@ -340,7 +346,7 @@ __global__ void __launch_bounds__(kQrThreads, 4) qr_batched_kernel(QrArgs g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_t[kSTSize];
   __shared__ double s_dstd[kQrMaxN];
-  __shared__ double s_red[4 + 4 * kQrNB];
+  __shared__ double s_red[4 + 5 * kQrNB];  // block sums | 4 warps x NB dots | NB panel coefficients
   __shared__ double s_misc[2 + 2 * kQrMaxN];
   __shared__ int s_item;
   const int ldp = g.m_max | 1;

@@ -95,3 +95,19 @@ def test_beta_zero_never_reads_c_and_k_zero(cuda, kind):
     a0, b0, c0 = _mats(5, 6, 0, False, 2)
     got = _run(cuda, kind, a0, b0, c0, 1.0, 3.0)
     assert np.allclose(got, 3.0 * c0)
+
+
+def test_split_extreme_scales_and_zero_rows(cuda):
+    """Row/column scales far outside FP32's range (2^-600 .. 2^600 per row of A,
+    2^-400 .. 2^400 per column of B) and an all-zero row: the epilogue rebuilds
+    the FP64 result exactly from the FP32 accumulator and the two exponents."""
+    rng = np.random.default_rng(12)
+    m, n, k = 160, 272, 96
+    a = rng.standard_normal((m, k)) * 2.0 ** rng.integers(-600, 601, size=(m, 1))
+    b = rng.standard_normal((k, n)) * 2.0 ** rng.integers(-400, 401, size=(1, n))
+    a[7, :] = 0.0
+    got = _run(cuda, "split", a, b, np.zeros((m, n)), 1.0, 0.0, 3)
+    ref = O.gemm_dot2(1.0, a, b)
+    scale = np.abs(a) @ np.abs(b)
+    assert np.all(np.abs(got - ref) <= 1e-5 * scale)
+    assert np.all(got[7, :] == 0.0)
