@@ -147,6 +147,26 @@ def backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample)
     return worst
 
 
+def forward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample):
+    """Max over a sample of ||x - x_ref||_inf / ||x_ref||_inf per right-hand
+    side, x_ref the oracle's FP64 solve (nalgebra's Cholesky::solve restated)."""
+    import oracle as O
+
+    worst = 0.0
+    for s in sample:
+        n = int(ns[s])
+        a = a_host[aoff[s]:aoff[s] + n * n].reshape(n, n).T
+        b = b_host[boff[s]:boff[s] + n * nrhs].reshape(nrhs, n).T
+        x = x_host[boff[s]:boff[s] + n * nrhs].reshape(nrhs, n).T
+        l, info = O.cholesky(a)
+        if info != 0:
+            continue
+        xr = O.cholesky_solve(l, b)
+        fe = np.max(np.max(np.abs(x - xr), axis=0) / np.max(np.abs(xr), axis=0))
+        worst = max(worst, float(fe))
+    return worst
+
+
 def bench_ragged_ours(args, rank, world):
     import torch
 
@@ -232,6 +252,7 @@ def bench_ragged_ours(args, rank, world):
     b_host = b0.cpu().numpy()
     x_host = B.cpu().numpy()
     berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample)
+    ferr64 = forward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample[:16])
 
     # precision form: FP32 factor + FP64 refinement, same inputs, one launch
     mixed = bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host)
@@ -299,7 +320,8 @@ def bench_ragged_ours(args, rank, world):
     flops = ragged_flops(ns, nrhs)
     achieved = flops / (kern_ms * 1e-3)
     fp64_form = {"solves_per_s": count / (kern_ms * 1e-3), "gflops": achieved / 1e9, "ms_per_step": kern_ms,
-                 "frac_of_fp64_peak": achieved / peak, "backward_error_max_over_sample_in_n_eps": berr}
+                 "frac_of_fp64_peak": achieved / peak, "backward_error_max_over_sample_in_n_eps": berr,
+                 "forward_error_max_vs_fp64_oracle_over_sample": ferr64}
     mixed["frac_of_fp64_peak_executed"] = mixed["fp64_flops_executed_per_launch"] / (mixed["ms_per_step"] * 1e-3) / peak
     head_ms = mixed["ms_per_step"] if use_mixed else kern_ms
     value = count * world / (head_ms * 1e-3)
@@ -394,14 +416,17 @@ def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_
         raise RuntimeError("mixed form: systems reported not SPD")
     rng = np.random.default_rng(2)
     sample = rng.choice(count, size=min(48, count), replace=False)
-    berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, out.data.cpu().numpy(), nrhs, sample)
+    x_host = out.data.cpu().numpy()
+    berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample)
+    ferr = forward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample[:16])
     n = ns.astype(np.float64)
     fp64_flops = float(np.sum(np.abs(it) * 2.0 * nrhs * n * n))  # FP64 residual work actually executed
     return {"solves_per_s": count / (ms * 1e-3), "ms_per_step": ms,
             "gflops_fp64_equivalent": ragged_flops(ns, nrhs) / (ms * 1e-3) / 1e9,
             "fp64_flops_executed_per_launch": fp64_flops,
             "residuals_per_system_mean": float(np.mean(np.abs(it))), "fp64_fallbacks": int(np.sum(it < 0)),
-            "backward_error_max_over_sample_in_n_eps": berr, "_objects": (chol, rhs, out)}
+            "backward_error_max_over_sample_in_n_eps": berr,
+            "forward_error_max_vs_fp64_oracle_over_sample": ferr, "_objects": (chol, rhs, out)}
 
 
 _FP64_PEAK = {}
@@ -657,7 +682,7 @@ def bench_adjoint_ours(args, rank, world):
 
             def bwd():
                 _lib.call(f"nacu_{pre}posv_logdet_backward", n, (A if rec else Lf).data_ptr(), n * n, 1 if rec else 0,
-                          X.data_ptr(), Wt.data_ptr(), dA.data_ptr(), db.data_ptr(), info.data_ptr(), count, sp)
+                          X.data_ptr(), Wt.data_ptr(), None, dA.data_ptr(), db.data_ptr(), info.data_ptr(), count, sp)
 
             for _ in range(args.warmup):
                 fwd(); bwd()
@@ -813,7 +838,7 @@ def bench_mixed_lu_ours(args, rank, world):
                 _lib.call("nacu_dgetrs", n, work.data_ptr(), n, ipiv.data_ptr(), x.data_ptr(), info[1:].data_ptr(),
                           wsf.data_ptr(), wsf.numel(), sp)
 
-            res = {}
+            res, xs = {}, {}
             steps = max(1, args.steps if n <= 4096 else min(args.steps, 3))
             for name, fn in (("mixed_ir", mixed), ("fp64", plain)):
                 times = []
@@ -830,6 +855,7 @@ def bench_mixed_lu_ours(args, rank, world):
                             times.append(e0.elapsed_time(e1))
                 ms = float(np.median(times))
                 xr = x.clone()
+                xs[name] = xr
                 r = b - (A.view(n, n).t() @ xr)
                 be = float(r.abs().max() / (A.view(n, n).abs().sum(dim=0).max() * xr.abs().max() + b.abs().max()))
                 res[name] = {"ms": ms, "solves_per_s": 1e3 / ms, "gflops_fp64_equivalent": flops / (ms * 1e-3) / 1e9,
@@ -838,6 +864,8 @@ def bench_mixed_lu_ours(args, rank, world):
                 if name == "mixed_ir":
                     res[name].update({"refinement_steps": it.value, "fp64_fallback": bool(fb.value)})
             res["speedup_mixed_over_fp64"] = res["fp64"]["ms"] / res["mixed_ir"]["ms"]
+            res["mixed_ir"]["forward_error_vs_fp64_form"] = float((xs["mixed_ir"] - xs["fp64"]).abs().max() /
+                                                                  xs["fp64"].abs().max())
             forms[f"n{n}_cond{cond:.0e}"] = res
             if headline is None or (n == max(sizes) and cond == 1e5):
                 headline = (n, cond, res)

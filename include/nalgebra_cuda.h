@@ -212,17 +212,19 @@ int nacu_dposv_logdet_forward(int n, const double* A, int64_t strideA, const dou
 int nacu_sposv_logdet_forward(int n, const float* A, int64_t strideA, const float* B, float* X, float* L,
                               float* logdet, int32_t* info, int batch, nacu_stream_t stream);
 
-/* Backward of l = sum_s w_s^T x_s + logdet A_s: db[s*n..] = A^-1 w and the
- * gradient with respect to the lower-triangle entries of A in dA's lower
- * triangle (dA_ii = -v_i x_i + (A^-1)_ii, dA_ij = -(v_i x_j + v_j x_i) +
- * 2 (A^-1)_ij for i > j, v = A^-1 w; zeros above).  AL holds the stored factor
- * L (recompute = 0) or the original A (recompute = 1: the factor is rebuilt,
+/* Reverse mode: given the cotangents W = dl/dx (n per system) and G =
+ * dl/dlogdet (one per system; NULL: all 1, i.e. l = sum_s w_s^T x_s +
+ * logdet A_s), db[s*n..] = A^-T w = dl/db and dA's lower triangle = dl/dA with
+ * respect to the lower-triangle entries that nalgebra reads
+ * (dA_ii = -v_i x_i + g (A^-1)_ii, dA_ij = -(v_i x_j + v_j x_i) + 2 g (A^-1)_ij
+ * for i > j, v = A^-1 w; zeros above).  AL holds the stored factor L
+ * (recompute = 0) or the original A (recompute = 1: the factor is rebuilt,
  * trading n^3/3 flops for n^2 stored values per matrix). */
 int nacu_dposv_logdet_backward(int n, const double* AL, int64_t strideA, int recompute, const double* X,
-                               const double* W, double* dA, double* db, int32_t* info, int batch,
-                               nacu_stream_t stream);
+                               const double* W, const double* G, double* dA, double* db, int32_t* info,
+                               int batch, nacu_stream_t stream);
 int nacu_sposv_logdet_backward(int n, const float* AL, int64_t strideA, int recompute, const float* X,
-                               const float* W, float* dA, float* db, int32_t* info, int batch,
+                               const float* W, const float* G, float* dA, float* db, int32_t* info, int batch,
                                nacu_stream_t stream);
 
 /* ---- Householder QR and least squares (batched, tall-skinny) ------------- */

@@ -34,6 +34,7 @@ from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 
 __all__ = [
     "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch", "solve_refined", "gemm",
+    "PosvLogdet",
     "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE",
 ]
 
@@ -528,3 +529,62 @@ class QRBatch:
     def diag_host(self) -> np.ndarray:
         self.factor()
         return self.diag.cpu().numpy()[: len(self.batch) * self.n].reshape(len(self.batch), self.n)
+
+
+class PosvLogdet:
+    """The differentiation form (no nalgebra counterpart: nalgebra has no
+    autodiff): a batch of equal-order SPD systems (n <= 128), f64 or f32,
+
+        x_s = A_s^-1 b_s,   logdet_s = ln det A_s      (forward)
+
+    and the reverse-mode adjoint
+
+        (x_bar, logdet_bar) -> (A_bar, b_bar)          (backward)
+
+    where A_bar is the gradient with respect to the lower-triangle entries
+    nalgebra reads (off-diagonal entries count for A_ij and A_ji).  The
+    store form keeps the Cholesky factor from the forward pass; the recompute
+    form keeps nothing and refactors A in the backward pass (n^2 values per
+    matrix saved for n^3/3 extra flops).  A is (batch, n*n) column-major rows,
+    b (batch, n); device tensors."""
+
+    def __init__(self, n: int, batch: int, dtype="float64", recompute: bool = False):
+        torch = _torch()
+        self.n, self.batch = int(n), int(batch)
+        self.tdt = torch.float64 if str(dtype).endswith("64") else torch.float32
+        self.pre = "d" if self.tdt == torch.float64 else "s"
+        self.recompute = bool(recompute)
+        self.L = None if self.recompute else torch.zeros((self.batch, self.n * self.n), dtype=self.tdt,
+                                                          device="cuda")
+        self.info = torch.zeros(self.batch, dtype=torch.int32, device="cuda")
+        self._A = self._x = None
+
+    def forward(self, A, b):
+        torch = _torch()
+        A = A.to(device="cuda", dtype=self.tdt).contiguous()
+        b = b.to(device="cuda", dtype=self.tdt).contiguous()
+        x = torch.empty((self.batch, self.n), dtype=self.tdt, device="cuda")
+        logdet = torch.empty(self.batch, dtype=self.tdt, device="cuda")
+        _lib.call(f"nacu_{self.pre}posv_logdet_forward", self.n, A.data_ptr(), self.n * self.n, b.data_ptr(),
+                  x.data_ptr(), None if self.L is None else self.L.data_ptr(), logdet.data_ptr(),
+                  self.info.data_ptr(), self.batch, _stream_ptr())
+        self._A, self._x = A, x
+        return x, logdet
+
+    def backward(self, x_bar, logdet_bar=None):
+        """Returns (A_bar, b_bar); logdet_bar None means 1 for every system."""
+        torch = _torch()
+        if self._x is None:
+            raise RuntimeError("backward before forward")
+        w = x_bar.to(device="cuda", dtype=self.tdt).contiguous()
+        g = None if logdet_bar is None else logdet_bar.to(device="cuda", dtype=self.tdt).contiguous()
+        dA = torch.empty((self.batch, self.n * self.n), dtype=self.tdt, device="cuda")
+        db = torch.empty((self.batch, self.n), dtype=self.tdt, device="cuda")
+        src = self._A if self.recompute else self.L
+        _lib.call(f"nacu_{self.pre}posv_logdet_backward", self.n, src.data_ptr(), self.n * self.n,
+                  1 if self.recompute else 0, self._x.data_ptr(), w.data_ptr(), None if g is None else g.data_ptr(),
+                  dA.data_ptr(), db.data_ptr(), self.info.data_ptr(), self.batch, _stream_ptr())
+        return dA, db
+
+    def is_ok(self) -> np.ndarray:
+        return self.info.cpu().numpy() == 0

@@ -48,8 +48,8 @@ SIGNATURES = {
                                      _d, _i, _vp]),
     "nacu_dposv_logdet_forward": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "nacu_sposv_logdet_forward": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
-    "nacu_dposv_logdet_backward": (_i, [_i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
-    "nacu_sposv_logdet_backward": (_i, [_i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
+    "nacu_dposv_logdet_backward": (_i, [_i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
+    "nacu_sposv_logdet_backward": (_i, [_i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "nacu_qr_workspace_bytes": (_sz, [_i]),
     "nacu_dgels_batched": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_getrf_workspace_bytes": (_sz, [_i]),

@@ -6,15 +6,16 @@
 // logdet A = sum ln(L_ii^2); the factor L is written out (the "store" form)
 // or discarded (the "recompute" form keeps only A).
 //
-// Backward, for the loss  l = sum_s w_s^T x_s + logdet A_s  (nalgebra has no
-// autodiff; this is the chosen differentiation form):
+// Backward, for the cotangents w = dl/dx and g = dl/dlogdet of a loss l
+// (default g = 1: the loss l = sum_s w_s^T x_s + logdet A_s; nalgebra has no
+// autodiff, this is the chosen differentiation form):
 //   v  = A^-1 w                       (dl/db)
-//   Abar = -v x^T + A^-1              (dl/dA for an unstructured A)
+//   Abar = -v x^T + g A^-1            (dl/dA for an unstructured A)
 // nalgebra reads only the lower triangle, so the parameters are the lower
 // entries theta_ij (i >= j) with A_ij = A_ji = theta_ij; the gradient
 // returned in dA's lower triangle is
-//   dA_ii = Abar_ii = -v_i x_i + (A^-1)_ii,
-//   dA_ij = Abar_ij + Abar_ji = -(v_i x_j + v_j x_i) + 2 (A^-1)_ij  (i > j),
+//   dA_ii = Abar_ii = -v_i x_i + g (A^-1)_ii,
+//   dA_ij = Abar_ij + Abar_ji = -(v_i x_j + v_j x_i) + 2 g (A^-1)_ij  (i > j),
 // which is what central differences on theta_ij measure.  (Giles 2008,
 // "Collected matrix derivative results for forward and reverse mode AD";
 // Murray 2016, "Differentiation of the Cholesky decomposition".)
@@ -230,7 +231,8 @@ __global__ void __launch_bounds__(kAdjThreads) adj_forward_kernel(int n, const T
 template <typename T>
 __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const T* __restrict__ AL, int64_t strideA,
                                                                    int recompute, const T* __restrict__ X,
-                                                                   const T* __restrict__ Wt, T* __restrict__ dA,
+                                                                   const T* __restrict__ Wt,
+                                                                   const T* __restrict__ Glog, T* __restrict__ dA,
                                                                    T* __restrict__ db, int32_t* __restrict__ info,
                                                                    int batch) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -270,11 +272,13 @@ __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const 
       __syncthreads();
       for (int i = tid; i < n; i += blockDim.x) db[(size_t)s * n + i] = v[i];
       T* g = dA + (size_t)s * strideA;
+      const T gl = Glog ? Glog[s] : T(1);
+      const T gl2 = T(2) * gl;
       for (int e = tid; e < n * n; e += blockDim.x) {
         const int c = e / n, r = e - c * n;
         T val = T(0);
-        if (r == c) val = fma_t(-v[r], xs[r], S[(size_t)c * ld + r]);
-        else if (r > c) val = fma_t(-v[r], xs[c], fma_t(-v[c], xs[r], T(2) * S[(size_t)c * ld + r]));
+        if (r == c) val = fma_t(-v[r], xs[r], gl * S[(size_t)c * ld + r]);
+        else if (r > c) val = fma_t(-v[r], xs[c], fma_t(-v[c], xs[r], gl2 * S[(size_t)c * ld + r]));
         g[e] = val;
       }
     }
@@ -299,8 +303,8 @@ int adj_launch_forward(int n, const T* A, int64_t strideA, const T* B, T* X, T* 
 }
 
 template <typename T>
-int adj_launch_backward(int n, const T* AL, int64_t strideA, int recompute, const T* X, const T* W, T* dA, T* db,
-                        int32_t* info, int batch, cudaStream_t stream, const char* name) {
+int adj_launch_backward(int n, const T* AL, int64_t strideA, int recompute, const T* X, const T* W, const T* G, T* dA,
+                        T* db, int32_t* info, int batch, cudaStream_t stream, const char* name) {
   if (n < 1 || n > kAdjMaxN) return record_arg_error(-1, "posv_logdet_backward: n out of range [1, 128]");
   if (batch < 0) return record_arg_error(-10, "posv_logdet_backward: negative batch");
   if (batch == 0) return NACU_SUCCESS;
@@ -309,7 +313,8 @@ int adj_launch_backward(int n, const T* AL, int64_t strideA, int recompute, cons
   const size_t smem = ((size_t)(n | 1) * n + 4 * (size_t)n) * sizeof(T);
   cudaError_t e = cudaFuncSetAttribute(adj_backward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
-  adj_backward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, AL, strideA, recompute, X, W, dA, db, info, batch);
+  adj_backward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, AL, strideA, recompute, X, W, G, dA, db, info,
+                                                               batch);
   return check_launch(name);
 }
 
@@ -329,15 +334,15 @@ int nacu_sposv_logdet_forward(int n, const float* A, int64_t strideA, const floa
                                          "nacu_sposv_logdet_forward");
 }
 int nacu_dposv_logdet_backward(int n, const double* AL, int64_t strideA, int recompute, const double* X,
-                               const double* W, double* dA, double* db, int32_t* info, int batch,
+                               const double* W, const double* G, double* dA, double* db, int32_t* info, int batch,
                                nacu_stream_t stream) {
-  return nacu::adj_launch_backward<double>(n, AL, strideA, recompute, X, W, dA, db, info, batch,
+  return nacu::adj_launch_backward<double>(n, AL, strideA, recompute, X, W, G, dA, db, info, batch,
                                            (cudaStream_t)stream, "nacu_dposv_logdet_backward");
 }
 int nacu_sposv_logdet_backward(int n, const float* AL, int64_t strideA, int recompute, const float* X,
-                               const float* W, float* dA, float* db, int32_t* info, int batch,
+                               const float* W, const float* G, float* dA, float* db, int32_t* info, int batch,
                                nacu_stream_t stream) {
-  return nacu::adj_launch_backward<float>(n, AL, strideA, recompute, X, W, dA, db, info, batch,
+  return nacu::adj_launch_backward<float>(n, AL, strideA, recompute, X, W, G, dA, db, info, batch,
                                           (cudaStream_t)stream, "nacu_sposv_logdet_backward");
 }
 
