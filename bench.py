@@ -192,7 +192,7 @@ def bench_ragged_ours(args, rank, world):
     n_max = int(ns.max())
     from nalgebra_gb300 import tuning
 
-    tune_res = tuning.autotune(save=False) if args.autotune else None
+    tune_res = tuning.autotune(per_bucket=2500, save=False) if args.autotune else None
     tiles_table = tuning.current(L)
 
     def launch():  # the stream is read at call time: inside a capture it is the capture stream

@@ -161,8 +161,8 @@ __device__ __forceinline__ int bucket_hi_dev(int b) {
   return hi[b];
 }
 // Measured on GB300 by nacu_ragged_autotune (FP64 form, 4 right-hand sides,
-// 1500 systems per bucket); replaced by nacu_ragged_set_tuning / autotune.
-int g_tuning[NACU_RAGGED_BUCKETS] = {0, 0, 0, 1, 1, 1, 3, 3};
+// 2500 systems per bucket); replaced by nacu_ragged_set_tuning / autotune.
+int g_tuning[NACU_RAGGED_BUCKETS] = {0, 0, 0, 0, 0, 1, 3, 3};
 
 typedef void (*CholKernel)(CholArgs);
 CholKernel chol_kernel(bool exact, int tile) {
