@@ -204,8 +204,10 @@ int nacu_dposv_ragged_mixed(int count, int n_max, const int32_t* ns, const int64
 /* Forward: for `batch` SPD matrices A + s*strideA (lower triangle read),
  * X[s*n..] = A^-1 B[s*n..] and logdet[s] = sum ln(L_ii^2)
  * (src/linalg/cholesky.rs:221-272, 122-143, 172-185).  L (nullable) receives
- * the factor (lower triangle, zeros above): the "store" form keeps it for the
- * backward pass; pass NULL to keep nothing (the "recompute" form).  No
+ * the factor in its lower triangle (the FP64 form leaves A's values above the
+ * diagonal, as nalgebra's factor does; the FP32 form writes zeros there): the
+ * "store" form keeps it for the backward pass; pass NULL to keep nothing (the
+ * "recompute" form).  info is required in the FP64 store form.  No
  * reference counterpart for the adjoint itself: nalgebra has no autodiff. */
 int nacu_dposv_logdet_forward(int n, const double* A, int64_t strideA, const double* B, double* X, double* L,
                               double* logdet, int32_t* info, int batch, nacu_stream_t stream);

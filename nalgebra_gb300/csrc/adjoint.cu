@@ -67,9 +67,9 @@ __device__ void chol_smem(int n, T* S, int ld, int* s_info, T* s_sc) {
     if (tid == 0) {
       const T d = cj[j];
       if (!(d <= T(0)) && d >= T(0)) {
-        const T den = sqrt(d);
-        cj[j] = den;
-        s_sc[0] = T(1) / den;
+        const T r = rsqrt(d);  // L_jj = d * rsqrt(d), 1/L_jj = rsqrt(d): one dependent FP64 chain
+        cj[j] = d * r;
+        s_sc[0] = r;
       } else if (*s_info == 0) {
         *s_info = j + 1;
       }
@@ -97,67 +97,52 @@ __device__ void chol_smem(int n, T* S, int ld, int* s_info, T* s_sc) {
 }
 
 // In place L -> L^-1 (lower), columns from right to left (LAPACK trti2 order):
-// L^-1[j+1.., j] = -(1/L_jj) * L^-1[j+1.., j+1..] * L[j+1.., j].
-// Thread t owns rows j+1+t and n-1-t so every thread walks n-j-1 terms.
+// L^-1[i][j] = -(1/L_jj) * sum_{k=j+1..i} L^-1[i][k] L[k][j]  (i > j).
+// Two threads per row i (k split by parity, combined by a shuffle), so all
+// warps share each column's dot products; fused multiply-adds; the
+// reciprocals of the diagonal (rdiag) are formed once beforehand.
 template <typename T>
-__device__ void trinv_smem(int n, T* S, int ld, T* tmp) {
+__device__ void trinv_smem(int n, T* S, int ld, T* tmp, const T* rdiag) {
   const int tid = threadIdx.x;
+  const int ri = tid >> 1, h = tid & 1;
   for (int j = n - 1; j >= 0; --j) {
-    T* cj = S + (size_t)j * ld;
-    const T ajj = T(1) / cj[j];
-    const int m = n - j - 1;
-    const int half = (m + 1) >> 1;
-    for (int t = tid; t < half; t += blockDim.x) {
-      const int i1 = j + 1 + t, i2 = n - 1 - t;
-      const int len1 = i1 - j, len2 = (i2 != i1) ? (i2 - j) : 0;
-      T s1 = T(0), s2 = T(0);
-      for (int q = 0; q < len1 + len2; ++q) {  // one loop: no divergence
-        const bool first = q < len1;
-        const int i = first ? i1 : i2;
-        const int k = j + 1 + (first ? q : q - len1);
-        const T p = S[(size_t)k * ld + i] * cj[k];  // L^-1[i][k] * L[k][j]
-        if (first) s1 += p;
-        else s2 += p;
-      }
-      tmp[i1] = -ajj * s1;
-      if (len2) tmp[i2] = -ajj * s2;
-    }
+    const T* cj = S + (size_t)j * ld;
+    const T ajj = rdiag[j];
+    const int i = j + 1 + ri;
+    T acc = T(0);
+    if (i < n)
+      for (int k = j + 1 + h; k <= i; k += 2) acc = fma_t(S[(size_t)k * ld + i], cj[k], acc);  // L^-1[i][k] L[k][j]
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    if (i < n && h == 0) tmp[i] = -ajj * acc;
     __syncthreads();
-    for (int i = j + 1 + tid; i < n; i += blockDim.x) cj[i] = tmp[i];
-    if (tid == 0) cj[j] = ajj;
+    T* cw = S + (size_t)j * ld;
+    for (int r = j + 1 + tid; r < n; r += blockDim.x) cw[r] = tmp[r];
+    if (tid == 0) cw[j] = ajj;
     __syncthreads();
   }
 }
 
 // In place L^-1 -> A^-1 = L^-T L^-1 (lower triangle), column by column:
 // (A^-1)_ij = sum_{k >= i} Linv_ki Linv_kj  (i >= j); column j needs only
-// columns >= j of L^-1, so it can be overwritten once computed.
+// columns >= j of L^-1, so it can be overwritten once computed.  Two threads
+// per row, k split by parity.
 template <typename T>
 __device__ void inv_from_trinv_smem(int n, T* S, int ld, T* tmp) {
   const int tid = threadIdx.x;
+  const int ri = tid >> 1, h = tid & 1;
   for (int j = 0; j < n; ++j) {
     const T* cj = S + (size_t)j * ld;
-    const int m = n - j;
-    const int half = (m + 1) >> 1;
-    for (int t = tid; t < half; t += blockDim.x) {
-      // rows i1 = j+t (sum over k = i1..n-1: n-i1 terms) and i2 = n-1-t
-      const int i1 = j + t, i2 = n - 1 - t;
-      const int len1 = n - i1, len2 = (i2 != i1) ? (n - i2) : 0;
-      T s1 = T(0), s2 = T(0);
-      for (int q = 0; q < len1 + len2; ++q) {
-        const bool first = q < len1;
-        const int i = first ? i1 : i2;
-        const int k = (first ? i1 + q : i2 + (q - len1));
-        const T p = S[(size_t)i * ld + k] * cj[k];  // Linv[k][i] * Linv[k][j]
-        if (first) s1 += p;
-        else s2 += p;
-      }
-      tmp[i1] = s1;
-      if (len2) tmp[i2] = s2;
+    const int i = j + ri;
+    T acc = T(0);
+    if (i < n) {
+      const T* ci = S + (size_t)i * ld;
+      for (int k = i + h; k < n; k += 2) acc = fma_t(ci[k], cj[k], acc);  // Linv[k][i] Linv[k][j]
     }
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    if (i < n && h == 0) tmp[i] = acc;
     __syncthreads();
     T* cw = S + (size_t)j * ld;
-    for (int i = j + tid; i < n; i += blockDim.x) cw[i] = tmp[i];
+    for (int r = j + tid; r < n; r += blockDim.x) cw[r] = tmp[r];
     __syncthreads();
   }
 }
@@ -244,6 +229,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const 
   T* v = tmp + n;
   T* xs = v + n;
   T* ws = xs + n;
+  T* rdiag = ws + n;
   const int tid = threadIdx.x;
   for (int s = blockIdx.x; s < batch; s += gridDim.x) {
     const T* a = AL + (size_t)s * strideA;
@@ -260,7 +246,9 @@ __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const 
     if (recompute) chol_smem<T>(n, S, ld, &s_info, s_sc);  // refactor instead of storing L
     const int inf = s_info;
     if (inf == 0) {
-      trinv_smem<T>(n, S, ld, tmp);
+      for (int i = tid; i < n; i += blockDim.x) rdiag[i] = T(1) / S[(size_t)i * ld + i];
+      __syncthreads();
+      trinv_smem<T>(n, S, ld, tmp, rdiag);
       inv_from_trinv_smem<T>(n, S, ld, tmp);
       // v = A^-1 w from the lower triangle of the symmetric A^-1
       for (int i = tid; i < n; i += blockDim.x) {
@@ -310,7 +298,7 @@ int adj_launch_backward(int n, const T* AL, int64_t strideA, int recompute, cons
   if (batch == 0) return NACU_SUCCESS;
   if (!AL || !X || !W || !dA || !db) return record_arg_error(-2, "posv_logdet_backward: null argument");
   if (strideA < (int64_t)n * n) return record_arg_error(-3, "posv_logdet_backward: strideA < n*n");
-  const size_t smem = ((size_t)(n | 1) * n + 4 * (size_t)n) * sizeof(T);
+  const size_t smem = ((size_t)(n | 1) * n + 5 * (size_t)n) * sizeof(T);
   cudaError_t e = cudaFuncSetAttribute(adj_backward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   adj_backward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, AL, strideA, recompute, X, W, G, dA, db, info,
@@ -325,8 +313,23 @@ extern "C" {
 
 int nacu_dposv_logdet_forward(int n, const double* A, int64_t strideA, const double* B, double* X, double* L,
                               double* logdet, int32_t* info, int batch, nacu_stream_t stream) {
-  return nacu::adj_launch_forward<double>(n, A, strideA, B, X, L, logdet, info, batch, (cudaStream_t)stream,
-                                          "nacu_dposv_logdet_forward");
+  using namespace nacu;
+  if (L == nullptr)  // recompute form: no factor buffer, the shared-memory kernel keeps nothing
+    return adj_launch_forward<double>(n, A, strideA, B, X, L, logdet, info, batch, (cudaStream_t)stream,
+                                      "nacu_dposv_logdet_forward");
+  // store form: the factor is built in L by the FP64 batched Cholesky kernel
+  // (factor + solve + log-det in place on copies of A and b)
+  if (n < 1 || n > kAdjMaxN) return record_arg_error(-1, "posv_logdet_forward: n out of range [1, 128]");
+  if (batch < 0) return record_arg_error(-9, "posv_logdet_forward: negative batch");
+  if (batch == 0) return NACU_SUCCESS;
+  if (!A || !B || !X || !logdet || !info)
+    return record_arg_error(-2, "posv_logdet_forward: null A, B, X, logdet or info");
+  if (strideA < (int64_t)n * n) return record_arg_error(-3, "posv_logdet_forward: strideA < n*n");
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(L, A, (size_t)batch * strideA * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(X, B, (size_t)batch * n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return record_cuda_error(e, "nacu_dposv_logdet_forward");
+  return chol_uniform_posv(n, L, strideA, 1, X, n, info, logdet, batch, s, "nacu_dposv_logdet_forward");
 }
 int nacu_sposv_logdet_forward(int n, const float* A, int64_t strideA, const float* B, float* X, float* L,
                               float* logdet, int32_t* info, int batch, nacu_stream_t stream) {

@@ -45,6 +45,7 @@ struct CholArgs {
   double subst;
   int do_factor;         // 0: A already holds the factor (solve only)
   const int32_t* range;  // [start, end) of this launch within `order` (device), or null: [0, count)
+  int64_t astride, bstride;  // equal-order batches without offset tables: system s at s * stride
 };
 
 template <bool EXACT, int NB>
@@ -58,7 +59,7 @@ __device__ void chol_solve_one(const CholArgs& g, int s, double* P, double* X, i
     }
     return;
   }
-  double* a = g.A + (g.aoff ? g.aoff[s] : 0);
+  double* a = g.A + (g.aoff ? g.aoff[s] : (int64_t)s * g.astride);
   if (tid == 0) *s_info = 0;
   __syncthreads();
   const int ldp = g.n_max | 1;
@@ -72,7 +73,7 @@ __device__ void chol_solve_one(const CholArgs& g, int s, double* P, double* X, i
   const int inf = *s_info;
   if (inf == 0) {
     if (g.nrhs > 0 && g.B) {
-      double* b = g.B + (g.boff ? g.boff[s] : 0);
+      double* b = g.B + (g.boff ? g.boff[s] : (int64_t)s * g.bstride);
       const int ldx = ldp;
       for (int c0 = 0; c0 < g.nrhs; c0 += kRhsChunk) {
         const int nr = min(kRhsChunk, g.nrhs - c0);
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(THREADS, MINB) chol_ragged_kernel(CholArgs g) 
   const int start = g.range ? g.range[0] : 0;
   const int end = g.range ? g.range[1] : g.count;
   for (;;) {
-    if (threadIdx.x == 0) s_item = g.counter ? atomicAdd(g.counter, 1) : 0;
+    if (threadIdx.x == 0) s_item = g.counter ? atomicAdd(g.counter, 1) : (int)blockIdx.x;  // no queue: one system per CTA
     __syncthreads();
     const int idx = start + s_item;
     __syncthreads();
@@ -344,6 +345,30 @@ int chol_launch_ragged(CholArgs g, int flags, cudaStream_t s, const char* name) 
   if (g.order) return chol_launch(g, flags, s, true, name);
   return chol_launch_bucketed(g, flags, s, name);
 }
+
+}  // namespace
+
+// Equal-order batch (system s at A + s*strideA, B + s*strideB), one CTA per
+// system, factor + solve + log-determinant in place with the tuned tile of
+// the order's size bucket (used by the adjoint's forward pass).
+int chol_uniform_posv(int n, double* A, int64_t strideA, int nrhs, double* B, int64_t strideB, int32_t* info,
+                      double* logdet, int batch, cudaStream_t s, const char* name) {
+  if (batch <= 0) return NACU_SUCCESS;
+  int b = 0;
+  while (b < NACU_RAGGED_BUCKETS - 1 && n > kBucketHi[b]) ++b;
+  CholArgs g{batch, n, nullptr, nullptr, A, nrhs, nullptr, B, info, logdet, nullptr, nullptr, 0, 0.0, 1, nullptr,
+             strideA, strideB};
+  int tile = g_tuning[b];
+  if (tile < 0 || tile >= NACU_RAGGED_TILES) tile = kDefaultTile;
+  CholKernel kern = chol_kernel(false, tile);
+  const size_t smem = chol_smem_bytes(n, kCholTiles[tile].nb);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  kern<<<batch, kCholTiles[tile].threads, smem, s>>>(g);
+  return check_launch(name);
+}
+
+namespace {
 
 }  // namespace
 }  // namespace nacu

@@ -12,6 +12,11 @@ template <typename TI, typename TO>
 int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, const TI* B, int64_t ldb, double beta,
                    TO* C, int64_t ldc, int slices, void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
+// Equal-order batched Cholesky factor + solve + log-determinant in place, FP64
+// (chol_ragged.cu).
+int chol_uniform_posv(int n, double* A, int64_t strideA, int nrhs, double* B, int64_t strideB, int32_t* info,
+                      double* logdet, int batch, cudaStream_t s, const char* name);
+
 // Records a CUDA error (from a launch or a runtime call) for nacu_last_error().
 int record_cuda_error(cudaError_t e, const char* where);
 // Records an argument error message; returns `code`.
