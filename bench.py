@@ -701,11 +701,21 @@ def bench_adjoint_ours(args, rank, world):
                          "systems_per_s_fwd_bwd": count / ((fms + bms) * 1e-3),
                          "stored_intermediate_bytes": 0 if rec else int(count * n * n * np.dtype(dtype).itemsize)}
         out[pre + "_" + np.dtype(dtype).name] = res
+    # FP64 work per system (store form): forward n^3/3 + 2n^2 (factor, solve, log-det); backward the
+    # triangular inverse n^3/3, A^-1 = L^-T L^-1 n^3/3, v = A^-1 w 2n^2 and the gradient 4n^2
+    peak = ctypes_probe(L)
+    st = out["d_float64"]["store"]
+    flops_sys = n ** 3 + 8.0 * n * n
+    achieved = count * flops_sys / ((st["forward_ms"] + st["backward_ms"]) * 1e-3)
     return {"metric": "adjoint of batched Cholesky solve + logdet (2048 x 128, f64 and f32)",
             "value": out["d_float64"]["store"]["systems_per_s_fwd_bwd"], "unit": "systems/s (forward+backward, f64)",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "adjoint", "count": count, "n": n}, "forms": out, "gpu_launches": 2 * args.steps}
+            "config": {"workload": "adjoint", "count": count, "n": n}, "forms": out,
+            "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": fp64_peak_source(),
+                         "note": "FP64 store form, forward + backward: n^3 + 8 n^2 flops per system"},
+            "gpu_launches": 2 * args.steps}
 
 
 # ----------------------------------------------------------------------------- GEMM
@@ -871,13 +881,20 @@ def bench_mixed_lu_ours(args, rank, world):
                 headline = (n, cond, res)
             del A, b
     n, cond, res = headline
+    peak = ctypes_probe(L)
+    fp64_rate = res["fp64"]["gflops_fp64_equivalent"] * 1e9
+    roof = {"bound": "fp64", "achieved": fp64_rate / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+            "frac": fp64_rate / peak, "traffic": None, "peak_source": fp64_peak_source(),
+            "note": ("the plain FP64 form (blocked LU, FP64 DGEMM trailing updates): 2/3 n^3 + 2 n^2 per solve; "
+                     "the mixed form's trailing updates run on the BF16 tensor pipe (split_gemm_kernel<float>) "
+                     "and its panel is latency-bound")}
     return {"metric": "mixed-precision LU + FP64 refinement (backward error <= n eps64) vs plain FP64 GPU LU",
             "value": res["mixed_ir"]["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 factor (bf16x3 tensor-core updates) + f64 refinement", "data": "synthetic",
             "config": {"workload": "mixed_lu", "n": n, "cond": cond, "nrhs": 1, "sizes": sizes,
                        "conds": conds, "inputs": "A = U diag(s) V^T, U, V from QR of N(0,1), s log-uniform"},
-            "forms": forms, "gpu_launches": None}
+            "forms": forms, "roofline": roof, "gpu_launches": None}
 
 
 # ----------------------------------------------------------------------------- main

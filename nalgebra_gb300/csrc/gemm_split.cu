@@ -130,15 +130,24 @@ __device__ __forceinline__ double f32_scaled_to_f64(float f, int e) {
 }
 
 // Per-row max exponent of A (column-major m x k), atomicMax into rexp (init INT_MIN).
+constexpr int kRowExpChunk = 32;  // columns per thread: k / 32 CTAs along K
 template <typename TI>
 __global__ void row_exp_kernel(int m, int k, const TI* __restrict__ A, int64_t lda, int* __restrict__ rexp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
-  const int c0 = blockIdx.y * 256, c1 = min(k, c0 + 256);
+  const int c0 = blockIdx.y * kRowExpChunk, c1 = min(k, c0 + kRowExpChunk);
   int e = INT_MIN;
   for (int c = c0; c < c1; ++c) {
-    const double v = (double)A[(size_t)c * lda + i];
-    if (v != 0.0) e = max(e, exp_of(v));
+    const TI x = A[(size_t)c * lda + i];
+    if constexpr (sizeof(TI) == 4) {  // FP32: the exponent from the bits (no FP64 conversion)
+      const uint32_t b = __float_as_uint((float)x) & 0x7fffffffu;
+      if (b == 0u) continue;
+      const int ex = (int)(b >> 23);
+      e = max(e, ex != 0 ? ex - 127 : exp_of((double)x));
+    } else {
+      const double v = (double)x;
+      if (v != 0.0) e = max(e, exp_of(v));
+    }
   }
   if (e != INT_MIN) atomicMax(&rexp[i], e);
 }
@@ -249,6 +258,21 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base_sh;
 
+  if (warp >= 2 && g.beta != 0.0) {
+    // warps 2-3 are idle until the epilogue: bring the C tile the epilogue
+    // reads (beta != 0) into L2 while the products run (one 128-byte line per
+    // prefetch, valid elements only)
+    constexpr int kLineElems = 128 / (int)sizeof(TO);
+    const int lines_per_col = kTM / kLineElems;
+    for (int q = threadIdx.x - 64; q < kTN * lines_per_col; q += 64) {
+      const int col = n0 + q / lines_per_col;
+      const int row = m0 + (q % lines_per_col) * kLineElems;
+      if (col < g.n && row < g.m) {
+        const TO* cp = static_cast<const TO*>(g.C) + (size_t)col * g.ldc + row;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(cp));
+      }
+    }
+  }
   if (warp == 0 && lane == 0) {
     // producer: TMA loads of (A slice tile, B slice tile) per iteration
     for (int it = 0; it < iters; ++it) {
@@ -421,7 +445,8 @@ int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, 
   if (e == cudaSuccess) e = cudaMemsetAsync(rexp, 0x80, (size_t)L.mp * 4, s);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgemm_split_bf16");
   if (k > 0) {
-    row_exp_kernel<TI><<<dim3((m + 255) / 256, (k + 255) / 256), 256, 0, s>>>(m, k, A, lda, rexp);
+    row_exp_kernel<TI><<<dim3((m + 255) / 256, (k + kRowExpChunk - 1) / kRowExpChunk), 256, 0, s>>>(m, k, A, lda,
+                                                                                                 rexp);
     col_exp_kernel<TI><<<(n + 7) / 8, 256, 0, s>>>(k, n, B, ldb, cexp);
     split_a_kernel<TI><<<dim3((k + 31) / 32, (m + 31) / 32), 256, 0, s>>>(m, k, A, lda, rexp, L.mp, L.kp, slices, as);
     split_b_kernel<TI><<<dim3((L.kp + 255) / 256, n), 256, 0, s>>>(k, n, B, ldb, cexp, L.np, L.kp, slices, bs);
