@@ -39,7 +39,8 @@ def _solve(cuda, a, b, tol_units=1.0, max_iter=30):
     return X.cpu().numpy(), it.value, berr.value, fb.value
 
 
-@pytest.mark.parametrize("n,cond", [(256, 1e2), (640, 1e2), (1000, 1e5), (1536, 1e5), (777, 1e3)])
+@pytest.mark.parametrize("n,cond", [(256, 1e2), (640, 1e2), (1000, 1e5), (1536, 1e5), (777, 1e3), (778, 1e4),
+                                    (128, 1e2), (132, 1e3)])
 def test_refined_solution_meets_backward_error(cuda, n, cond):
     a, b = workloads.conditioned(n, cond, seed=n)
     x, iters, berr, fb = _solve(cuda, a, b)
