@@ -342,13 +342,17 @@ struct MixedSmem {
   size_t x32, rd32, u, xd, total;
   int ldl;
 };
+constexpr int kHeadFloats = (kCholThreads / 32) * (kNB * kNB + kNB);
 __host__ __device__ inline MixedSmem mixed_smem_layout(int n_max) {
   MixedSmem L;
   const size_t ldp = (size_t)(n_max | 1);
   L.ldl = ((n_max + 3 + 3) / 4) * 4;  // float4 reads may run 3 past the last row
   auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
   L.x32 = 0;
-  L.rd32 = L.x32 + ldp * kRhsChunk * sizeof(float);
+  // X32 is idle during the factor: the per-warp 16 x 16 heads of the FP32
+  // panel share its space (no static shared memory for them)
+  const size_t x32 = ldp * kRhsChunk * sizeof(float), heads = (size_t)kHeadFloats * sizeof(float);
+  L.rd32 = up16(L.x32 + (x32 > heads ? x32 : heads));
   L.u = up16(L.rd32 + ldp * sizeof(float));
   const size_t p32 = ldp * kNB * sizeof(float), rd = ldp * kRhsChunk * sizeof(double);
   L.xd = up16(L.u + (p32 > rd ? p32 : rd));
@@ -561,14 +565,14 @@ __global__ void __launch_bounds__(kCholThreads, 4) chol_mixed_fallback_kernel(Mi
   }
 }
 
-__global__ void __launch_bounds__(kCholThreads, 6) chol_mixed_kernel(MixedArgs g) {
+__global__ void __launch_bounds__(kCholThreads, 7) chol_mixed_kernel(MixedArgs g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   __shared__ int s_info;
   __shared__ double s_scal[2 + kCholThreads / 32];
   __shared__ unsigned long long red[4 * kRhsChunk];
-  __shared__ float hs[(kCholThreads / 32) * (kNB * kNB + kNB)];
   __shared__ unsigned long long nrm[kNrmSize];
+  float* hs = reinterpret_cast<float*>(smem_raw + mixed_smem_layout(g.n_max).x32);
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1);
     __syncthreads();
