@@ -182,7 +182,7 @@ double orc_dbackward_error(int64_t n, const double* a, int64_t lda, const double
 }
 
 // ||P A - L U||_F / (||A||_F * n * eps64) for packed factors and a per-step
-// pivot list (the spec LU reconstruction criterion).
+// pivot list (the LU parity criterion: at most 10).
 double orc_dlu_reconstruction(int64_t n, const double* a, int64_t lda, const double* lu,
                               int64_t ldlu, const int32_t* ipiv) {
   std::vector<double> pa(n * n);
