@@ -683,8 +683,43 @@ int coop_grid(const void* kern, int threads, size_t smem) {
 // The panel's exchange area (sized for FP64 and the widest panel).
 size_t getrf_ws_bytes() { return (sizeof(PanelPub<double>) + 255) & ~(size_t)255; }
 
+// slot 0: the next panel's columns (on the panel stream), slot 1: the rest of
+// the trailing update (on the update stream, concurrently)
 typedef int (*UpdateFn)(int m, int n, int k, const void* L21, const void* U12, void* A22, int64_t lda, void* ctx,
-                        cudaStream_t s);
+                        int slot, cudaStream_t s);
+
+// Internal streams of the look-ahead schedule (per device, created on first
+// use): the panel chain runs at the highest stream priority, the bulk of each
+// trailing update at the lowest, so the next panel's CTAs are dispatched as
+// soon as SMs free up.
+struct LookaheadStreams {
+  cudaStream_t panel = nullptr, rest = nullptr;
+  cudaEvent_t fork = nullptr, trsm_done = nullptr, rest_done = nullptr, join = nullptr;
+  bool ready = false;
+};
+LookaheadStreams g_lookahead[64];
+
+int lookahead_streams(LookaheadStreams** out, const char* name) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  if (dev < 0 || dev >= 64) return record_arg_error(-99, "getrf: device index >= 64");
+  LookaheadStreams& L = g_lookahead[dev];
+  if (!L.ready) {
+    int least = 0, greatest = 0;
+    e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&L.panel, cudaStreamNonBlocking, greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&L.rest, cudaStreamNonBlocking, least);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.trsm_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.rest_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.join, cudaEventDisableTiming);
+    if (e != cudaSuccess) return record_cuda_error(e, name);
+    L.ready = true;
+  }
+  *out = &L;
+  return NACU_SUCCESS;
+}
 
 // CTAs per cluster for the cluster-form panel (16, else 8, else 0 = grid
 // form only), from the occupancy API with the largest panel's shared memory;
@@ -722,6 +757,11 @@ int panel_cluster_ctas() {
   return ctas;
 }
 
+// Blocked LU with look-ahead: step k's panel chain (panel, row swaps, TRSM,
+// and the update of the next panel's columns) runs on the panel stream; the
+// rest of step k's trailing update runs on the update stream while panel k+1
+// is factored.  Step k+1's row swaps wait for that update.  Forks from and
+// joins to the caller's stream.
 template <typename T>
 int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* ws, int nb, UpdateFn update,
                   void* ctx, cudaStream_t s, const char* name) {
@@ -732,7 +772,16 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
   if (e != cudaSuccess) return record_cuda_error(e, name);
   const int cluster = panel_cluster_ctas<T>();
   const int gmax = std::min(kPanelMaxG, sm_count());
-  info_init_kernel<<<1, 1, 0, s>>>(info);
+  LookaheadStreams* la = nullptr;
+  int rc = lookahead_streams(&la, name);
+  if (rc != NACU_SUCCESS) return rc;
+  const cudaStream_t sp = la->panel, su = la->rest;
+  e = cudaEventRecord(la->fork, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(sp, la->fork, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(su, la->fork, 0);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  info_init_kernel<<<1, 1, 0, sp>>>(info);
+  bool rest_pending = false;
   for (int j0 = 0; j0 < n; j0 += nb) {
     const int jb = std::min(nb, n - j0);
     const int rows = n - j0;
@@ -745,7 +794,7 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
       cfg.gridDim = dim3(cluster);
       cfg.blockDim = dim3(kPanelThreads);
       cfg.dynamicSmemBytes = csmem;
-      cfg.stream = s;
+      cfg.stream = sp;
       cudaLaunchAttribute at[1];
       at[0].id = cudaLaunchAttributeClusterDimension;
       at[0].val.clusterDim.x = cluster;
@@ -763,22 +812,47 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
       if (chunk > max_rows) return record_arg_error(-1, "getrf: n too large for the shared-memory panel");
       pa.chunk = chunk;
       void* args[] = {&pa};
-      e = cudaLaunchCooperativeKernel(pk, G, kPanelThreads, args, (size_t)chunk * jb * sizeof(T), s);
+      e = cudaLaunchCooperativeKernel(pk, G, kPanelThreads, args, (size_t)chunk * jb * sizeof(T), sp);
       if (e != cudaSuccess) return record_cuda_error(e, name);
     }
-    if (n > jb) lu_swap_kernel<T><<<(n - jb + 7) / 8, 256, 0, s>>>(n, A, lda, pa.pub, j0, jb);
+    if (rest_pending) {  // the swaps below touch the columns the previous update is still writing
+      e = cudaStreamWaitEvent(sp, la->rest_done, 0);
+      if (e != cudaSuccess) return record_cuda_error(e, name);
+      rest_pending = false;
+    }
+    if (n > jb) lu_swap_kernel<T><<<(n - jb + 7) / 8, 256, 0, sp>>>(n, A, lda, pa.pub, j0, jb);
     const int rest = n - j0 - jb;
     if (rest > 0) {
-      e = launch_trsm<T>(n, A, lda, j0, jb, rest, s);
+      e = launch_trsm<T>(n, A, lda, j0, jb, rest, sp);
       if (e != cudaSuccess) return record_cuda_error(e, name);
-      int rc = update(rest, rest, jb, A + (size_t)j0 * lda + j0 + jb, A + (size_t)(j0 + jb) * lda + j0,
-                      A + (size_t)(j0 + jb) * lda + j0 + jb, lda, ctx, s);
+      const T* L21 = A + (size_t)j0 * lda + j0 + jb;
+      const T* U12 = A + (size_t)(j0 + jb) * lda + j0;
+      T* A22 = A + (size_t)(j0 + jb) * lda + j0 + jb;
+      const int nn = std::min(nb, rest);  // the next panel's columns
+      rc = update(rest, nn, jb, L21, U12, A22, lda, ctx, 0, sp);
       if (rc != NACU_SUCCESS) return rc;
+      if (rest > nn) {
+        e = cudaEventRecord(la->trsm_done, sp);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(su, la->trsm_done, 0);
+        if (e != cudaSuccess) return record_cuda_error(e, name);
+        rc = update(rest, rest - nn, jb, L21, U12 + (size_t)nn * lda, A22 + (size_t)nn * lda, lda, ctx, 1, su);
+        if (rc != NACU_SUCCESS) return rc;
+        e = cudaEventRecord(la->rest_done, su);
+        if (e != cudaSuccess) return record_cuda_error(e, name);
+        rest_pending = true;
+      }
     }
-    int rc = check_launch(name);
+    rc = check_launch(name);
     if (rc != NACU_SUCCESS) return rc;
   }
-  info_finalize_kernel<<<1, 1, 0, s>>>(info);
+  if (rest_pending) {
+    e = cudaStreamWaitEvent(sp, la->rest_done, 0);
+    if (e != cudaSuccess) return record_cuda_error(e, name);
+  }
+  info_finalize_kernel<<<1, 1, 0, sp>>>(info);
+  e = cudaEventRecord(la->join, sp);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, la->join, 0);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
   return check_launch(name);
 }
 
@@ -822,7 +896,8 @@ int getrs_one(int n, const T* LU, int64_t lda, const int32_t* ipiv, T* x, int32_
   return check_launch(name);
 }
 
-int update_fp64(int m, int n, int k, const void* L21, const void* U12, void* A22, int64_t lda, void*, cudaStream_t s) {
+int update_fp64(int m, int n, int k, const void* L21, const void* U12, void* A22, int64_t lda, void*, int,
+                cudaStream_t s) {
   return nacu_dgemm(m, n, k, -1.0, static_cast<const double*>(L21), lda, static_cast<const double*>(U12), lda, 1.0,
                     static_cast<double*>(A22), lda, s);
 }
@@ -831,16 +906,16 @@ int update_fp64(int m, int n, int k, const void* L21, const void* U12, void* A22
 // mixed precision: FP32 factor (tensor-core trailing updates), FP64 refinement
 // ---------------------------------------------------------------------------
 struct Update32Ctx {
-  void* ws;
-  size_t ws_bytes;
+  void* ws[2];  // one split-GEMM workspace per concurrent update (slot)
+  size_t ws_bytes[2];
 };
 
 int update_fp32_split(int m, int n, int k, const void* L21, const void* U12, void* A22, int64_t lda, void* ctx,
-                      cudaStream_t s) {
+                      int slot, cudaStream_t s) {
   const Update32Ctx* c = static_cast<const Update32Ctx*>(ctx);
   return split_gemm_run<float, float>(m, n, k, -1.0, static_cast<const float*>(L21), lda,
                                       static_cast<const float*>(U12), lda, 1.0, static_cast<float*>(A22), lda, 3,
-                                      c->ws, c->ws_bytes, s);
+                                      c->ws[slot], c->ws_bytes[slot], s);
 }
 
 __global__ void to_fp32_kernel(int n, const double* __restrict__ A, int64_t lda, float* __restrict__ A32) {
@@ -926,7 +1001,7 @@ __global__ void accumulate_kernel(int n, const float* __restrict__ d32, int e, d
 }
 
 struct MixedLuLayout {
-  size_t a32, ipiv, perm, info, cand, split, r, d32, part, nrm, a64, total;
+  size_t a32, ipiv, perm, info, cand, split, split2, r, d32, part, nrm, a64, total;
 };
 inline size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 MixedLuLayout mixed_lu_layout(int n, int nb) {
@@ -939,6 +1014,8 @@ MixedLuLayout mixed_lu_layout(int n, int nb) {
   L.cand = o;  o = up256(o + getrf_ws_bytes());
   o = (o + 1023) & ~(size_t)1023;
   L.split = o; o = up256(o + nacu_gemm_split_workspace_bytes(n, n, nb));
+  o = (o + 1023) & ~(size_t)1023;
+  L.split2 = o; o = up256(o + nacu_gemm_split_workspace_bytes(n, nb, nb));
   L.r = o;     o = up256(o + (size_t)n * 8);
   L.d32 = o;   o = up256(o + (size_t)n * 4);
   L.part = o;  o = up256(o + (size_t)kGemvChunks * n * 8);
@@ -1002,7 +1079,8 @@ int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, do
   const double bnorm = __builtin_bit_cast(double, h[2]);
   // FP32 factor
   to_fp32_kernel<<<sm_count() * 8, 256, 0, s>>>(n, A, lda, A32);
-  Update32Ctx uctx{split_ws, nacu_gemm_split_workspace_bytes(n, n, nb)};
+  Update32Ctx uctx{{base + L.split2, split_ws},
+                   {nacu_gemm_split_workspace_bytes(n, nb, nb), nacu_gemm_split_workspace_bytes(n, n, nb)}};
   int rc = getrf_blocked<float>(n, A32, n, ipiv, info, cand, nb, update_fp32_split, &uctx, s, "nacu_dgesv_mixed_ir");
   if (rc != NACU_SUCCESS) return rc;
   int32_t hinfo = 0;
