@@ -86,10 +86,10 @@ __device__ __forceinline__ void block_max4(unsigned long long (&v)[kRhsChunk], u
 // Thread = row: elements left of the diagonal block come from column j (row
 // i of L, coalesced), elements right of it from column i (A_ij = A_ji).
 __device__ __noinline__ void residual_fp64(int n, const double* __restrict__ a, const double* __restrict__ b, int nr,
-                              const double* Xd, double* Rd, int ldx, bool with_norm, double* rowmax) {
+                              const double* Xd, double* Rd, int ldx, bool with_norm, float* rowmax) {
   constexpr int U = 8;  // independent loads in flight per thread
   const int tid = threadIdx.x;
-  double my_rowmax = 0.0;
+  float my_rowmax = 0.0f;
   for (int rb = (tid >> 5) * 32; rb < n; rb += kCholThreads) {
     const int i = rb + (tid & 31);
     const bool valid = i < n;
@@ -97,7 +97,7 @@ __device__ __noinline__ void residual_fp64(int n, const double* __restrict__ a, 
     double acc[kRhsChunk];
 #pragma unroll
     for (int c = 0; c < kRhsChunk; ++c) acc[c] = (c < nr) ? b[(size_t)c * n + ii] : 0.0;
-    double rs = 0.0;  // sum |A_ij| over the row (first residual only)
+    float rs = 0.0f;  // sum |A_ij| over the row in FP32 (first residual only; off the FP64 pipe)
     const int dend = min(rb + 32, n);
     const double* colii = a + (size_t)ii * n;
     // element (ii, j): column j (left of / in the diagonal block, j <= ii) or
@@ -113,7 +113,7 @@ __device__ __noinline__ void residual_fp64(int n, const double* __restrict__ a, 
       for (int u = 0; u < U; ++u) {
         const int j = j0 + u;
         if (j < n) {
-          if (with_norm) rs += fabs(av[u]);
+          if (with_norm) rs += abs_f32_lower(av[u]);
 #pragma unroll
           for (int c = 0; c < kRhsChunk; ++c) acc[c] = fma(-av[u], Xd[(size_t)c * ldx + j], acc[c]);
         }
@@ -392,24 +392,33 @@ __device__ void mixed_one(const MixedArgs& g, int s, unsigned char* smem, int* s
   float* W32 = reinterpret_cast<float*>(g.W + g.aoff[s]);
 
   // 1. convert A's lower triangle to FP32 (one conversion per element: on
-  //    this part an FP64<->FP32 conversion costs an FP64 issue slot).
+  //    this part a hardware FP64<->FP32 conversion costs an FP64 issue slot,
+  //    so the normal-range conversion is done with integer instructions).
+  //    Only the lower triangle is read: warp w takes the column pairs
+  //    (c, n-1-c), c = w, w + 4, ..., whose n + 1 rows are one run of
+  //    coalesced 32-row chunks, up to 9 loads in flight per lane.
   //    ||A||_inf is accumulated by the first FP64 residual pass.
   if (tid == 0) *s_info = 0;
   {
-    const int nn = n * n;
-    for (int e0 = tid; e0 < nn; e0 += 8 * kCholThreads) {
-      double v[8];
+    constexpr int U = 9;
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int c = warp; c < (n + 1) / 2; c += kCholThreads / 32) {
+      const int c2 = n - 1 - c;
+      const int len1 = n - c;                             // rows c..n-1 of column c
+      const int len = (c2 == c) ? len1 : len1 + (c + 1);  // and rows c2..n-1 of column c2
+      for (int k0 = 0; k0 < len; k0 += U * 32) {
+        double v[U];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + u * kCholThreads;
-        v[u] = (e < nn) ? a[e] : 0.0;
-      }
+        for (int u = 0; u < U; ++u) {
+          const int k = k0 + u * 32 + lane;
+          const int idx = (k < len1) ? c * n + c + k : c2 * n + c2 + (k - len1);  // n*n < 2^31
+          v[u] = (k < len) ? a[idx] : 0.0;
+        }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + u * kCholThreads;
-        if (e < nn) {
-          const int c = e / n, r = e - c * n;
-          if (r >= c) W32[e] = (float)v[u];
+        for (int u = 0; u < U; ++u) {
+          const int k = k0 + u * 32 + lane;
+          const int idx = (k < len1) ? c * n + c + k : c2 * n + c2 + (k - len1);
+          if (k < len) W32[idx] = f64_to_f32_rn(v[u]);
         }
       }
     }
@@ -438,14 +447,14 @@ __device__ void mixed_one(const MixedArgs& g, int s, unsigned char* smem, int* s
     if (tid < kRhsChunk) nrm[kDprev + tid] = 0;
     for (int it = 0; it < g.max_iter; ++it) {
       __syncthreads();
-      double rowmax = 0.0;
+      float rowmax = 0.0f;
       residual_fp64(n, a, b, nr, Xd, Rd, ldp, it == 0, &rowmax);
       ++used;
       __syncthreads();
       if (it == 0) {  // ||A||_inf: max over the CTA (integer compare on the bits)
-        unsigned long long av[kRhsChunk] = {abs_bits(rowmax), 0, 0, 0};
+        unsigned long long av[kRhsChunk] = {(unsigned long long)__float_as_uint(rowmax), 0, 0, 0};
         block_max4(av, red);
-        anorm = __longlong_as_double((long long)av[0]);
+        anorm = (double)__uint_as_float((unsigned)av[0]);  // FP32 row sums; inf only past FLT_MAX
       }
       {
         unsigned long long rn[kRhsChunk] = {0, 0, 0, 0}, xn[kRhsChunk] = {0, 0, 0, 0};
@@ -459,7 +468,7 @@ __device__ void mixed_one(const MixedArgs& g, int s, unsigned char* smem, int* s
         block_max4_to(rn, red, nrm + kRn);
         block_max4_to(xn, red, nrm + kXn);
       }
-      bool ok = true, finite = true;
+      bool ok = true, finite = !isinf(anorm);  // ||A||_inf beyond FP32: the FP64 form takes over
       for (int c = 0; c < nr; ++c) {
         if (nrm[kRn + c] >= 0x7ff0000000000000ull || nrm[kXn + c] >= 0x7ff0000000000000ull) finite = false;
         const double rr = __longlong_as_double((long long)nrm[kRn + c]);

@@ -87,4 +87,34 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// binary64 -> binary32, round to nearest even, from the IEEE 754 bit fields
+// with integer instructions: where the result is a normal binary32 number
+// (biased binary64 exponent 897..1150) the exponent is re-biased by
+// 1023 - 127 = 896, the top 23 of the 52 fraction bits are kept and the 29
+// dropped bits round (ties to even; a carry into the exponent is the correct
+// rounding, up to infinity).  Zero, subnormal results, overflow, inf and NaN
+// take the hardware conversion.  Bit-identical to (float)x, and keeps the
+// conversion off the FP64 pipe, which the residuals need.
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned ah = hi & 0x7fffffffu;
+  if (ah >= 0x38100000u && ah < 0x47f00000u) {
+    unsigned m = __funnelshift_l(lo, ah, 3) - (896u << 23);  // exponent and 23 fraction bits (mod 2^32)
+    const unsigned rest = lo & 0x1fffffffu;
+    m += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(m | (hi & 0x80000000u));
+  }
+  return (float)x;
+}
+
+// A lower bound of |x| in binary32 for norm sums, from the high word alone:
+// the fraction truncated to 20 bits, magnitudes below 2^-127 counted as 0 and
+// above the binary32 range clamped just under FLT_MAX (a smaller ||A|| only
+// tightens the stopping test).
+__device__ __forceinline__ float abs_f32_lower(double x) {
+  unsigned h = (unsigned)__double2hiint(x) & 0x7fffffffu;
+  h = min(max(h, 0x38000000u), 0x47efffffu);
+  return __uint_as_float((h - 0x38000000u) << 3);
+}
+
 }  // namespace nacu
