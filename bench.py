@@ -435,9 +435,9 @@ _FP64_PEAK = {}
 # dominant kernel, from one ncu capture of a smaller case of the same workload,
 # scaled to a full launch by the systems processed (traffic grows with them).
 PROFILED_TRAFFIC = {
-    # 1.342 GB read + 0.245 GB written for a 2000-system slice of the same size
+    # 1.269 GB read + 0.277 GB written for a 2000-system slice of the same size
     # distribution (profiles/chol_mixed_kernel__ragged_spd_2000.md), x 10 systems
-    "chol_mixed_kernel": (15.87e9, "ncu capture of 2000 systems, scaled x10 by systems processed "
+    "chol_mixed_kernel": (15.46e9, "ncu capture of 2000 systems, scaled x10 by systems processed "
                                    "(profiles/chol_mixed_kernel__ragged_spd_2000.md)"),
 }
 

@@ -67,17 +67,20 @@ __device__ __forceinline__ uint64_t pivot_key(float x, bool first) {
   return (uint64_t)b;
 }
 
-// Warp argmax of (key, idx): larger key wins, equal keys keep the lower index.
+// Warp argmax of (key, idx): larger key wins, equal keys keep the lower index;
+// every lane receives the result.  Three warp-wide reductions (redux.sync:
+// max of the key's high word, max of the low word among the lanes holding
+// that high word, min of the index among the lanes holding the whole key)
+// instead of a five-round shuffle butterfly of three values: the pivot search
+// sits on the critical path of every elimination step.
 __device__ __forceinline__ void warp_argmax(uint64_t& key, int& idx) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    uint64_t k2 = __shfl_xor_sync(0xffffffffu, key, off);
-    int i2 = __shfl_xor_sync(0xffffffffu, idx, off);
-    if (k2 > key || (k2 == key && i2 < idx)) {
-      key = k2;
-      idx = i2;
-    }
-  }
+  const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+  const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  const bool win = (hi == mh && lo == ml);
+  const unsigned mi = __reduce_min_sync(0xffffffffu, win ? (unsigned)idx : 0xffffffffu);
+  key = ((uint64_t)mh << 32) | ml;
+  idx = (int)mi;
 }
 
 template <typename T>

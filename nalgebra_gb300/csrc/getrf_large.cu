@@ -189,16 +189,11 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
           bw = q;
         }
       }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const uint64_t k2 = __shfl_xor_sync(0xffffffffu, bk, off);
-        const int i2 = __shfl_xor_sync(0xffffffffu, bi, off);
-        const int w2 = __shfl_xor_sync(0xffffffffu, bw, off);
-        if (k2 > bk || (k2 == bk && i2 < bi)) {
-          bk = k2;
-          bi = i2;
-          bw = w2;
-        }
+      {  // the winner's CTA: the lane holding the winning row (rows have one owner)
+        const int myi = bi;
+        warp_argmax(bk, bi);
+        const unsigned holder = __ballot_sync(0xffffffffu, myi == bi);
+        bw = __shfl_sync(0xffffffffu, bw, __ffs(holder) - 1);
       }
       if (lane == 0) {
         const bool zero = (bi == 0x7fffffff || bk == 0);  // all |x| == 0: skipped, lu.rs:107-110
