@@ -65,21 +65,55 @@ struct PanelArgs {
   PanelPub<T>* pub;
 };
 
-// The cluster form keeps each CTA's publication slots in its own shared
-// memory; the other CTAs of the cluster read them through distributed shared
-// memory.
-template <typename T>
-struct ClusterPub {
-  unsigned long long key[2];
-  int idx[2];
-  T row[2][kPanelMaxNb];
-  T diag[2][kPanelMaxNb];
-};
-template <typename T>
-__host__ __device__ constexpr size_t cluster_pub_bytes() {
-  return (sizeof(ClusterPub<T>) + 15) & ~(size_t)15;
-}
+// The cluster form gives each CTA a copy of every CTA's publication slots in
+// its own shared memory: each CTA pushes its candidate (key, row index, row)
+// and, when it owns it, row c into all CTAs of the cluster with remote
+// stores before the cluster barrier, so that after it the pivot decision and
+// the pivot row are local reads.  The header is followed by
+// T row[2][kClusterMaxCtas][nb] and T diag[2][nb].
 constexpr int kClusterMaxCtas = 16;
+struct ClusterPub {
+  unsigned long long key[2][kClusterMaxCtas];
+  int idx[2][kClusterMaxCtas];
+};
+constexpr size_t kClusterPubHead = (sizeof(ClusterPub) + 15) & ~(size_t)15;
+// Rows are stored with a stride of nb rounded up to 16 bytes (vector pushes).
+template <typename T>
+__host__ __device__ constexpr int cpub_stride(int nb) {
+  return (nb + (int)(16 / sizeof(T)) - 1) & ~((int)(16 / sizeof(T)) - 1);
+}
+template <typename T>
+__host__ __device__ constexpr size_t cluster_pub_bytes(int nb) {
+  return kClusterPubHead + (size_t)(2 * kClusterMaxCtas + 2) * cpub_stride<T>(nb) * sizeof(T);
+}
+template <typename T>
+__device__ __forceinline__ T* cpub_row(ClusterPub* p, int nb, int par, int q) {
+  return reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(p) + kClusterPubHead) +
+         (size_t)(par * kClusterMaxCtas + q) * cpub_stride<T>(nb);
+}
+template <typename T>
+__device__ __forceinline__ T* cpub_diag(ClusterPub* p, int nb, int par) {
+  return reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(p) + kClusterPubHead) +
+         (size_t)(2 * kClusterMaxCtas + par) * cpub_stride<T>(nb);
+}
+// Row r of the panel (columns 0..nb) into dst in 16-byte vectors: 16 threads
+// per destination (sub = 0..15), the tail element by element.
+template <typename T>
+__device__ __forceinline__ void push_row(T* dst, const T* P, int ldp, int r, int nb, int sub) {
+  constexpr int kV = 16 / sizeof(T);
+  const int nv = nb / kV;
+  for (int v = sub; v < nv; v += 16) {
+    T x[kV];
+#pragma unroll
+    for (int i = 0; i < kV; ++i) x[i] = P[(v * kV + i) * ldp + r];
+    if constexpr (kV == 4) {
+      *reinterpret_cast<float4*>(dst + v * kV) = make_float4(x[0], x[1], x[2], x[3]);
+    } else {
+      *reinterpret_cast<double2*>(dst + v * kV) = make_double2(x[0], x[1]);
+    }
+  }
+  for (int t = nv * kV + sub; t < nb; t += 16) dst[t] = P[t * ldp + r];
+}
 
 // One barrier per column: the candidates and the candidate rows are published
 // before it, so after it every CTA knows the pivot row's values without a
@@ -92,8 +126,8 @@ constexpr int kClusterMaxCtas = 16;
 template <typename T, bool CLUSTER>
 __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ClusterPub<T>* cpub = reinterpret_cast<ClusterPub<T>*>(smem_raw);  // cluster form only
-  T* P = reinterpret_cast<T*>(smem_raw + (CLUSTER ? cluster_pub_bytes<T>() : 0));  // P[t * ldp + r]
+  ClusterPub* cpub = reinterpret_cast<ClusterPub*>(smem_raw);  // cluster form only
+  T* P = reinterpret_cast<T*>(smem_raw + (CLUSTER ? cluster_pub_bytes<T>(g.nb) : 0));  // P[t * ldp + r]
   __shared__ uint64_t s_key[kPanelThreads / 32];
   __shared__ int s_idx[kPanelThreads / 32];
   __shared__ T s_prow[kPanelMaxNb];
@@ -109,7 +143,7 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
     G = gridDim.x;
     b = blockIdx.x;
   }
-  const int nb = g.nb, ldp = g.chunk;
+  const int nb = g.nb, ldp = g.chunk | 1;  // odd: row walks (t varies) hit distinct banks
   const int rb = g.j0 + b * g.chunk;
   const int nr = max(0, min(g.n, rb + g.chunk) - rb);
   T* A = g.A;
@@ -146,8 +180,7 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
       if (lane == 0) {
         s_win = idx;
         if constexpr (CLUSTER) {
-          cpub->key[par] = key;
-          cpub->idx[par] = (idx == 0x7fffffff) ? -1 : idx;
+          s_key[0] = key;  // read back after the barrier, for the push
         } else {
           pub->key[par][b] = key;
           pub->idx[par][b] = (idx == 0x7fffffff) ? -1 : idx;
@@ -156,17 +189,33 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
     }
     __syncthreads();
     // 2. publish my candidate row and, if I own it, row c
-    {
+    if constexpr (CLUSTER) {
+      // pushed into every CTA's copy of my slots (remote stores; the cluster
+      // barrier's release/acquire makes them visible)
+      cg::cluster_group cl = cg::this_cluster();
       const int w = s_win;
-      T* prow_out = CLUSTER ? cpub->row[par] : pub->row[par][b];
-      T* diag_out = CLUSTER ? cpub->diag[par] : pub->diag[par];
+      if (tid < G) {
+        ClusterPub* dst = cl.map_shared_rank(cpub, tid);
+        dst->key[par][b] = s_key[0];
+        dst->idx[par][b] = (w == 0x7fffffff) ? -1 : w;
+      }
+      const int q = tid >> 4;  // 16 threads per destination CTA
+      if (q < G) {
+        ClusterPub* dst = cl.map_shared_rank(cpub, q);
+        if (w != 0x7fffffff) push_row<T>(cpub_row<T>(dst, nb, par, b), P, ldp, w - rb, nb, tid & 15);
+        if (c >= rb && c < rb + nr) push_row<T>(cpub_diag<T>(dst, nb, par), P, ldp, c - rb, nb, tid & 15);
+      }
+      cl.sync();
+    } else {
+      const int w = s_win;
+      T* prow_out = pub->row[par][b];
+      T* diag_out = pub->diag[par];
       if (w != 0x7fffffff)
         for (int t = tid; t < nb; t += kPanelThreads) prow_out[t] = P[t * ldp + (w - rb)];
       if (c >= rb && c < rb + nr)
         for (int t = tid; t < nb; t += kPanelThreads) diag_out[t] = P[t * ldp + (c - rb)];
+      cg::this_grid().sync();
     }
-    if constexpr (CLUSTER) cg::this_cluster().sync();
-    else cg::this_grid().sync();
     // 3. the pivot: every CTA reduces the G candidates the same way
     if (warp == 0) {
       uint64_t bk = 0;
@@ -175,9 +224,8 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
         int ri;
         uint64_t kk;
         if constexpr (CLUSTER) {
-          const ClusterPub<T>* rp = cg::this_cluster().map_shared_rank(cpub, q);
-          ri = rp->idx[par];
-          kk = rp->key[par];
+          ri = cpub->idx[par][q];  // local copies
+          kk = cpub->key[par][q];
         } else {
           ri = pub->idx[par][q];
           kk = pub->key[par][q];
@@ -203,6 +251,8 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
           g.ipiv[c] = zero ? c : bi;
           if (zero) atomicMin(g.info, c + 1);
         }
+        if constexpr (CLUSTER)
+          if (!zero) s_inv = T(1) / cpub_row<T>(cpub, nb, par, bw)[j];
       }
     }
     __syncthreads();
@@ -210,25 +260,27 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
     if (piv < 0) continue;
     // 4. swap rows c and piv (their owners), from the published copies
     const bool own_c = (c >= rb && c < rb + nr), own_p = (piv >= rb && piv < rb + nr);
-    const T* win_row;
+    const T* prow;  // the pivot row
     const T* c_row;
     if constexpr (CLUSTER) {
-      win_row = cg::this_cluster().map_shared_rank(cpub, s_wcta)->row[par];
-      c_row = cg::this_cluster().map_shared_rank(cpub, (c - g.j0) / g.chunk)->diag[par];
+      prow = cpub_row<T>(cpub, nb, par, s_wcta);
+      c_row = cpub_diag<T>(cpub, nb, par);
     } else {
-      win_row = pub->row[par][s_wcta];
+      const T* win_row = pub->row[par][s_wcta];
       c_row = pub->diag[par];
+      for (int t = tid; t < nb; t += kPanelThreads) {
+        s_prow[t] = win_row[t];
+        if (own_p && piv != c) s_drow[t] = c_row[t];
+      }
+      if (tid == 0) s_inv = T(1) / win_row[j];
+      __syncthreads();
+      prow = s_prow;
+      c_row = s_drow;
     }
-    for (int t = tid; t < nb; t += kPanelThreads) {
-      s_prow[t] = win_row[t];
-      if (own_p && piv != c) s_drow[t] = c_row[t];
-    }
-    if (tid == 0) s_inv = T(1) / win_row[j];
-    __syncthreads();
     if (piv != c) {
       for (int t = tid; t < nb; t += kPanelThreads) {
-        if (own_c) P[t * ldp + (c - rb)] = s_prow[t];
-        if (own_p) P[t * ldp + (piv - rb)] = s_drow[t];
+        if (own_c) P[t * ldp + (c - rb)] = prow[t];
+        if (own_p) P[t * ldp + (piv - rb)] = c_row[t];
       }
       __syncthreads();
     }
@@ -246,13 +298,13 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
         for (; t + 12 < nb; t += 16) {
           const T p0 = P[t * ldp + r], p1 = P[(t + 4) * ldp + r], p2 = P[(t + 8) * ldp + r],
                   p3 = P[(t + 12) * ldp + r];
-          const T q0 = s_prow[t], q1 = s_prow[t + 4], q2 = s_prow[t + 8], q3 = s_prow[t + 12];
+          const T q0 = prow[t], q1 = prow[t + 4], q2 = prow[t + 8], q3 = prow[t + 12];
           P[t * ldp + r] = axpy1<false>(p0, -q0, l);
           P[(t + 4) * ldp + r] = axpy1<false>(p1, -q1, l);
           P[(t + 8) * ldp + r] = axpy1<false>(p2, -q2, l);
           P[(t + 12) * ldp + r] = axpy1<false>(p3, -q3, l);
         }
-        for (; t < nb; t += 4) P[t * ldp + r] = axpy1<false>(P[t * ldp + r], -s_prow[t], l);
+        for (; t < nb; t += 4) P[t * ldp + r] = axpy1<false>(P[t * ldp + r], -prow[t], l);
       }
     }
     __syncthreads();
@@ -782,7 +834,7 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
     const int rows = n - j0;
     PanelArgs<T> pa{n, A, lda, j0, jb, 0, ipiv, info, reinterpret_cast<PanelPub<T>*>(ws)};
     const int cchunk = cluster ? (rows + cluster - 1) / cluster : 0;
-    const size_t csmem = cluster_pub_bytes<T>() + (size_t)cchunk * jb * sizeof(T);
+    const size_t csmem = cluster_pub_bytes<T>(jb) + (size_t)(cchunk | 1) * jb * sizeof(T);
     if (cluster && csmem <= kPanelMaxSmem) {
       pa.chunk = cchunk;
       cudaLaunchConfig_t cfg = {};
@@ -800,14 +852,14 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
       e = cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, true>, pa);
       if (e != cudaSuccess) return record_cuda_error(e, name);
     } else {
-      const int max_rows = (int)(kPanelMaxSmem / ((size_t)jb * sizeof(T)));
+      const int max_rows = (int)(kPanelMaxSmem / ((size_t)jb * sizeof(T))) - 1;  // leading dimension chunk | 1
       int G = std::max((rows + kPanelRowsPerCta - 1) / kPanelRowsPerCta, (rows + max_rows - 1) / max_rows);
       G = std::max(1, std::min(G, gmax));
       const int chunk = (rows + G - 1) / G;
       if (chunk > max_rows) return record_arg_error(-1, "getrf: n too large for the shared-memory panel");
       pa.chunk = chunk;
       void* args[] = {&pa};
-      e = cudaLaunchCooperativeKernel(pk, G, kPanelThreads, args, (size_t)chunk * jb * sizeof(T), sp);
+      e = cudaLaunchCooperativeKernel(pk, G, kPanelThreads, args, (size_t)(chunk | 1) * jb * sizeof(T), sp);
       if (e != cudaSuccess) return record_cuda_error(e, name);
     }
     if (rest_pending) {  // the swaps below touch the columns the previous update is still writing
