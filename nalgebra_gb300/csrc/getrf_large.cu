@@ -115,6 +115,51 @@ __device__ __forceinline__ void push_row(T* dst, const T* P, int ldp, int r, int
   for (int t = nv * kV + sub; t < nb; t += 16) dst[t] = P[t * ldp + r];
 }
 
+// Composes the panel's swaps into one mapping for the columns outside it
+// (one CTA): slots 0..nb-1 are rows j0.., slot nb + i the first swap partner
+// ipiv[j0+i] below the panel.
+template <typename T>
+__device__ void panel_compose_swaps(const PanelArgs<T>& g, int nb, int tid) {
+  PanelPub<T>* pub = g.pub;
+  __shared__ int s_slot[kPanelMaxNb];
+  __shared__ int s_row[2 * kPanelMaxNb];
+  __shared__ int s_src[2 * kPanelMaxNb];
+  for (int i = tid; i < nb; i += kPanelThreads) {
+    const int p = g.ipiv[g.j0 + i];
+    int slot = p - g.j0;
+    if (p >= g.j0 + nb) {
+      int f = i;
+      for (int q = 0; q < i; ++q)
+        if (g.ipiv[g.j0 + q] == p) {
+          f = q;
+          break;
+        }
+      slot = nb + f;
+    }
+    s_slot[i] = slot;
+    s_row[i] = g.j0 + i;
+    s_row[nb + i] = p;
+  }
+  for (int sl = tid; sl < 2 * nb; sl += kPanelThreads) s_src[sl] = sl;
+  __syncthreads();
+  if (tid == 0) {
+    for (int i = 0; i < nb; ++i) {
+      const int o = s_slot[i];
+      const int t = s_src[i];
+      s_src[i] = s_src[o];
+      s_src[o] = t;
+    }
+    int k = 0;
+    for (int sl = 0; sl < 2 * nb; ++sl)
+      if (s_src[sl] != sl) {
+        pub->pdst[k] = s_row[sl];
+        pub->psrc[k] = s_row[s_src[sl]];
+        ++k;
+      }
+    pub->npairs = k;
+  }
+}
+
 // One barrier per column: the candidates and the candidate rows are published
 // before it, so after it every CTA knows the pivot row's values without a
 // second exchange; row c and the pivot row are swapped by their owners
@@ -313,49 +358,201 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
     const int t = e / nr, r = e - t * nr;
     A[(size_t)(g.j0 + t) * lda + rb + r] = P[t * ldp + r];
   }
-  if (b == 0) {
-    // compose the panel's swaps into one mapping for the columns outside it:
-    // slots 0..nb-1 are rows j0.., slot nb + i the first swap partner ipiv[j0+i]
-    // below the panel (ipiv was written by this CTA's thread 0)
-    __shared__ int s_slot[kPanelMaxNb];
-    __shared__ int s_row[2 * kPanelMaxNb];
-    __shared__ int s_src[2 * kPanelMaxNb];
-    for (int i = tid; i < nb; i += kPanelThreads) {
-      const int p = g.ipiv[g.j0 + i];
-      int slot = p - g.j0;
-      if (p >= g.j0 + nb) {
-        int f = i;
-        for (int q = 0; q < i; ++q)
-          if (g.ipiv[g.j0 + q] == p) {
-            f = q;
-            break;
-          }
-        slot = nb + f;
-      }
-      s_slot[i] = slot;
-      s_row[i] = g.j0 + i;
-      s_row[nb + i] = p;
-    }
-    for (int sl = tid; sl < 2 * nb; sl += kPanelThreads) s_src[sl] = sl;
-    __syncthreads();
-    if (tid == 0) {
-      for (int i = 0; i < nb; ++i) {
-        const int o = s_slot[i];
-        const int t = s_src[i];
-        s_src[i] = s_src[o];
-        s_src[o] = t;
-      }
-      int k = 0;
-      for (int sl = 0; sl < 2 * nb; ++sl)
-        if (s_src[sl] != sl) {
-          pub->pdst[k] = s_row[sl];
-          pub->psrc[k] = s_row[s_src[sl]];
-          ++k;
-        }
-      pub->npairs = k;
-    }
-  }
+  __syncthreads();  // the pivots thread 0 wrote, for the composition
+  if (b == 0) panel_compose_swaps(g, nb, tid);
   if constexpr (CLUSTER) cg::this_cluster().sync();  // no CTA leaves while others may read its slots
+}
+
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// The cluster form with look-ahead inside the panel.  Column j's rank-1
+// update is split: the next column (j+1) is updated at once, so that its
+// pivot search can start, and the rest (columns j+2..) is deferred into the
+// next column's exchange, between the cluster barrier's arrive and wait, where
+// it hides the barrier's latency.  The candidate rows pushed for column j+1
+// therefore still lack column j's update of columns j+2..; every CTA applies
+// it to its copies with the same operands (fma(-u_t, l, x)), so the copies
+// stay bit-identical to the rows their owners update.  The pivot decision and
+// the pivot row are local reads (rows pushed into every CTA before the
+// barrier, as in lu_panel_kernel<T, true>).
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(PanelArgs<T> g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ClusterPub* cpub = reinterpret_cast<ClusterPub*>(smem_raw);
+  T* P = reinterpret_cast<T*>(smem_raw + cluster_pub_bytes<T>(g.nb));  // P[t * ldp + r]
+  constexpr int kWarps = kPanelThreads / 32;
+  __shared__ uint64_t s_key[kWarps];
+  __shared__ int s_idx[kWarps];
+  __shared__ T s_prev[kPanelMaxNb];  // the last eliminated column's pivot row (complete)
+  __shared__ uint64_t s_ckey;
+  __shared__ int s_win, s_piv, s_wcta;
+  __shared__ T s_inv;
+  cg::cluster_group cl = cg::this_cluster();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int G = (int)cl.num_blocks(), b = (int)cl.block_rank();
+  const int nb = g.nb, ldp = g.chunk | 1;
+  const int rb = g.j0 + b * g.chunk;
+  const int nr = max(0, min(g.n, rb + g.chunk) - rb);
+  T* A = g.A;
+  const int64_t lda = g.lda;
+  for (int e = tid; e < nb * nr; e += kPanelThreads) {
+    const int t = e / nr, r = e - t * nr;
+    P[t * ldp + r] = A[(size_t)(g.j0 + t) * lda + rb + r];
+  }
+  __syncthreads();
+  bool pend = false;  // column j-1 was eliminated and its update of columns j+1.. is pending
+  for (int j = 0; j < nb; ++j) {
+    const int c = g.j0 + j, par = j & 1;
+    // 1. my candidate: the largest |x| of column j over my rows >= c
+    //    (icamax, src/base/min_max.rs:221-240: first index on ties)
+    uint64_t key = 0;
+    int idx = 0x7fffffff;
+    for (int r = max(0, c - rb) + tid; r < nr; r += kPanelThreads) {
+      const uint64_t k = pivot_key(P[j * ldp + r], rb + r == c);
+      if (idx == 0x7fffffff || k > key) {
+        key = k;
+        idx = rb + r;
+      }
+    }
+    warp_argmax(key, idx);
+    if (lane == 0) {
+      s_key[warp] = key;
+      s_idx[warp] = idx;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      key = lane < kWarps ? s_key[lane] : 0ull;
+      idx = lane < kWarps ? s_idx[lane] : 0x7fffffff;
+      warp_argmax(key, idx);
+      if (lane == 0) {
+        s_win = idx;
+        s_ckey = key;
+      }
+    }
+    __syncthreads();
+    // 2. push my candidate (key, row index, row) and, if I own it, row c into
+    //    every CTA of the cluster
+    {
+      const int w = s_win;
+      if (tid < G) {
+        ClusterPub* dst = cl.map_shared_rank(cpub, tid);
+        dst->key[par][b] = s_ckey;
+        dst->idx[par][b] = (w == 0x7fffffff) ? -1 : w;
+      }
+      const int q = tid >> 4;  // 16 threads per destination CTA
+      if (q < G) {
+        ClusterPub* dst = cl.map_shared_rank(cpub, q);
+        if (w != 0x7fffffff) push_row<T>(cpub_row<T>(dst, nb, par, b), P, ldp, w - rb, nb, tid & 15);
+        if (c >= rb && c < rb + nr) push_row<T>(cpub_diag<T>(dst, nb, par), P, ldp, c - rb, nb, tid & 15);
+      }
+    }
+    __syncthreads();  // the rows are read out before the deferred update changes them
+    cluster_arrive_release();
+    // 3. deferred: column j-1's update of columns j+1.. (rows >= c; gauss_step,
+    //    lu.rs:340-357), while the other CTAs arrive
+    if (pend && j + 1 < nb) {
+      const int tr = tid & 63, tc = tid >> 6;  // rows r0 + tr + 64 i, columns j + 1 + tc + 4 k
+      for (int r = max(0, c - rb) + tr; r < nr; r += 64) {
+        const T l = P[(j - 1) * ldp + r];
+        int t = j + 1 + tc;
+        for (; t + 12 < nb; t += 16) {
+          const T p0 = P[t * ldp + r], p1 = P[(t + 4) * ldp + r], p2 = P[(t + 8) * ldp + r],
+                  p3 = P[(t + 12) * ldp + r];
+          const T q0 = s_prev[t], q1 = s_prev[t + 4], q2 = s_prev[t + 8], q3 = s_prev[t + 12];
+          P[t * ldp + r] = axpy1<false>(p0, -q0, l);
+          P[(t + 4) * ldp + r] = axpy1<false>(p1, -q1, l);
+          P[(t + 8) * ldp + r] = axpy1<false>(p2, -q2, l);
+          P[(t + 12) * ldp + r] = axpy1<false>(p3, -q3, l);
+        }
+        for (; t < nb; t += 4) P[t * ldp + r] = axpy1<false>(P[t * ldp + r], -s_prev[t], l);
+      }
+    }
+    cluster_wait_acquire();
+    // 4. the pivot, from the local copies of the G candidates
+    if (warp == 0) {
+      uint64_t bk = 0;
+      int bi = 0x7fffffff, bw = 0;
+      if (lane < G) {
+        const int ri = cpub->idx[par][lane];
+        if (ri >= 0) {
+          bk = cpub->key[par][lane];
+          bi = ri;
+          bw = lane;
+        }
+      }
+      const int myi = bi;
+      warp_argmax(bk, bi);
+      const unsigned holder = __ballot_sync(0xffffffffu, myi == bi);
+      bw = __shfl_sync(0xffffffffu, bw, __ffs(holder) - 1);
+      if (lane == 0) {
+        const bool zero = (bi == 0x7fffffff || bk == 0);  // all |x| == 0: skipped, lu.rs:107-110
+        s_piv = zero ? -1 : bi;
+        s_wcta = bw;
+        if (b == 0) {
+          g.ipiv[c] = zero ? c : bi;
+          if (zero) atomicMin(g.info, c + 1);
+        }
+        if (!zero) s_inv = T(1) / cpub_row<T>(cpub, nb, par, bw)[j];  // column j: complete in the copy
+      }
+    }
+    __syncthreads();
+    const int piv = s_piv;
+    if (piv < 0) {  // nothing to eliminate; column j+1 already has every earlier update
+      pend = false;
+      continue;
+    }
+    // 5. complete the copies (column j-1's pending update), keep the pivot row
+    //    for the next column, and swap rows c and piv (their owners)
+    {
+      const T* prow = cpub_row<T>(cpub, nb, par, s_wcta);
+      const T* crow = cpub_diag<T>(cpub, nb, par);
+      const bool own_c = (c >= rb && c < rb + nr), own_p = (piv >= rb && piv < rb + nr);
+      const bool swap = (piv != c);
+      const bool need_c = swap && own_p;
+      const T lp = pend ? prow[j - 1] : T(0);
+      const T lc = (pend && need_c) ? crow[j - 1] : T(0);
+      for (int t = tid; t < nb; t += kPanelThreads) {
+        T pv = prow[t];
+        T cv = need_c ? crow[t] : T(0);
+        if (pend && t > j) {
+          const T u = s_prev[t];
+          pv = axpy1<false>(pv, -u, lp);
+          if (need_c) cv = axpy1<false>(cv, -u, lc);
+        }
+        s_prev[t] = pv;
+        if (swap) {
+          if (own_c) P[t * ldp + (c - rb)] = pv;
+          if (own_p) P[t * ldp + (piv - rb)] = cv;
+        }
+      }
+    }
+    __syncthreads();
+    // 6. multipliers of column j below row c, and their update of column j+1
+    //    (the look-ahead column); the rest of the update is deferred
+    {
+      const T inv = s_inv;
+      const T u = (j + 1 < nb) ? s_prev[j + 1] : T(0);
+      for (int r = max(0, c + 1 - rb) + tid; r < nr; r += kPanelThreads) {
+        const T l = P[j * ldp + r] * inv;
+        P[j * ldp + r] = l;
+        if (j + 1 < nb) P[(j + 1) * ldp + r] = axpy1<false>(P[(j + 1) * ldp + r], -u, l);
+      }
+    }
+    pend = true;
+    __syncthreads();
+  }
+  for (int e = tid; e < nb * nr; e += kPanelThreads) {
+    const int t = e / nr, r = e - t * nr;
+    A[(size_t)(g.j0 + t) * lda + rb + r] = P[t * ldp + r];
+  }
+  __syncthreads();  // the pivots thread 0 wrote, for the composition
+  if (b == 0) panel_compose_swaps(g, nb, tid);
+  cl.sync();  // every remote access to this CTA's shared memory is over
 }
 
 // ---------------------------------------------------------------------------
@@ -776,7 +973,7 @@ int panel_cluster_ctas() {
   static int ctas = -1;
   if (ctas >= 0) return ctas;
   ctas = 0;
-  auto kern = lu_panel_kernel<T, true>;
+  auto kern = lu_panel_cluster_kernel<T>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelMaxSmem) != cudaSuccess ||
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
     cudaGetLastError();
@@ -849,7 +1046,7 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
       at[0].val.clusterDim.z = 1;
       cfg.attrs = at;
       cfg.numAttrs = 1;
-      e = cudaLaunchKernelEx(&cfg, lu_panel_kernel<T, true>, pa);
+      e = cudaLaunchKernelEx(&cfg, lu_panel_cluster_kernel<T>, pa);
       if (e != cudaSuccess) return record_cuda_error(e, name);
     } else {
       const int max_rows = (int)(kPanelMaxSmem / ((size_t)jb * sizeof(T))) - 1;  // leading dimension chunk | 1
