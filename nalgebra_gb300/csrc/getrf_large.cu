@@ -160,19 +160,17 @@ __device__ void panel_compose_swaps(const PanelArgs<T>& g, int nb, int tid) {
   }
 }
 
-// One barrier per column: the candidates and the candidate rows are published
-// before it, so after it every CTA knows the pivot row's values without a
-// second exchange; row c and the pivot row are swapped by their owners
-// (nalgebra swaps whole rows, lu.rs:111-116; the columns outside the panel are
-// swapped afterwards by lu_swap_kernel).  CLUSTER = false: a cooperative grid,
-// the exchange through global memory and a grid barrier; CLUSTER = true: one
-// thread-block cluster, the exchange through distributed shared memory and a
-// cluster barrier (about a quarter of the grid barrier's latency).
-template <typename T, bool CLUSTER>
-__global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g) {
+// The grid form (the panel's rows spread over a cooperative grid, for panels
+// too tall for one cluster's shared memory).  One grid barrier per column:
+// the candidates and the candidate rows are published in global memory before
+// it, so after it every CTA knows the pivot row's values without a second
+// exchange; row c and the pivot row are swapped by their owners (nalgebra
+// swaps whole rows, lu.rs:111-116; the columns outside the panel are swapped
+// afterwards by lu_swap_kernel).
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads) lu_panel_grid_kernel(PanelArgs<T> g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ClusterPub* cpub = reinterpret_cast<ClusterPub*>(smem_raw);  // cluster form only
-  T* P = reinterpret_cast<T*>(smem_raw + (CLUSTER ? cluster_pub_bytes<T>(g.nb) : 0));  // P[t * ldp + r]
+  T* P = reinterpret_cast<T*>(smem_raw);  // P[t * ldp + r]
   __shared__ uint64_t s_key[kPanelThreads / 32];
   __shared__ int s_idx[kPanelThreads / 32];
   __shared__ T s_prow[kPanelMaxNb];
@@ -180,14 +178,7 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
   __shared__ int s_win, s_piv, s_wcta;
   __shared__ T s_inv;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int G, b;
-  if constexpr (CLUSTER) {
-    G = (int)cg::this_cluster().num_blocks();
-    b = (int)cg::this_cluster().block_rank();
-  } else {
-    G = gridDim.x;
-    b = blockIdx.x;
-  }
+  const int G = gridDim.x, b = blockIdx.x;
   const int nb = g.nb, ldp = g.chunk | 1;  // odd: row walks (t varies) hit distinct banks
   const int rb = g.j0 + b * g.chunk;
   const int nr = max(0, min(g.n, rb + g.chunk) - rb);
@@ -224,34 +215,13 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
       warp_argmax(key, idx);
       if (lane == 0) {
         s_win = idx;
-        if constexpr (CLUSTER) {
-          s_key[0] = key;  // read back after the barrier, for the push
-        } else {
-          pub->key[par][b] = key;
-          pub->idx[par][b] = (idx == 0x7fffffff) ? -1 : idx;
-        }
+        pub->key[par][b] = key;
+        pub->idx[par][b] = (idx == 0x7fffffff) ? -1 : idx;
       }
     }
     __syncthreads();
     // 2. publish my candidate row and, if I own it, row c
-    if constexpr (CLUSTER) {
-      // pushed into every CTA's copy of my slots (remote stores; the cluster
-      // barrier's release/acquire makes them visible)
-      cg::cluster_group cl = cg::this_cluster();
-      const int w = s_win;
-      if (tid < G) {
-        ClusterPub* dst = cl.map_shared_rank(cpub, tid);
-        dst->key[par][b] = s_key[0];
-        dst->idx[par][b] = (w == 0x7fffffff) ? -1 : w;
-      }
-      const int q = tid >> 4;  // 16 threads per destination CTA
-      if (q < G) {
-        ClusterPub* dst = cl.map_shared_rank(cpub, q);
-        if (w != 0x7fffffff) push_row<T>(cpub_row<T>(dst, nb, par, b), P, ldp, w - rb, nb, tid & 15);
-        if (c >= rb && c < rb + nr) push_row<T>(cpub_diag<T>(dst, nb, par), P, ldp, c - rb, nb, tid & 15);
-      }
-      cl.sync();
-    } else {
+    {
       const int w = s_win;
       T* prow_out = pub->row[par][b];
       T* diag_out = pub->diag[par];
@@ -259,22 +229,15 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
         for (int t = tid; t < nb; t += kPanelThreads) prow_out[t] = P[t * ldp + (w - rb)];
       if (c >= rb && c < rb + nr)
         for (int t = tid; t < nb; t += kPanelThreads) diag_out[t] = P[t * ldp + (c - rb)];
-      cg::this_grid().sync();
     }
+    cg::this_grid().sync();
     // 3. the pivot: every CTA reduces the G candidates the same way
     if (warp == 0) {
       uint64_t bk = 0;
       int bi = 0x7fffffff, bw = 0;
       for (int q = lane; q < G; q += 32) {
-        int ri;
-        uint64_t kk;
-        if constexpr (CLUSTER) {
-          ri = cpub->idx[par][q];  // local copies
-          kk = cpub->key[par][q];
-        } else {
-          ri = pub->idx[par][q];
-          kk = pub->key[par][q];
-        }
+        const int ri = pub->idx[par][q];
+        const uint64_t kk = pub->key[par][q];
         if (ri < 0) continue;
         if (bi == 0x7fffffff || kk > bk || (kk == bk && ri < bi)) {
           bk = kk;
@@ -296,8 +259,6 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
           g.ipiv[c] = zero ? c : bi;
           if (zero) atomicMin(g.info, c + 1);
         }
-        if constexpr (CLUSTER)
-          if (!zero) s_inv = T(1) / cpub_row<T>(cpub, nb, par, bw)[j];
       }
     }
     __syncthreads();
@@ -305,27 +266,20 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
     if (piv < 0) continue;
     // 4. swap rows c and piv (their owners), from the published copies
     const bool own_c = (c >= rb && c < rb + nr), own_p = (piv >= rb && piv < rb + nr);
-    const T* prow;  // the pivot row
-    const T* c_row;
-    if constexpr (CLUSTER) {
-      prow = cpub_row<T>(cpub, nb, par, s_wcta);
-      c_row = cpub_diag<T>(cpub, nb, par);
-    } else {
+    {
       const T* win_row = pub->row[par][s_wcta];
-      c_row = pub->diag[par];
+      const T* c_row = pub->diag[par];
       for (int t = tid; t < nb; t += kPanelThreads) {
         s_prow[t] = win_row[t];
         if (own_p && piv != c) s_drow[t] = c_row[t];
       }
       if (tid == 0) s_inv = T(1) / win_row[j];
-      __syncthreads();
-      prow = s_prow;
-      c_row = s_drow;
     }
+    __syncthreads();
     if (piv != c) {
       for (int t = tid; t < nb; t += kPanelThreads) {
-        if (own_c) P[t * ldp + (c - rb)] = prow[t];
-        if (own_p) P[t * ldp + (piv - rb)] = c_row[t];
+        if (own_c) P[t * ldp + (c - rb)] = s_prow[t];
+        if (own_p) P[t * ldp + (piv - rb)] = s_drow[t];
       }
       __syncthreads();
     }
@@ -343,13 +297,13 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
         for (; t + 12 < nb; t += 16) {
           const T p0 = P[t * ldp + r], p1 = P[(t + 4) * ldp + r], p2 = P[(t + 8) * ldp + r],
                   p3 = P[(t + 12) * ldp + r];
-          const T q0 = prow[t], q1 = prow[t + 4], q2 = prow[t + 8], q3 = prow[t + 12];
+          const T q0 = s_prow[t], q1 = s_prow[t + 4], q2 = s_prow[t + 8], q3 = s_prow[t + 12];
           P[t * ldp + r] = axpy1<false>(p0, -q0, l);
           P[(t + 4) * ldp + r] = axpy1<false>(p1, -q1, l);
           P[(t + 8) * ldp + r] = axpy1<false>(p2, -q2, l);
           P[(t + 12) * ldp + r] = axpy1<false>(p3, -q3, l);
         }
-        for (; t < nb; t += 4) P[t * ldp + r] = axpy1<false>(P[t * ldp + r], -prow[t], l);
+        for (; t < nb; t += 4) P[t * ldp + r] = axpy1<false>(P[t * ldp + r], -s_prow[t], l);
       }
     }
     __syncthreads();
@@ -360,7 +314,6 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_kernel(PanelArgs<T> g)
   }
   __syncthreads();  // the pivots thread 0 wrote, for the composition
   if (b == 0) panel_compose_swaps(g, nb, tid);
-  if constexpr (CLUSTER) cg::this_cluster().sync();  // no CTA leaves while others may read its slots
 }
 
 __device__ __forceinline__ void cluster_arrive_release() {
@@ -379,7 +332,7 @@ __device__ __forceinline__ void cluster_wait_acquire() {
 // it to its copies with the same operands (fma(-u_t, l, x)), so the copies
 // stay bit-identical to the rows their owners update.  The pivot decision and
 // the pivot row are local reads (rows pushed into every CTA before the
-// barrier, as in lu_panel_kernel<T, true>).
+// barrier: no remote reads).
 template <typename T>
 __global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(PanelArgs<T> g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1011,7 +964,7 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
                   void* ctx, cudaStream_t s, const char* name) {
   cudaError_t e;
   if (nb > kPanelMaxNb) nb = kPanelMaxNb;
-  const void* pk = reinterpret_cast<const void*>(lu_panel_kernel<T, false>);
+  const void* pk = reinterpret_cast<const void*>(lu_panel_grid_kernel<T>);
   e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelMaxSmem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   const int cluster = panel_cluster_ctas<T>();
