@@ -114,3 +114,43 @@ def test_mirror_solve_refined_and_graph_capture(cuda):
     xs = out.to_numpy()
     for m, r, x in zip(mats, rhs, xs):
         assert O.backward_error(m, x, r) <= m.shape[0] * EPS64
+
+
+def test_reads_only_the_lower_triangle(cuda):
+    """nalgebra's Cholesky reads only the lower triangle (cholesky.rs:221-272):
+    NaN in the strict upper triangle leaves every result bit-identical."""
+    w = W.ragged_spd(60, 8, 200, nrhs=4, seed=11)
+    ns, aoff = w["ns"], w["a_offsets"]
+    poisoned = w["a_flat"].copy()
+    for s in range(ns.size):
+        n = int(ns[s])
+        m = poisoned[aoff[s]:aoff[s] + n * n].reshape(n, n)  # row-major view of the column-major matrix
+        m[np.tril_indices(n, -1)] = np.nan                   # (i > j) here is column i, row j < i: A's strict upper part
+    _, _, X0, info0, it0, _, _ = _mixed(cuda, ns, w["a_flat"], w["b_flat"], 4)
+    _, _, X1, info1, it1, _, _ = _mixed(cuda, ns, poisoned, w["b_flat"], 4)
+    assert np.array_equal(info0, info1) and np.array_equal(it0, it1)
+    assert np.array_equal(X0.view(np.uint64), X1.view(np.uint64))
+
+
+@pytest.mark.parametrize("scale", [1e-36, 1e-20, 1e20, 1e36])
+def test_extreme_scales_stay_correct(cuda, scale):
+    """Entries near the ends of the FP32 range: the FP32 copy (integer
+    conversion of the bit fields in the normal range, the hardware conversion
+    outside it), the FP32 row sums of ||A|| (FP64 fallback when they overflow)
+    and the refinement still meet the FP64 target, converged or fallen back."""
+    rng = np.random.default_rng(int(abs(np.log10(scale))))
+    mats = []
+    for n in (12, 40, 96):
+        bm = rng.standard_normal((n, n))
+        mats.append(scale * (bm @ bm.T + n * np.eye(n)))
+    ns = [m.shape[0] for m in mats]
+    a_flat = np.concatenate([m.ravel(order="F") for m in mats])
+    b_flat = scale * rng.standard_normal(sum(ns) * 2)
+    A, B, X, info, iters, aoff, boff = _mixed(cuda, ns, a_flat, b_flat, 2)
+    assert np.all(info == 0)
+    for s, m in enumerate(mats):
+        n = ns[s]
+        x = X[boff[s]:boff[s] + 2 * n].reshape(2, n).T
+        b = b_flat[boff[s]:boff[s] + 2 * n].reshape(2, n).T
+        assert np.all(np.isfinite(x))
+        assert O.backward_error(m, x, b) <= n * EPS64, (scale, s, iters[s])
