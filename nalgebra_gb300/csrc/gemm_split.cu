@@ -19,11 +19,13 @@
 // speed instead of the ~1 TFLOP/s FP64 pipe.
 //
 // Kernel: one 128 x 256 output tile per CTA, 128 threads.  Warp 0 / lane 0
-// issues TMA loads (cp.async.bulk.tensor.2d, 128-byte swizzle) of the A slice
-// tile (128 x 64 BF16) and the B slice tile (256 x 64 BF16) into a 4-stage
-// shared-memory ring; warp 1 / lane 0 issues tcgen05.mma 128 x 256 x 16 from
-// the staged tiles into a 256-column FP32 TMEM accumulator and releases each
-// stage with tcgen05.commit; after the last product all four warps read the
+// issues TMA loads (cp.async.bulk.tensor.2d, 64-byte swizzle) of every slice
+// tile of a 32-deep k-block -- s A tiles (128 x 32 BF16) and s B tiles
+// (256 x 32 BF16) -- into one stage of a 3-stage shared-memory ring, so each
+// slice tile crosses L2 once; warp 1 / lane 0 issues the k-block's slice
+// products as tcgen05.mma 128 x 256 x 16 from that stage into a 256-column
+// FP32 TMEM accumulator and releases the stage with tcgen05.commit; after the
+// last k-block all four warps read the
 // accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = rows) and
 // write C.  Every mbarrier wait is bounded: on time-out the kernel records an
 // error flag and finishes without further waiting.
@@ -35,12 +37,16 @@
 namespace nacu {
 namespace {
 
-constexpr int kTM = 128, kTN = 256, kTK = 64;  // output tile, K tile (BF16: 128 bytes)
-constexpr int kStages = 4;
+constexpr int kTM = 128, kTN = 256, kTK = 64;  // output tile; K padding of the slice buffers
+// One ring stage holds every slice tile of a 32-deep k-block (64-byte rows,
+// 64-byte swizzle): each slice tile crosses L2 once per k-block, and all the
+// slice products of that k-block are issued from the one stage.
+constexpr int kKB = 32;
+constexpr int kStages = 3;
 constexpr int kSplitThreads = 128;
-constexpr uint32_t kStageA = kTM * kTK * 2;  // 16 KB
-constexpr uint32_t kStageB = kTN * kTK * 2;  // 32 KB
-constexpr uint32_t kStageBytes = kStageA + kStageB;
+constexpr uint32_t kSliceA = kTM * kKB * 2;  // 8 KB
+constexpr uint32_t kSliceB = kTN * kKB * 2;  // 16 KB
+constexpr uint32_t kStageBytes = 3 * (kSliceA + kSliceB);  // 72 KB (three slices)
 constexpr uint32_t kTmemCols = 256;
 constexpr long long kWaitLimit = 1ll << 26;
 
@@ -78,15 +84,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
-// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
-// core-matrix groups 1024 bytes apart, descriptor version 1.
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+// tcgen05 shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row
+// core-matrix groups 512 bytes apart, descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3ffff) >> 4);  // start address
   d |= (uint64_t)1 << 16;                   // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)(512 >> 4) << 32;          // stride byte offset: 8 rows x 64 B
   d |= (uint64_t)1 << 46;                   // version
-  d |= (uint64_t)2 << 61;                   // swizzle: 128B
+  d |= (uint64_t)4 << 61;                   // swizzle: 64B
   return d;
 }
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
@@ -218,7 +224,7 @@ __global__ void split_b_kernel(int k, int n, const TI* __restrict__ B, int64_t l
 struct SplitArgs {
   int m, n, k;
   int mp, np, kp;
-  int npairs;
+  int npairs, slices;
   int pa[6], pb[6];  // slice pairs
   double alpha, beta;
   void* C;
@@ -232,14 +238,14 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                       const SplitArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-byte aligned stage ring (128-byte swizzle atoms)
+  // 1024-byte aligned stage ring (every slice tile starts on a 512-byte swizzle pattern)
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], acc_bar;
   __shared__ uint32_t tmem_base_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * kTN;
-  const int ktiles = g.kp / kTK;
-  const int iters = ktiles * g.npairs;
+  const int iters = (g.npairs > 0) ? g.kp / kKB : 0;  // k-blocks
+  const uint32_t stage_tx = (uint32_t)g.slices * (kSliceA + kSliceB);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -274,17 +280,16 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
     }
   }
   if (warp == 0 && lane == 0) {
-    // producer: TMA loads of (A slice tile, B slice tile) per iteration
+    // producer: TMA loads of every slice tile of A and B for k-block `it`
     for (int it = 0; it < iters; ++it) {
       const int s = it % kStages;
       const uint32_t ph = (uint32_t)(it / kStages) & 1u;
       if (!mbar_wait(&empty_bar[s], ph ^ 1u)) break;
-      const int pair = it / ktiles, kt = it - pair * ktiles;
       unsigned char* sa = smem + (size_t)s * kStageBytes;
-      unsigned char* sb = sa + kStageA;
-      mbar_expect_tx(&full_bar[s], kStageBytes);
-      tma_load_2d(sa, &mapA, kt * kTK, g.pa[pair] * g.mp + m0, &full_bar[s]);
-      tma_load_2d(sb, &mapB, kt * kTK, g.pb[pair] * g.np + n0, &full_bar[s]);
+      unsigned char* sb = sa + 3 * kSliceA;
+      mbar_expect_tx(&full_bar[s], stage_tx);
+      for (int p = 0; p < g.slices; ++p) tma_load_2d(sa + p * kSliceA, &mapA, it * kKB, p * g.mp + m0, &full_bar[s]);
+      for (int q = 0; q < g.slices; ++q) tma_load_2d(sb + q * kSliceB, &mapB, it * kKB, q * g.np + n0, &full_bar[s]);
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
@@ -297,11 +302,13 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t sa = smem_u32(smem + (size_t)s * kStageBytes);
-      const uint32_t sb = sa + kStageA;
+      const uint32_t sb = sa + 3 * kSliceA;
+      for (int pr = 0; pr < g.npairs; ++pr) {
+        const uint32_t ta = sa + (uint32_t)g.pa[pr] * kSliceA, tb = sb + (uint32_t)g.pb[pr] * kSliceB;
 #pragma unroll
-      for (int kk = 0; kk < kTK / 16; ++kk) {  // K = 16 per instruction: +32 bytes in the swizzled row
-        mma_bf16(tmem, smem_desc_sw128(sa + kk * 32), smem_desc_sw128(sb + kk * 32), idesc,
-                 (it > 0 || kk > 0) ? 1u : 0u);
+        for (int kk = 0; kk < kKB / 16; ++kk)  // K = 16 per instruction: +32 bytes in the swizzled row
+          mma_bf16(tmem, smem_desc_sw64(ta + kk * 32), smem_desc_sw64(tb + kk * 32), idesc,
+                   (it > 0 || pr > 0 || kk > 0) ? 1u : 0u);
       }
       mma_commit(&empty_bar[s]);  // stage free once these MMAs have read it
     }
@@ -371,10 +378,10 @@ int make_map(CUtensorMap* map, void* base, uint64_t rows, uint64_t kp, uint32_t 
   if (!f) return record_arg_error(-100, "split gemm: cuTensorMapEncodeTiled unavailable");
   const cuuint64_t dims[2] = {kp, rows};
   const cuuint64_t strides[1] = {kp * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)kTK, box_rows};
+  const cuuint32_t box[2] = {(cuuint32_t)kKB, box_rows};
   const cuuint32_t estr[2] = {1, 1};
   CUresult r = f(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return record_arg_error(-101, "split gemm: cuTensorMapEncodeTiled failed");
   return NACU_SUCCESS;
@@ -476,6 +483,7 @@ int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, 
       ++np_;
     }
   g.npairs = (k > 0) ? np_ : 0;
+  g.slices = slices;
   g.alpha = alpha;
   g.beta = beta;
   g.C = C;
