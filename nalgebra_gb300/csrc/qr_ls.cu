@@ -34,10 +34,10 @@ namespace {
 constexpr int kQrThreads = 128;
 constexpr int kQrNB = 8;
 constexpr int kQrMaxN = 64;
-// s_t layout: T (NB x NB) | tau (NB) | V^T V partials (4 warps x 32)
+// s_t layout: T (NB x NB) | tau (NB) | scratch (128) | V^T V strict upper part (28, padded to 32)
 constexpr int kTOff = 0;
 constexpr int kTauOff = kQrNB * kQrNB;
-constexpr int kGOff = kTauOff + kQrNB;            // 4 warps x 32 partials
+constexpr int kGOff = kTauOff + kQrNB;            // scratch (1 / |diag_i| of the back substitution)
 constexpr int kGSumOff = kGOff + 4 * 32;           // 28 reduced pairs (i < j)
 constexpr int kSTSize = kGSumOff + 32;
 
@@ -77,15 +77,18 @@ __device__ __forceinline__ void warp_reduce_scatter(double (&v)[N]) {
   for (int off = N; off < 32; off <<= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
 }
 
-__device__ __forceinline__ double block_sum(double v, double* red) {
+// CTA sum, valid in thread 0 only (the one thread that uses it: the other
+// threads add nothing, which saves the FP64 issue slots of 127 redundant sums).
+__device__ __forceinline__ double block_sum_to0(double v, double* red) {
   v = warp_sum(v);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
   double s = 0.0;
+  if (threadIdx.x == 0)
 #pragma unroll
-  for (int w = 0; w < kQrThreads / 32; ++w) s += red[w];
+    for (int w = 0; w < kQrThreads / 32; ++w) s += red[w];
   return s;
 }
 
@@ -117,7 +120,7 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
       double* pj = P + (size_t)j * ldp;
       double part = 0.0;
       for (int r = j + tid; r < rows; r += kQrThreads) part = fma(pj[r], pj[r], part);
-      const double sq = block_sum(part, s_red);
+      const double sq = block_sum_to0(part, s_red);
       if (tid == 0) {
         // householder.rs:19-53 (reflection_axis_mut) without the sign step
         const double nrm = sqrt(sq);
@@ -140,7 +143,9 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
       }
       __syncthreads();
       const double scale = s_misc[0], tau = s_misc[1];
-      // v = x * scale; dots of v with the remaining panel columns
+      // v = x * scale; dots of v with the remaining panel columns (c > j) and
+      // with the earlier reflection axes (c < j: the entries G[c][j] = v_c . v_j
+      // of V^T V that the T factor needs, v_j being zero above row j)
       double dots[kQrNB];
 #pragma unroll
       for (int c = 0; c < kQrNB; ++c) dots[c] = 0.0;
@@ -149,7 +154,7 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
         pj[r] = v;
 #pragma unroll
         for (int c = 0; c < kQrNB; ++c)
-          if (c > j && c < jb) dots[c] = fma(v, P[(size_t)c * ldp + r], dots[c]);
+          if (c != j && c < jb) dots[c] = fma(v, P[(size_t)c * ldp + r], dots[c]);
       }
       // reduce the dots (at most 7) across the CTA
       warp_reduce_scatter<kQrNB>(dots);
@@ -163,6 +168,7 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
 #pragma unroll
         for (int w = 0; w < kQrThreads / 32; ++w) d += s_red[4 + w * kQrNB + tid];
         s_coef[tid] = (tid > j && tid < jb) ? -tau * d : 0.0;
+        if (tid < j) s_t[kGSumOff + tid * kQrNB - tid * (tid + 1) / 2 + (j - tid - 1)] = d;  // G[tid][j]
       }
       __syncthreads();
       double coef[kQrNB];
@@ -177,36 +183,9 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
       __syncthreads();
     }
     // ---- T (forward, columnwise): T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] V^T v_j ----
-    // G = V^T V (strict upper part), V lower trapezoidal: v_j[r] = 0 for r < j.
+    // G = V^T V (strict upper part) was formed by the panel steps; thread 0
+    // runs the small T recurrence in shared memory.
     {
-      double gpart[32];  // the 28 pairs i < j, padded to 32 for the butterfly
-#pragma unroll
-      for (int k = 0; k < 32; ++k) gpart[k] = 0.0;
-      for (int r = tid; r < rows; r += kQrThreads) {
-        double v[kQrNB];
-#pragma unroll
-        for (int c = 0; c < kQrNB; ++c) v[c] = (c < jb && r >= c) ? P[(size_t)c * ldp + r] : 0.0;
-#pragma unroll
-        for (int i = 0; i < kQrNB; ++i)
-#pragma unroll
-          for (int j = i + 1; j < kQrNB; ++j) {
-            const int k = i * kQrNB - i * (i + 1) / 2 + (j - i - 1);
-            gpart[k] = fma(v[i], v[j], gpart[k]);
-          }
-      }
-      warp_reduce_scatter<32>(gpart);
-      double* gsh = s_t + kGOff;  // 28 partials per warp
-      gsh[warp * 32 + lane] = gpart[0];
-      __syncthreads();
-      // Reduce the 4 warps' partials into G (strict upper part), then thread 0
-      // runs the small T recurrence in shared memory.
-      if (tid < kQrNB * (kQrNB - 1) / 2) {
-        double acc = 0.0;
-#pragma unroll
-        for (int w = 0; w < kQrThreads / 32; ++w) acc += gsh[w * 32 + tid];
-        s_t[kGSumOff + tid] = acc;
-      }
-      __syncthreads();
       if (tid == 0) {
         for (int j = 0; j < kQrNB; ++j)
           for (int i = 0; i < kQrNB; ++i) s_t[kTOff + i * kQrNB + j] = 0.0;
