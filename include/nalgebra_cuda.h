@@ -279,7 +279,14 @@ size_t nacu_getrf_workspace_bytes(int n);
 /* LU with partial pivoting of one n x n matrix (column-major, lda), in place,
  * nalgebra's packed L\U with per-step pivots ipiv[0..n) (src/linalg/lu.rs:93-122;
  * icamax rule src/base/min_max.rs:221-240; a zero column is skipped,
- * lu.rs:107-110).  *info (device) = 0, or the first skipped column + 1. */
+ * lu.rs:107-110).  *info (device) = 0, or the first skipped column + 1.
+ * Look-ahead: the work forks from `stream` onto two internal streams of the
+ * library (per device; the panel chain at the highest stream priority, the
+ * bulk of each trailing update concurrently) and joins back before the call
+ * returns, so it is ordered like any work on `stream` and can be captured into
+ * a CUDA graph.  Calls that use the internal streams (this one,
+ * nacu_dgesv_mixed_ir) must not be issued concurrently from several host
+ * threads on one device. */
 int nacu_dgetrf(int n, double* A, int64_t lda, int32_t* ipiv, int32_t* info, void* workspace, size_t workspace_bytes,
                 nacu_stream_t stream);
 
@@ -304,7 +311,8 @@ size_t nacu_gesv_mixed_workspace_bytes(int n);
  * Synchronous: *iters_out, *berr_out, *fallback_out are host values.  No
  * reference counterpart (nalgebra has no mixed precision); it replaces
  * `m.lu().solve(&b)` (src/linalg/lu.rs:93-122, 221-260) when an FP64-accurate
- * solution, not the factor, is wanted. */
+ * solution, not the factor, is wanted.  The FP32 factorization forks onto the
+ * internal streams as nacu_dgetrf does. */
 int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, double* x, double tol_units,
                         int max_iter, int* iters_out, double* berr_out, int* fallback_out, void* workspace,
                         size_t workspace_bytes, nacu_stream_t stream);
