@@ -25,7 +25,7 @@
 namespace nacu {
 namespace {
 
-constexpr int kLuThreads = 128;
+constexpr int kLuThreads = 256;
 
 // Pivot of column c (icamax over rows c..n-1, one warp): s_piv[c] (c itself
 // for an all-zero column, which is skipped: lu.rs:107-110), and in s_rcp:
