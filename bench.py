@@ -269,14 +269,25 @@ def bench_ragged_ours(args, rank, world):
     a_pin.copy_(a0)
     b_pin.copy_(b0)
     e2e_steps = max(1, min(args.steps, 5))
+    # the mixed form from host memory: nacu_dposv_ragged_mixed_host pipelines
+    # the copies in, the solves and the copies out over chunks of the batch
+    it_pin = torch.empty(count, dtype=torch.int32, pin_memory=True)
+    ns_pin = torch.from_numpy(ns.astype(np.int32)).pin_memory()
+    aoff_pin = torch.from_numpy(aoff.astype(np.int64)).pin_memory()
+    boff_pin = torch.from_numpy(boff.astype(np.int64)).pin_memory()
+    n_max_all = int(ns.max())
+    host_ws = None
+    if use_mixed:
+        nbytes = L.nacu_mixed_host_workspace_bytes(count, n_max_all, ns_pin.data_ptr(), aoff_pin.data_ptr(),
+                                                   boff_pin.data_ptr(), nrhs, args.e2e_chunks)
+        host_ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
 
     def e2e_step():
-        if use_mixed:  # the mixed form reads A and B in place (read-only) and writes X
-            mchol.batch.data.copy_(a_pin, non_blocking=True)
-            mrhs.data.copy_(b_pin, non_blocking=True)
-            mchol.solve_refined_into(mrhs, mout)
-            x_pin.copy_(mout.data, non_blocking=True)
-            i_pin.copy_(mchol.info[:count], non_blocking=True)
+        if use_mixed:  # host arrays in, host solutions out (A and B read-only)
+            _lib.call("nacu_dposv_ragged_mixed_host", count, n_max_all, ns_pin.data_ptr(), aoff_pin.data_ptr(),
+                      a_pin.data_ptr(), nrhs, boff_pin.data_ptr(), b_pin.data_ptr(), x_pin.data_ptr(),
+                      i_pin.data_ptr(), it_pin.data_ptr(), args.e2e_chunks, host_ws.data_ptr(), host_ws.numel(),
+                      0.0, 0, 0.0, 0, int(stream.cuda_stream))
         else:
             A.copy_(a_pin, non_blocking=True)
             B.copy_(b_pin, non_blocking=True)
@@ -296,8 +307,8 @@ def bench_ragged_ours(args, rank, world):
     t1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = t0.elapsed_time(t1) / e2e_steps
-    h2d = (a0.numel() + b0.numel()) * 8
-    d2h = b0.numel() * 8 + count * (4 if use_mixed else 12)
+    h2d = (a0.numel() + b0.numel()) * 8 + (count * 20 if use_mixed else 0)
+    d2h = b0.numel() * 8 + count * (8 if use_mixed else 12)
 
     # one plain FP64 launch per matrix (nacu_dposv), on a sample, one stream
     plain_sample = rng.choice(count, size=min(1000, count), replace=False)
@@ -915,6 +926,8 @@ def main():
                     help="ragged_cholesky: re-run the tile autotuner before timing (not saved)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--count", type=int, default=0, help="ragged_cholesky: override the number of systems")
+    ap.add_argument("--e2e-chunks", type=int, default=8,
+                    help="ragged_cholesky e2e: chunks of the host-memory pipeline (copy in / solve / copy out)")
     ap.add_argument("--profile", action="store_true", help="timed kernel only (for ncu captures)")
     ap.add_argument("--profile-mixed", action="store_true", help="with --profile: also run the mixed-precision form")
     args = ap.parse_args()

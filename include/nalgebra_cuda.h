@@ -199,6 +199,28 @@ int nacu_dposv_ragged_mixed(int count, int n_max, const int32_t* ns, const int64
                             size_t workspace_bytes, double tol_units, int max_iter, double substitute, int flags,
                             nacu_stream_t stream);
 
+/* The same solve from host memory, pipelined: every array (ns, offsets, A,
+ * B, X, info, iters) is a host array in the layout of nacu_dposv_ragged_mixed,
+ * with non-decreasing offsets.  The batch is cut into `chunks` parts of about
+ * equal bytes (<= 0: 8; at most 64); while one part is solved on the GPU the
+ * next is copied in and the previous one copied out, on internal streams of
+ * the library forked from `stream` and joined back to it before the call
+ * returns (the results are in host memory once `stream` has been
+ * synchronized).  Page-locked host memory gives the overlap; pageable memory
+ * works but serializes the copies.  Each system's results are bit-identical to
+ * nacu_dposv_ragged_mixed's.  workspace: device memory of
+ * nacu_mixed_host_workspace_bytes bytes (same arguments), 256-byte aligned;
+ * calls must not be issued concurrently from several host threads on one
+ * device.  It is the form a host-resident caller uses in place of
+ * `m.cholesky()` + `.solve(&b)` per matrix (src/linalg/cholesky.rs:221-272,
+ * 122-143).  Returns 0 bytes for invalid arguments. */
+size_t nacu_mixed_host_workspace_bytes(int count, int n_max, const int32_t* ns, const int64_t* a_offsets,
+                                       const int64_t* b_offsets, int nrhs, int chunks);
+int nacu_dposv_ragged_mixed_host(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, const double* A,
+                                 int nrhs, const int64_t* b_offsets, const double* B, double* X, int32_t* info,
+                                 int32_t* iters, int chunks, void* workspace, size_t workspace_bytes,
+                                 double tol_units, int max_iter, double substitute, int flags, nacu_stream_t stream);
+
 /* ---- Adjoint of the Cholesky solve and log-determinant (batched, n <= 128) - */
 
 /* Forward: for `batch` SPD matrices A + s*strideA (lower triangle read),

@@ -46,6 +46,9 @@ SIGNATURES = {
     "nacu_mixed_workspace_bytes": (_sz, [_i, _i64]),
     "nacu_dposv_ragged_mixed": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _sz, _d, _i,
                                      _d, _i, _vp]),
+    "nacu_mixed_host_workspace_bytes": (_sz, [_i, _i, _vp, _vp, _vp, _i, _i]),
+    "nacu_dposv_ragged_mixed_host": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp, _sz, _d, _i,
+                                          _d, _i, _vp]),
     "nacu_dposv_logdet_forward": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "nacu_sposv_logdet_forward": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "nacu_dposv_logdet_backward": (_i, [_i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),

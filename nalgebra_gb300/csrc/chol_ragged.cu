@@ -348,6 +348,24 @@ int chol_launch_ragged(CholArgs g, int flags, cudaStream_t s, const char* name) 
 
 }  // namespace
 
+size_t ragged_order_scratch_bytes() { return kWsOrder; }
+
+int ragged_order_desc(int count, int n_max, const int32_t* ns, int32_t* order, void* scratch, cudaStream_t s,
+                      const char* name) {
+  if (count <= 0) return NACU_SUCCESS;
+  unsigned char* ws = static_cast<unsigned char*>(scratch);
+  int32_t* heads = reinterpret_cast<int32_t*>(ws);
+  int32_t* ranges = reinterpret_cast<int32_t*>(ws + kWsRanges);
+  int32_t* hist = reinterpret_cast<int32_t*>(ws + kWsHist);
+  cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)(NACU_CHOL_RAGGED_MAX_N + 2) * 4, s);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  const int blocks = std::min(sm_count() * 4, (count + 255) / 256);
+  ragged_hist_kernel<<<blocks, 256, 0, s>>>(count, n_max, ns, hist);
+  ragged_scan_kernel<<<1, 32, 0, s>>>(count, n_max, hist, ranges, heads);
+  ragged_scatter_kernel<<<blocks, 256, 0, s>>>(count, n_max, ns, hist, order);
+  return check_launch(name);
+}
+
 // Equal-order batch (system s at A + s*strideA, B + s*strideB), one CTA per
 // system, factor + solve + log-determinant in place with the tuned tile of
 // the order's size bucket (used by the adjoint's forward pass).

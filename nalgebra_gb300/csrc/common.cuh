@@ -17,6 +17,13 @@ int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, 
 int chol_uniform_posv(int n, double* A, int64_t strideA, int nrhs, double* B, int64_t strideB, int32_t* info,
                       double* logdet, int batch, cudaStream_t s, const char* name);
 
+// Processing order of a ragged batch, largest order first (a counting sort
+// over n = 0..n_max on the device; chol_ragged.cu).  scratch: at least
+// ragged_order_scratch_bytes() bytes, 256-byte aligned.
+size_t ragged_order_scratch_bytes();
+int ragged_order_desc(int count, int n_max, const int32_t* ns, int32_t* order, void* scratch, cudaStream_t s,
+                      const char* name);
+
 // Records a CUDA error (from a launch or a runtime call) for nacu_last_error().
 int record_cuda_error(cudaError_t e, const char* where);
 // Records an argument error message; returns `code`.

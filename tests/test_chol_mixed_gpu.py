@@ -154,3 +154,45 @@ def test_extreme_scales_stay_correct(cuda, scale):
         b = b_flat[boff[s]:boff[s] + 2 * n].reshape(2, n).T
         assert np.all(np.isfinite(x))
         assert O.backward_error(m, x, b) <= n * EPS64, (scale, s, iters[s])
+
+
+@pytest.mark.parametrize("chunks,pinned", [(3, True), (7, False), (1, True)])
+def test_host_pipeline_matches_device_call(cuda, chunks, pinned):
+    """nacu_dposv_ragged_mixed_host (host arrays, chunked copy-in / solve /
+    copy-out on internal streams) gives every system the device call's
+    results bit for bit, pinned or pageable host memory."""
+    torch = cuda
+    w = W.ragged_spd(300, 8, 256, nrhs=4, seed=21)
+    ns, aoff, boff = w["ns"], w["a_offsets"], w["b_offsets"]
+    A0, B0, X0, info0, it0, _, _ = _mixed(cuda, ns, w["a_flat"], w["b_flat"], 4)
+
+    def host(x):
+        t = torch.from_numpy(np.ascontiguousarray(x))
+        return t.pin_memory() if pinned else t
+
+    hns, haoff, hboff = host(ns.astype(np.int32)), host(aoff.astype(np.int64)), host(boff.astype(np.int64))
+    hA, hB = host(w["a_flat"]), host(w["b_flat"])
+    hX = host(np.full(w["b_flat"].size, np.nan))
+    hinfo = host(np.full(ns.size, -7, dtype=np.int32))
+    hit = host(np.zeros(ns.size, dtype=np.int32))
+    L = _lib.load()
+    nbytes = L.nacu_mixed_host_workspace_bytes(ns.size, int(ns.max()), hns.data_ptr(), haoff.data_ptr(),
+                                               hboff.data_ptr(), 4, chunks)
+    assert nbytes > 0
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    _lib.call("nacu_dposv_ragged_mixed_host", ns.size, int(ns.max()), hns.data_ptr(), haoff.data_ptr(), hA.data_ptr(),
+              4, hboff.data_ptr(), hB.data_ptr(), hX.data_ptr(), hinfo.data_ptr(), hit.data_ptr(), chunks,
+              ws.data_ptr(), ws.numel(), 0.0, 0, 0.0, 0, stream.cuda_stream)
+    stream.synchronize()
+    assert np.array_equal(hinfo.numpy(), info0) and np.array_equal(hit.numpy(), it0)
+    assert np.array_equal(hX.numpy().view(np.uint64), X0.view(np.uint64))
+    assert np.array_equal(hA.numpy(), w["a_flat"]) and np.array_equal(hB.numpy(), w["b_flat"])
+
+
+def test_host_pipeline_rejects_unordered_offsets(cuda):
+    L = _lib.load()
+    ns = np.array([4, 4], dtype=np.int32)
+    aoff = np.array([16, 0], dtype=np.int64)  # decreasing
+    boff = np.array([0, 4], dtype=np.int64)
+    assert L.nacu_mixed_host_workspace_bytes(2, 4, ns.ctypes.data, aoff.ctypes.data, boff.ctypes.data, 1, 2) == 0
