@@ -34,7 +34,7 @@ from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 
 __all__ = [
     "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch", "solve_refined", "gemm",
-    "PosvLogdet",
+    "PosvLogdet", "cholesky_solve_refined_host",
     "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE",
 ]
 
@@ -193,6 +193,47 @@ def solve_refined(a: DeviceMatrix, b: DeviceMatrix, tol_units: float = 1.0, max_
               float(tol_units), int(max_iter), C.byref(it), C.byref(berr), C.byref(fb), ws.data_ptr(), ws.numel(),
               _stream_ptr())
     return x, {"iters": it.value, "berr": berr.value, "fallback": bool(fb.value)}
+
+
+def cholesky_solve_refined_host(ns, a_offsets, a, b_offsets, b, nrhs: int, chunks: int = 8, tol_units: float = 1.0,
+                                max_iter: int = 0):
+    """The ragged precision-form SPD solve from host memory (no nalgebra
+    counterpart; it replaces `m.cholesky()` + `.solve(&b)` per matrix,
+    src/linalg/cholesky.rs:221-272, 122-143): ``a`` and ``b`` are host arrays in
+    the packed ragged layout (matrix s at a[a_offsets[s]:], ns[s] x ns[s]
+    column-major; its nrhs right-hand sides at b[b_offsets[s]:]).  The copies in
+    and out are pipelined with the solves over ``chunks`` parts
+    (nacu_dposv_ragged_mixed_host); page-locked host memory (torch tensors
+    with pin_memory) gives the overlap.  Returns (x, info, iters) as host
+    arrays, x in the layout of b."""
+    torch = _torch()
+
+    def host(v, dtype):
+        if isinstance(v, torch.Tensor):
+            return v.contiguous()
+        return torch.from_numpy(np.ascontiguousarray(v, dtype=dtype))
+
+    hns, haoff, hboff = host(ns, np.int32), host(a_offsets, np.int64), host(b_offsets, np.int64)
+    ha, hb = host(a, np.float64), host(b, np.float64)
+    count = int(hns.numel())
+    pinned = bool(ha.is_pinned())
+    hx = torch.empty(hb.numel(), dtype=torch.float64, pin_memory=pinned)
+    hinfo = torch.empty(count, dtype=torch.int32, pin_memory=pinned)
+    hit = torch.empty(count, dtype=torch.int32, pin_memory=pinned)
+    n_max = int(hns.max()) if count else 0
+    L = _lib.load()
+    nbytes = L.nacu_mixed_host_workspace_bytes(count, n_max, hns.data_ptr(), haoff.data_ptr(), hboff.data_ptr(),
+                                               int(nrhs), int(chunks))
+    if count and nbytes == 0:
+        raise NacuError("cholesky_solve_refined_host: invalid layout (orders or offsets)")
+    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    _lib.call("nacu_dposv_ragged_mixed_host", count, n_max, hns.data_ptr(), haoff.data_ptr(), ha.data_ptr(),
+              int(nrhs), hboff.data_ptr(), hb.data_ptr(), hx.data_ptr(), hinfo.data_ptr(), hit.data_ptr(),
+              int(chunks), ws.data_ptr(), ws.numel(), float(tol_units), int(max_iter), 0.0, 0,
+              int(stream.cuda_stream))
+    stream.synchronize()
+    return hx.numpy(), hinfo.numpy(), hit.numpy()
 
 
 def gemm(c: DeviceMatrix, alpha: float, a: DeviceMatrix, b: DeviceMatrix, beta: float, split_slices: int = 0):

@@ -196,3 +196,20 @@ def test_host_pipeline_rejects_unordered_offsets(cuda):
     aoff = np.array([16, 0], dtype=np.int64)  # decreasing
     boff = np.array([0, 4], dtype=np.int64)
     assert L.nacu_mixed_host_workspace_bytes(2, 4, ns.ctypes.data, aoff.ctypes.data, boff.ctypes.data, 1, 2) == 0
+
+
+def test_mirror_host_solve(cuda):
+    """cholesky_solve_refined_host (the mirror of the host-memory entry point)
+    meets the FP64 backward-error target on a workload slice."""
+    from nalgebra_gb300 import cholesky_solve_refined_host
+    w = W.ragged_spd(120, 8, 200, nrhs=2, seed=31)
+    ns = w["ns"]
+    x, info, iters = cholesky_solve_refined_host(ns, w["a_offsets"], w["a_flat"], w["b_offsets"], w["b_flat"], 2,
+                                                 chunks=4)
+    assert np.all(info == 0) and np.all(iters != 0)
+    for s in range(0, ns.size, 7):
+        n = int(ns[s])
+        a = w["a_flat"][w["a_offsets"][s]:w["a_offsets"][s] + n * n].reshape(n, n).T
+        xs = x[w["b_offsets"][s]:w["b_offsets"][s] + 2 * n].reshape(2, n).T
+        bs = w["b_flat"][w["b_offsets"][s]:w["b_offsets"][s] + 2 * n].reshape(2, n).T
+        assert O.backward_error(a, xs, bs) <= n * EPS64
