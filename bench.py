@@ -598,6 +598,80 @@ def bench_lu_ours(args, rank, world):
             "gpu_launches": args.steps, "clocks": clk.summary()}
 
 
+def bench_lu_inverse_ours(args, rank, world):
+    """Batched `m.try_inverse()` for n > 4 (src/linalg/inverse.rs:135-137 ->
+    lu.rs:266-297): nacu_dgetrf_batched then nacu_dgetri_batched on 4096
+    64x64 f64 systems per step; work counted as nalgebra's 2/3 n^3 (factor)
+    + 2 n^3 (n solves with the identity) flops per inverse."""
+    import time
+
+    import torch
+
+    import oracle as O
+    from nalgebra_gb300 import _lib
+    from nalgebra_gb300 import workloads as W
+
+    L = _lib.load()
+    count, n = 4096, 64
+    a, _ = W.dense_lu(count, n, 1, seed=rank)
+    a0 = torch.from_numpy(a).cuda().reshape(-1)
+    A = a0.clone()
+    inv = torch.empty(count * n * n, dtype=torch.float64, device="cuda")
+    ipiv = torch.zeros(count * n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    flags = 1 if args.exact else 0
+
+    def launch():
+        _lib.call("nacu_dgetrf_batched", n, A.data_ptr(), n * n, ipiv.data_ptr(), info.data_ptr(), count, flags, sp)
+        _lib.call("nacu_dgetri_batched", n, A.data_ptr(), n * n, ipiv.data_ptr(), inv.data_ptr(), n * n,
+                  info.data_ptr(), count, flags, sp)
+
+    for _ in range(args.warmup):
+        A.copy_(a0); launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            A.copy_(a0); flush.zero_()
+            ev[i][0].record(stream)
+            launch()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+    assert int((info != 0).sum().item()) == 0
+    # accuracy on a sample: A * inv(A) - I
+    worst = 0.0
+    for s in range(0, count, 512):
+        m = a[s].reshape(n, n).T
+        x = inv[s * n * n:(s + 1) * n * n].cpu().numpy().reshape(n, n).T
+        worst = max(worst, float(np.abs(m @ x - np.eye(n)).max()))
+    flops = count * (2.0 / 3 * n ** 3 + 2.0 * n ** 3)
+    peak = ctypes_probe(L)
+    res = {"metric": "inverses/s (batched LU factor + try_inverse, 4096 x 64x64 f64)", "value": count / (ms * 1e-3),
+           "unit": "inverses/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "lu_inverse", "count": count, "n": n, "exact": bool(args.exact),
+                      "l2": "256 MB flush between steps"},
+           "gflops": flops / (ms * 1e-3) / 1e9, "max_abs_A_Ainv_minus_I_sample": worst,
+           "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak / 1e12,
+                        "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / peak, "traffic": None,
+                        "peak_source": fp64_peak_source()},
+           "gpu_launches": args.steps * (2 + (n + 15) // 16), "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = 256
+        t0 = time.perf_counter()
+        for s in range(sample):
+            lu_, piv, _ = O.lu(a[s].reshape(n, n).T)
+            O.lu_try_inverse(lu_, piv)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": sample / dt, "unit": "inverses/s", "cores": 1, "kind": "port",
+                               "sample": f"{sample} of the {count} systems, oracle LU::new + try_inverse, one thread"}
+    return res
+
+
 # ----------------------------------------------------------------------------- QR least squares
 
 def bench_ls_ours(args, rank, world):
@@ -917,7 +991,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
-                                                                  "mixed_lu"])
+                                                                  "mixed_lu", "lu_inverse"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--single-launch", action="store_true",
                     help="ragged_cholesky: one launch over a host-sorted order with the default tile "
@@ -953,9 +1027,10 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
-    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu"):
+    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse"):
         res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
-               "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours}[args.workload](args, rank, world)
+               "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours,
+               "lu_inverse": bench_lu_inverse_ours}[args.workload](args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

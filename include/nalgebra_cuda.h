@@ -98,6 +98,16 @@ int nacu_dgetrf_batched(int n, double* A, int64_t strideA, int32_t* ipiv, int32_
 int nacu_dgetrs_batched(int n, int nrhs, double* LU, int64_t strideA, int32_t* ipiv, double* B,
                         int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
 
+/* Inverse from getrf factors: `lu.try_inverse()` (src/linalg/lu.rs:266-297:
+ * out = I, then solve_mut(out)), and with nacu_dgetrf_batched before it
+ * `m.try_inverse()` for n > 4 (src/linalg/inverse.rs:135-137).  Ainv + s*strideInv
+ * (n x n) receives the inverse; LU and ipiv are read only.  info[s] = first
+ * zero U_kk + 1 (nalgebra's None; Ainv then holds garbage, as nalgebra's
+ * `out` may), or 0.  NACU_FLAG_EXACT: bit-identical to nalgebra's
+ * solve_mut on the identity. */
+int nacu_dgetri_batched(int n, const double* LU, int64_t strideA, const int32_t* ipiv, double* Ainv,
+                        int64_t strideInv, int32_t* info, int batch, int flags, nacu_stream_t stream);
+
 /* Fused factor + solve in one launch: `m.lu()` then `.solve(&b)`
  * (src/linalg/decomposition.rs:48-54, src/linalg/lu.rs:221-236). */
 int nacu_dgesv_batched(int n, int nrhs, double* A, int64_t strideA, int32_t* ipiv, double* B,

@@ -20,6 +20,8 @@
 // separately rounded multiply and add, true division in the back solve), so
 // factors, pivots and solutions are bit-identical to nalgebra's CPU results.
 // EXACT = false contracts each update to one FMA (half the FP64 issue slots).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace nacu {
@@ -283,6 +285,16 @@ int lu_launch(int n, int nrhs, T* A, int64_t strideA, int32_t* ipiv, T* B, int64
   return check_launch(name);
 }
 
+// X_s = I for every system (the right-hand sides of the inverse).
+__global__ void identity_batched_kernel(int n, double* X, int64_t stride, int batch) {
+  const int64_t nn = (int64_t)n * n, total = nn * batch;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t sys = e / nn, rem = e - sys * nn;
+    const int c = (int)(rem / n), r = (int)(rem - (int64_t)c * n);
+    X[sys * stride + rem] = (r == c) ? 1.0 : 0.0;
+  }
+}
+
 }  // namespace
 }  // namespace nacu
 
@@ -300,6 +312,31 @@ int nacu_dgetrs_batched(int n, int nrhs, double* LU, int64_t strideA, int32_t* i
                         int32_t* info, int batch, int flags, nacu_stream_t stream) {
   return lu_launch<double>(n, nrhs, LU, strideA, ipiv, B, strideB, info, batch, 2, flags, (cudaStream_t)stream,
                            "nacu_dgetrs_batched");
+}
+
+// LU::try_inverse (src/linalg/lu.rs:266-297): out = I, then solve_mut(out),
+// NACU_LU_BATCHED_MAX_NRHS columns of the identity per solve launch.
+int nacu_dgetri_batched(int n, const double* LU, int64_t strideA, const int32_t* ipiv, double* Ainv,
+                        int64_t strideInv, int32_t* info, int batch, int flags, nacu_stream_t stream) {
+  using namespace nacu;
+  const char* name = "nacu_dgetri_batched";
+  if (n < 0 || n > NACU_LU_BATCHED_MAX_N) return record_arg_error(-1, "getri batched: n out of range [0, 128]");
+  if (batch < 0) return record_arg_error(-8, "getri batched: negative batch");
+  if (batch == 0 || n == 0) return NACU_SUCCESS;
+  if (!LU || !ipiv || !Ainv || !info) return record_arg_error(-2, "getri batched: null LU, ipiv, Ainv or info");
+  if (strideA < (int64_t)n * n) return record_arg_error(-3, "getri batched: strideA < n*n");
+  if (strideInv < (int64_t)n * n) return record_arg_error(-6, "getri batched: strideInv < n*n");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t total = (int64_t)n * n * batch;
+  const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 8);
+  identity_batched_kernel<<<grid, 256, 0, s>>>(n, Ainv, strideInv, batch);
+  int rc = check_launch(name);
+  for (int c0 = 0; c0 < n && rc == NACU_SUCCESS; c0 += NACU_LU_BATCHED_MAX_NRHS) {
+    const int nr = std::min(NACU_LU_BATCHED_MAX_NRHS, n - c0);
+    rc = lu_launch<double>(n, nr, const_cast<double*>(LU), strideA, const_cast<int32_t*>(ipiv), Ainv + (size_t)c0 * n,
+                           strideInv, info, batch, 2, flags, s, name);
+  }
+  return rc;
 }
 
 int nacu_dgesv_batched(int n, int nrhs, double* A, int64_t strideA, int32_t* ipiv, double* B, int64_t strideB,

@@ -121,6 +121,13 @@ def lu_solve(lu_, ipiv, b):
     return x if ok else None
 
 
+def lu_try_inverse(lu_, ipiv):
+    """LU::try_inverse (src/linalg/lu.rs:266-297): the identity, then
+    LU::solve_mut on it (lu.rs:242-260); None when some U_ii == 0."""
+    n = np.asarray(lu_).shape[0]
+    return lu_solve(lu_, ipiv, np.eye(n))
+
+
 def lu_determinant(lu_, length) -> float:
     lu_ = _f64(lu_)
     return lib().orc_dlu_determinant(lu_.shape[0], _p(lu_), max(lu_.shape[0], 1), length)

@@ -160,3 +160,62 @@ def test_device_batch_lazy_fused(cuda):
     assert np.array_equal(lub.pivots(), ipiv_o)
     x2 = lub.solve(rhs)  # second solve uses the stored factors
     assert np.array_equal(np.stack([xx.T.ravel() for xx in x2.to_numpy()]), x_o)
+
+
+def _getri(cuda, a_colmaj, n, flags=0):
+    torch = cuda
+    batch = a_colmaj.shape[0]
+    A = torch.from_numpy(np.ascontiguousarray(a_colmaj)).cuda()
+    inv = torch.full((batch, n * n), np.nan, dtype=torch.float64, device="cuda")
+    ipiv = torch.full((batch * max(n, 1),), -7, dtype=torch.int32, device="cuda")
+    info = torch.full((batch,), -7, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    _lib.call("nacu_dgetrf_batched", n, A.data_ptr(), n * n, ipiv.data_ptr(), info.data_ptr(), batch, flags, s)
+    _lib.call("nacu_dgetri_batched", n, A.data_ptr(), n * n, ipiv.data_ptr(), inv.data_ptr(), n * n, info.data_ptr(),
+              batch, flags, s)
+    torch.cuda.synchronize()
+    return inv.cpu().numpy(), info.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [5, 17, 33, 64, 100, 128])
+def test_try_inverse_exact_bit_identical_to_oracle(cuda, n):
+    """nacu_dgetri_batched (LU::try_inverse, lu.rs:266-297) in EXACT form
+    equals the oracle's identity-then-solve_mut bit for bit."""
+    rng = np.random.default_rng(300 + n)
+    mats = [rng.standard_normal((n, n)) + (float(n) if k % 2 else 0.0) * np.eye(n) for k in range(3)]
+    inv, info = _getri(cuda, np.stack([m.ravel(order="F") for m in mats]), n, FLAG_EXACT)
+    assert np.all(info == 0)
+    for k, m in enumerate(mats):
+        lu, ipiv, _ = O.lu(m)
+        ref = O.lu_try_inverse(lu, ipiv)
+        assert np.array_equal(inv[k].reshape(n, n).T, ref), (n, k)
+
+
+def test_try_inverse_known_answer_and_singular(cuda):
+    """tests/linalg/inverse.rs:62-81 (relative 1e-4) through the GPU path, in
+    the FMA form; a singular matrix reports info (nalgebra's None)."""
+    import json
+    with open(os.path.join(os.path.dirname(__file__), "golden", "reference_known_answers.json")) as f:
+        k = json.load(f)["inverse_matrix5"]
+    m = np.array(k["rows"], dtype=np.float64)
+    sing = np.array([[1.0, 2.0, 3.0, 0.0, 1.0], [2.0, 4.0, 6.0, 0.0, 2.0], [0.0, 1.0, 1.0, 1.0, 0.0],
+                     [1.0, 0.0, 2.0, 3.0, 1.0], [0.0, 0.0, 1.0, 1.0, 1.0]])
+    sing[:, 3] = 0.0  # an exactly zero column: skipped by the LU (lu.rs:107-110), U_33 = 0
+    inv, info = _getri(cuda, np.stack([m.ravel(order="F"), sing.ravel(order="F")]), 5)
+    exp = np.array(k["expected_inverse_rows"])
+    got = inv[0].reshape(5, 5).T
+    d = np.abs(got - exp)
+    assert np.all((d <= np.finfo(np.float64).eps) | (d <= k["max_relative"] * np.maximum(np.abs(got), np.abs(exp))))
+    assert info[0] == 0 and info[1] > 0
+
+
+def test_try_inverse_fma_workload(cuda):
+    """The 64 x 64 workload matrices: A Ainv = I to 1e-12 relative (FMA form)."""
+    n = 64
+    a, _ = W.dense_lu(16, n, 1, seed=9)
+    inv, info = _getri(cuda, a, n)
+    assert np.all(info == 0)
+    for k in range(16):
+        m = a[k].reshape(n, n).T
+        r = m @ inv[k].reshape(n, n).T - np.eye(n)
+        assert np.abs(r).max() <= 1e-12 * n, k

@@ -237,3 +237,33 @@ def test_golden_fixtures_reproduce():
                 assert np.allclose(got, ref, rtol=1e-14, atol=0), key
             else:
                 assert np.array_equal(got, ref, equal_nan=True), key
+
+
+def _relative_eq(a, b, max_relative, epsilon=np.finfo(np.float64).eps):
+    """approx's relative_eq per entry: equal, or |a-b| <= epsilon (absolute,
+    f64::EPSILON by default), or |a-b| <= max_relative * max(|a|, |b|)."""
+    a, b = np.asarray(a), np.asarray(b)
+    d = np.abs(a - b)
+    return bool(np.all((a == b) | (d <= epsilon) | (d <= max_relative * np.maximum(np.abs(a), np.abs(b)))))
+
+
+def test_try_inverse_known_answers():
+    """tests/linalg/inverse.rs:62-81 and 126-142 (the n = 5 Gaussian-elimination
+    inverse, lu::try_invert_to), restated through the oracle's LU::try_inverse."""
+    k = _known()["inverse_matrix5"]
+    m = _rows(k["rows"])
+    lu, ipiv, _ = O.lu(m)
+    inv = O.lu_try_inverse(lu, ipiv)
+    exp = _rows(k["expected_inverse_rows"])
+    assert _relative_eq(inv, exp, k["max_relative"])
+    k = _known()["inverse_matrix5_scaled_identity"]
+    m = k["diagonal"] * np.eye(k["n"])
+    lu, ipiv, _ = O.lu(m)
+    inv = O.lu_try_inverse(lu, ipiv)
+    assert _relative_eq(inv, k["expected_inverse_diagonal"] * np.eye(k["n"]), k["max_relative"])
+
+
+def test_try_inverse_singular_is_none():
+    a = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [0.0, 1.0, 1.0]])
+    lu, ipiv, _ = O.lu(a)
+    assert O.lu_try_inverse(lu, ipiv) is None
