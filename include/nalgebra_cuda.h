@@ -108,6 +108,20 @@ int nacu_dgetrs_batched(int n, int nrhs, double* LU, int64_t strideA, int32_t* i
 int nacu_dgetri_batched(int n, const double* LU, int64_t strideA, const int32_t* ipiv, double* Ainv,
                         int64_t strideInv, int32_t* info, int batch, int flags, nacu_stream_t stream);
 
+/* Batched triangular solves (n <= 128): B + s*strideB (n x nrhs) <- T_s^-1 B
+ * (trans = 0) or T_s^-T B (trans = 1), T_s = T + s*strideT lower (upper = 0)
+ * or upper (upper = 1) triangular, only that triangle read.  Replaces
+ * Matrix::solve_{lower,upper}_triangular_mut (src/linalg/solve.rs:55-101,
+ * 137-181), tr_solve_*_mut and ad_solve_*_mut (:233-283, 325-372; the same for
+ * real scalars, dot form :374-442).  has_diag = 1 (lower, trans = 0 only):
+ * solve_lower_triangular_with_diag_mut (:106-134), the diagonal never read,
+ * `diag` assumed.  info[s] (nullable) = 1-based index of the zero diagonal
+ * that stops the solve (nalgebra's false; B then holds partial results), or
+ * 0.  NACU_FLAG_EXACT: bit-identical to nalgebra's arithmetic. */
+int nacu_dtrsv_batched(int n, int nrhs, int upper, int trans, int has_diag, double diag, const double* T,
+                       int64_t strideT, double* B, int64_t strideB, int32_t* info, int batch, int flags,
+                       nacu_stream_t stream);
+
 /* Fused factor + solve in one launch: `m.lu()` then `.solve(&b)`
  * (src/linalg/decomposition.rs:48-54, src/linalg/lu.rs:221-236). */
 int nacu_dgesv_batched(int n, int nrhs, double* A, int64_t strideA, int32_t* ipiv, double* B,

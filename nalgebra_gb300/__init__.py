@@ -167,6 +167,19 @@ class LU:
     def is_invertible(self) -> bool:
         return int(self.info[0].item()) == 0
 
+    def try_inverse(self):
+        """LU::try_inverse (src/linalg/lu.rs:266-297): the inverse as a new
+        DeviceMatrix, or None when some U_ii == 0 (n <= 128)."""
+        n = self.lu.nrows
+        if self.large:
+            raise NotImplementedError("try_inverse: n <= 128 (the batched kernels)")
+        torch = _torch()
+        out = DeviceMatrix(torch.empty(n * n, dtype=torch.float64, device="cuda"), n, n)
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _lib.call("nacu_dgetri_batched", n, self.lu.data.data_ptr(), n * n, self.ipiv.data_ptr(), out.data.data_ptr(),
+                  n * n, info.data_ptr(), 1, self.flags, _stream_ptr())
+        return out if int(info.item()) == 0 else None
+
     def l(self) -> np.ndarray:
         lu = self.lu.to_numpy()
         return np.tril(lu, -1) + np.eye(lu.shape[0])
@@ -388,6 +401,20 @@ class LUBatch:
         res = b.clone_owned()
         self.solve_mut(res)
         return res
+
+    def try_inverse(self):
+        """LU::try_inverse (src/linalg/lu.rs:266-297) of every matrix: returns
+        (inverses as a DeviceBatch, device info: 0 = invertible, k = U_kk == 0,
+        nalgebra's None)."""
+        torch = _torch()
+        self.factor()
+        n, cnt = self.n, len(self.batch)
+        data = torch.empty(cnt * n * n, dtype=torch.float64, device="cuda")
+        info = torch.zeros(cnt, dtype=torch.int32, device="cuda")
+        _lib.call("nacu_dgetri_batched", n, self.batch.data.data_ptr(), n * n, self.ipiv.data_ptr(), data.data_ptr(),
+                  n * n, info.data_ptr(), cnt, self.flags, _stream_ptr())
+        nn = np.full(cnt, n, dtype=np.int32)
+        return DeviceBatch(data, nn, nn, np.arange(cnt, dtype=np.int64) * n * n), info
 
     def pivots(self) -> np.ndarray:
         self.factor()

@@ -51,6 +51,7 @@ def lib():
             "orc_sgetrf": (_i64, [_i64, _i64, _fp, _i64, _i32p]),
             "orc_dgetrs": (C.c_int, [_i64, _dp, _i64, _i32p, _dp, _i64, _i64]),
             "orc_dlu_determinant": (C.c_double, [_i64, _dp, _i64, _i64]),
+            "orc_dtrsv": (C.c_int, [_i64, _dp, _i64, _dp, _i64, _i64, C.c_int, C.c_int, C.c_int, C.c_double]),
             "orc_dpotrf": (C.c_int, [_i64, _dp, _i64, C.c_int, C.c_double]),
             "orc_spotrf": (C.c_int, [_i64, _fp, _i64, C.c_int, C.c_float]),
             "orc_dpotrs": (None, [_i64, _dp, _i64, _dp, _i64, _i64]),
@@ -118,6 +119,19 @@ def lu_solve(lu_, ipiv, b):
     x2 = x.reshape(n, -1, order="F")
     ok = lib().orc_dgetrs(n, _p(lu_), max(n, 1), _p(np.ascontiguousarray(ipiv, dtype=np.int32), _i32p),
                           _p(x2), max(n, 1), x2.shape[1])
+    return x if ok else None
+
+
+def triangular_solve(t, b, upper=False, trans=False, diag=None):
+    """Matrix::{solve,tr_solve}_{lower,upper}_triangular_mut and
+    solve_lower_triangular_with_diag_mut (src/linalg/solve.rs:55-442) on a copy
+    of b; returns x, or None at a zero diagonal (nalgebra's false)."""
+    t = _f64(t)
+    n = t.shape[0]
+    x = np.array(b, dtype=np.float64, order="F", copy=True)
+    x2 = x.reshape(n, -1, order="F")
+    ok = lib().orc_dtrsv(n, _p(t), max(n, 1), _p(x2), max(n, 1), x2.shape[1], int(upper), int(trans),
+                         int(diag is not None), float(diag if diag is not None else 0.0))
     return x if ok else None
 
 

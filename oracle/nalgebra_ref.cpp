@@ -67,6 +67,14 @@ int orc_dqr_ls_solve(int64_t m, int64_t n, const double* qr, int64_t lda, const 
   return orc::qr_ls_solve<double>(m, n, qr, lda, diag, b, ldb, x, ldx, nrhs);
 }
 
+// Triangular solve of b (n x nrhs) by t (solve.rs:55-442): uplo 0 lower / 1
+// upper, trans 0 / 1 (tr_ and ad_ forms), has_diag (lower only): the
+// with_diag form.  1 = solved, 0 = a zero diagonal (nalgebra's false).
+int orc_dtrsv(int64_t n, const double* t, int64_t lda, double* b, int64_t ldb, int64_t nrhs, int uplo, int trans,
+              int has_diag, double diag) {
+  return orc::triangular_solve<double>(n, t, lda, b, ldb, nrhs, uplo != 0, trans != 0, has_diag != 0, diag) ? 1 : 0;
+}
+
 // ---- batched drivers (the CPU baseline) -----------------------------------
 // `batch` dense n x n systems packed back to back (stride n*n), one n x nrhs
 // right-hand side each (stride n*nrhs).  Factor in place, solve in place.

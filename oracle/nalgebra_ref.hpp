@@ -203,6 +203,67 @@ inline bool lu_solve(std::size_t n, const T* lu, std::size_t lda, const int32_t*
   return true;
 }
 
+// Triangular solves of Matrix (src/linalg/solve.rs), one column of b at a time
+// (the `_mut` forms loop over the columns, returning false at the first zero
+// diagonal; the columns after a failing one are left as they are).
+// lower = solve_lower_triangular_vector_mut (solve.rs:74-101): axpy form.
+// upper = solve_upper_triangular_vector_mut (solve.rs:156-181).
+// tr lower = xx_solve_lower_triangular_vector_mut (solve.rs:374-407): dot
+//   form, i descending; tr upper = xx_solve_upper_triangular_vector_mut
+//   (solve.rs:409-442), i ascending (ad_ = tr_ for real scalars).
+// with_diag = solve_lower_triangular_with_diag_mut (solve.rs:106-134): the
+//   diagonal is never read; b_i itself is not rewritten (i < n-1 only).
+template <class T>
+inline bool triangular_solve(std::size_t n, const T* t, std::size_t lda, T* b, std::size_t ldb, std::size_t nrhs,
+                             bool upper, bool trans, bool has_diag, T diag) {
+  if (has_diag) {
+    if (diag == T(0)) return false;
+    for (std::size_t c = 0; c < nrhs; ++c) {
+      T* bc = b + c * ldb;
+      for (std::size_t i = 0; i + 1 < n; ++i) {
+        const T coeff = bc[i] / diag;
+        axpy(n - i - 1, -coeff, t + (i + 1) + i * lda, T(1), bc + i + 1);
+      }
+    }
+    return true;
+  }
+  for (std::size_t c = 0; c < nrhs; ++c) {
+    T* bc = b + c * ldb;
+    if (!upper && !trans) {
+      for (std::size_t i = 0; i < n; ++i) {
+        const T d = t[i + i * lda];
+        if (d == T(0)) return false;
+        const T coeff = bc[i] / d;
+        bc[i] = coeff;
+        axpy(n - i - 1, -coeff, t + (i + 1) + i * lda, T(1), bc + i + 1);
+      }
+    } else if (upper && !trans) {
+      for (std::size_t i = n; i-- > 0;) {
+        const T d = t[i + i * lda];
+        if (d == T(0)) return false;
+        const T coeff = bc[i] / d;
+        bc[i] = coeff;
+        axpy(i, -coeff, t + i * lda, T(1), bc);
+      }
+    } else if (!upper && trans) {
+      for (std::size_t i = n; i-- > 0;) {
+        const T dt = dot(n - i - 1, t + (i + 1) + i * lda, bc + i + 1);
+        const T d = t[i + i * lda];
+        if (d == T(0)) return false;
+        bc[i] = (bc[i] - dt) / d;
+      }
+    } else {
+      for (std::size_t i = 0; i < n; ++i) {
+        const T dt = dot(i, t + i * lda, bc);
+        const T d = t[i + i * lda];
+        if (d == T(0)) return false;
+        bc[i] = (bc[i] - dt) / d;
+      }
+    }
+  }
+  return true;
+}
+
 // LU::determinant (lu.rs:301-314): product of the diagonal times the sign of
 // the permutation (permutation_sequence.rs:158-164).
 template <class T>

@@ -219,3 +219,19 @@ def test_try_inverse_fma_workload(cuda):
         m = a[k].reshape(n, n).T
         r = m @ inv[k].reshape(n, n).T - np.eye(n)
         assert np.abs(r).max() <= 1e-12 * n, k
+
+
+def test_mirror_try_inverse(cuda):
+    """LU.try_inverse / LUBatch.try_inverse in the mirror."""
+    rng = np.random.default_rng(77)
+    m = rng.standard_normal((20, 20)) + 20 * np.eye(20)
+    inv = DeviceMatrix.from_numpy(m).lu().try_inverse()
+    assert inv is not None and np.abs(m @ inv.to_numpy() - np.eye(20)).max() < 1e-12
+    z = m.copy()
+    z[:, 5] = 0.0
+    assert DeviceMatrix.from_numpy(z).lu().try_inverse() is None
+    mats = [rng.standard_normal((9, 9)) + 9 * np.eye(9) for _ in range(5)]
+    invs, info = DeviceBatch.from_numpy(mats).lu().try_inverse()
+    assert np.all(info.cpu().numpy() == 0)
+    for a, x in zip(mats, invs.to_numpy()):
+        assert np.abs(a @ x - np.eye(9)).max() < 1e-12

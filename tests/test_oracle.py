@@ -267,3 +267,22 @@ def test_try_inverse_singular_is_none():
     a = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [0.0, 1.0, 1.0]])
     lu, ipiv, _ = O.lu(a)
     assert O.lu_try_inverse(lu, ipiv) is None
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_triangular_solve_properties(seed):
+    """tests/linalg/solve.rs:20-60: 4x4 matrices with near-zero diagonals set to
+    1 (unzero_diagonal), 4x5 right-hand sides, tri * x == b to 1e-7 for the
+    lower / upper / tr_ forms."""
+    rng = np.random.default_rng(500 + seed)
+    a = rng.uniform(-1, 1, size=(4, 4))
+    d = np.diag(a).copy()
+    d[np.abs(d) < 1e-7] = 1.0
+    a[np.arange(4), np.arange(4)] = d
+    b = rng.uniform(-1, 1, size=(4, 5))
+    for upper, trans in ((False, False), (True, False), (False, True), (True, True)):
+        tri = np.triu(a) if upper else np.tril(a)
+        x = O.triangular_solve(a, b, upper=upper, trans=trans)
+        assert np.allclose((tri.T if trans else tri) @ x, b, atol=1e-7, rtol=0)
+    x = O.triangular_solve(a, b, diag=1.0)
+    assert np.allclose((np.tril(a, -1) + np.eye(4)) @ x, b, atol=1e-7, rtol=0)
