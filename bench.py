@@ -672,6 +672,91 @@ def bench_lu_inverse_ours(args, rank, world):
     return res
 
 
+def bench_trsv_ours(args, rank, world):
+    """Batched triangular solves at the reference's solve benchmark shape
+    (benches/linalg/solve.rs: 100x100, one vector): 4096 systems per step for
+    solve_lower_triangular (the headline form), solve_upper_triangular and
+    tr_solve_lower_triangular (nacu_dtrsv_batched).  Entries U[0, 1) as
+    DMatrix::new_random, plus n on the diagonal so the solutions stay finite.
+    HBM roofline: the triangle (n(n+1)/2 doubles) read, b read and written."""
+    import time
+
+    import torch
+
+    import oracle as O
+    from nalgebra_gb300 import _lib
+
+    count, n = 4096, 100
+    rng = np.random.default_rng(rank)
+    t = rng.random((count, n, n)) + n * np.eye(n)
+    b = rng.random((count, n))
+    T = torch.from_numpy(np.ascontiguousarray(np.transpose(t, (0, 2, 1))).reshape(count, n * n)).cuda()
+    b0 = torch.from_numpy(b).cuda()
+    B = b0.clone()
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    flags = 1 if args.exact else 0
+    forms = {}
+    for name, upper, trans in (("solve_lower_triangular", 0, 0), ("solve_upper_triangular", 1, 0),
+                               ("tr_solve_lower_triangular", 0, 1)):
+        def launch():
+            _lib.call("nacu_dtrsv_batched", n, 1, upper, trans, 0, 0.0, T.data_ptr(), n * n, B.data_ptr(), n,
+                      info.data_ptr(), count, flags, sp)
+        for _ in range(args.warmup):
+            B.copy_(b0); launch()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            for i in range(args.steps):
+                B.copy_(b0); flush.zero_()
+                ev[i][0].record(stream)
+                launch()
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()
+        ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+        x = B.cpu().numpy()
+        errs = []
+        for s in range(0, count, 512):
+            tri = np.triu(t[s]) if upper else np.tril(t[s])
+            m = tri.T if trans else tri
+            errs.append(float(np.abs(m @ x[s] - b[s]).max() / np.abs(b[s]).max()))
+        forms[name] = {"ms": ms, "solves_per_s": count / (ms * 1e-3), "max_rel_residual_sample": max(errs),
+                       "clocks": clk.summary()}
+    head = forms["solve_lower_triangular"]
+    bytes_per = (n * (n + 1) / 2 + 2 * n) * 8
+    flops_per = float(n * n)  # n(n-1)/2 multiply-adds and n divisions
+    peaks = read_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6794.8)) if peaks else 6794.8
+    L = _lib.load()
+    fp64 = ctypes_probe(L)
+    achieved = count * flops_per / (head["ms"] * 1e-3)
+    res = {"metric": "solves/s (batched solve_lower_triangular, 4096 x 100x100 f64, one vector)",
+           "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (U[0,1) entries, n added on the diagonal)",
+           "config": {"workload": "trsv_batched", "count": count, "n": n, "nrhs": 1, "exact": bool(args.exact),
+                      "l2": "256 MB flush between steps"},
+           "forms": forms,
+           "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": fp64 / 1e12, "unit": "TFLOP/s",
+                        "frac": achieved / fp64, "traffic": None, "peak_source": fp64_peak_source(),
+                        "note": ("n^2 flops per solve; at 2 flops per 8 bytes the FP64 pipe binds before HBM "
+                                 "(%.2f of the measured HBM rate)" % (count * bytes_per / (head["ms"] * 1e-3)
+                                                                       / (hbm * 1e9)))},
+           "gpu_launches": 3 * args.steps, "clocks": head["clocks"]}
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = 1000
+        t0 = time.perf_counter()
+        for s in range(sample):
+            O.triangular_solve(t[s], b[s])
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": sample / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                               "sample": f"{sample} of the {count} systems, oracle solve_lower_triangular, one thread "
+                                         "(includes the ctypes call per system)"}
+    return res
+
+
 # ----------------------------------------------------------------------------- QR least squares
 
 def bench_ls_ours(args, rank, world):
@@ -991,7 +1076,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
-                                                                  "mixed_lu", "lu_inverse"])
+                                                                  "mixed_lu", "lu_inverse", "trsv_batched"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--single-launch", action="store_true",
                     help="ragged_cholesky: one launch over a host-sorted order with the default tile "
@@ -1027,10 +1112,10 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
-    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse"):
+    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse", "trsv_batched"):
         res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
                "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours,
-               "lu_inverse": bench_lu_inverse_ours}[args.workload](args, rank, world)
+               "lu_inverse": bench_lu_inverse_ours, "trsv_batched": bench_trsv_ours}[args.workload](args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

@@ -13,9 +13,12 @@
 //   transposed forms: b_i = (b_i - dot) / T_ii with the dot of Matrix::dotx
 //     (src/base/blas.rs:96-165): eight accumulators over blocks of 8, combined
 //     (a0+a4), (a1+a5), (a2+a6), (a3+a7), then the tail one product at a time.
-// EXACT (NACU_FLAG_EXACT) rounds every product and sum separately, as Rust
-// does (bit-identical results); the default form contracts to FMA and uses a
-// warp reduction for the dots.
+// EXACT (NACU_FLAG_EXACT) rounds every product and sum separately and divides
+// at every step, as Rust does (bit-identical results); the default form
+// contracts to FMA, uses a warp reduction for the dots and multiplies by the
+// reciprocals of the diagonal, formed 32 at a time before the sweep: on this
+// part an FP64 instruction costs the same pipe time whether one lane or 32 run
+// it, and a division is a chain of them.
 #include <algorithm>
 
 #include "common.cuh"
@@ -67,6 +70,7 @@ __device__ __forceinline__ double warp_dot(int len, const double* x, const doubl
 template <bool EXACT>
 __global__ void __launch_bounds__(kTrsvBWarps * 32) trsv_batched_kernel(TrsvBArgs g) {
   __shared__ double xs_all[kTrsvBWarps][kTrsvBMaxN];
+  __shared__ double rd_all[kTrsvBWarps][kTrsvBMaxN];  // FMA form: 1 / T_ii
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t pair = (int64_t)blockIdx.x * kTrsvBWarps + warp;
   const int n = g.n;
@@ -75,7 +79,10 @@ __global__ void __launch_bounds__(kTrsvBWarps * 32) trsv_batched_kernel(TrsvBArg
   const double* t = g.T + (size_t)s * g.strideT;
   double* bcol = g.B + (size_t)s * g.strideB + (size_t)c * n;
   double* xs = xs_all[warp];
+  double* rd = rd_all[warp];
   for (int j = lane; j < n; j += 32) xs[j] = bcol[j];
+  if (!EXACT && !g.has_diag)  // the n divisions at once, 32 lanes per FP64 warp instruction
+    for (int j = lane; j < n; j += 32) rd[j] = 1.0 / t[(size_t)j * n + j];
   __syncwarp();
   int fail = 0;  // 1-based index of the zero diagonal that stops the solve
   if (g.has_diag) {  // solve_lower_triangular_with_diag_mut: b_i is not rewritten
@@ -99,7 +106,7 @@ __global__ void __launch_bounds__(kTrsvBWarps * 32) trsv_batched_kernel(TrsvBArg
       }
       double coeff = 0.0;
       if (lane == 0) {
-        coeff = xs[i] / d;
+        coeff = EXACT ? xs[i] / d : xs[i] * rd[i];
         xs[i] = coeff;
       }
       coeff = __shfl_sync(0xffffffffu, coeff, 0);
@@ -119,7 +126,7 @@ __global__ void __launch_bounds__(kTrsvBWarps * 32) trsv_batched_kernel(TrsvBArg
         fail = i + 1;
         break;
       }
-      if (lane == 0) xs[i] = EXACT ? __ddiv_rn(__dsub_rn(xs[i], dt), d) : (xs[i] - dt) / d;
+      if (lane == 0) xs[i] = EXACT ? __ddiv_rn(__dsub_rn(xs[i], dt), d) : (xs[i] - dt) * rd[i];
       __syncwarp();
     }
   }
