@@ -93,6 +93,59 @@ class DeviceMatrix:
         return DeviceMatrix(self.data.clone(), self.nrows, self.ncols)
 
     # -- factorizations (consume self: the buffer is factored in place) --------
+    def _trsv(self, b: "DeviceMatrix", upper: bool, trans: bool, diag=None, flags: int = 0) -> bool:
+        """nacu_dtrsv_batched on one matrix (n <= 128): b is overwritten."""
+        torch = _torch()
+        n = self.nrows
+        assert self.is_square() and b.nrows == n, "triangular solve dimension mismatch"
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _lib.call("nacu_dtrsv_batched", n, b.ncols, int(upper), int(trans), int(diag is not None),
+                  float(diag if diag is not None else 0.0), self.data.data_ptr(), n * n, b.data.data_ptr(),
+                  n * b.ncols, info.data_ptr(), 1, flags, _stream_ptr())
+        return int(info.item()) == 0
+
+    def solve_lower_triangular_mut(self, b: "DeviceMatrix", flags: int = 0) -> bool:
+        """Matrix::solve_lower_triangular_mut (src/linalg/solve.rs:55-101)."""
+        return self._trsv(b, False, False, None, flags)
+
+    def solve_upper_triangular_mut(self, b: "DeviceMatrix", flags: int = 0) -> bool:
+        """Matrix::solve_upper_triangular_mut (src/linalg/solve.rs:137-181)."""
+        return self._trsv(b, True, False, None, flags)
+
+    def tr_solve_lower_triangular_mut(self, b: "DeviceMatrix", flags: int = 0) -> bool:
+        """Matrix::tr_solve_lower_triangular_mut (src/linalg/solve.rs:233-256); ad_ is the same for f64."""
+        return self._trsv(b, False, True, None, flags)
+
+    def tr_solve_upper_triangular_mut(self, b: "DeviceMatrix", flags: int = 0) -> bool:
+        """Matrix::tr_solve_upper_triangular_mut (src/linalg/solve.rs:258-283)."""
+        return self._trsv(b, True, True, None, flags)
+
+    def solve_lower_triangular_with_diag_mut(self, b: "DeviceMatrix", diag: float, flags: int = 0) -> bool:
+        """Matrix::solve_lower_triangular_with_diag_mut (src/linalg/solve.rs:106-134)."""
+        return self._trsv(b, False, False, float(diag), flags)
+
+    def solve_lower_triangular(self, b: "DeviceMatrix", flags: int = 0):
+        """Matrix::solve_lower_triangular (solve.rs:15-34): a new matrix, or None."""
+        res = b.clone_owned()
+        return res if self.solve_lower_triangular_mut(res, flags) else None
+
+    def solve_upper_triangular(self, b: "DeviceMatrix", flags: int = 0):
+        res = b.clone_owned()
+        return res if self.solve_upper_triangular_mut(res, flags) else None
+
+    def tr_solve_lower_triangular(self, b: "DeviceMatrix", flags: int = 0):
+        res = b.clone_owned()
+        return res if self.tr_solve_lower_triangular_mut(res, flags) else None
+
+    def tr_solve_upper_triangular(self, b: "DeviceMatrix", flags: int = 0):
+        res = b.clone_owned()
+        return res if self.tr_solve_upper_triangular_mut(res, flags) else None
+
+    ad_solve_lower_triangular = tr_solve_lower_triangular
+    ad_solve_upper_triangular = tr_solve_upper_triangular
+    ad_solve_lower_triangular_mut = tr_solve_lower_triangular_mut
+    ad_solve_upper_triangular_mut = tr_solve_upper_triangular_mut
+
     def lu(self, flags: int = 0) -> "LU":
         """Matrix::lu (src/linalg/decomposition.rs:48-54).  flags apply to the
         batched kernel (n <= 128)."""

@@ -73,3 +73,19 @@ def test_zero_diagonal_reports_the_stopping_index(cuda, upper, trans):
     first = 31 if (upper != trans) else 17  # the sweep order: descending for upper / tr-lower
     assert info[0] == 0 and info[1] == first + 1
     assert O.triangular_solve(ts[1], bs[1], upper=upper, trans=trans) is None
+
+
+def test_mirror_methods(cuda):
+    """DeviceMatrix.{solve,tr_solve,ad_solve}_{lower,upper}_triangular: the
+    oracle's results bit for bit in the EXACT form; None at a zero diagonal."""
+    from nalgebra_gb300 import DeviceMatrix
+    ts, bs = _mats(50, 1, 2, 9)
+    t, b = ts[0], bs[0]
+    m = DeviceMatrix.from_numpy(t)
+    for meth, upper, trans in (("solve_lower_triangular", False, False), ("solve_upper_triangular", True, False),
+                               ("tr_solve_lower_triangular", False, True), ("ad_solve_upper_triangular", True, True)):
+        x = getattr(m, meth)(DeviceMatrix.from_numpy(b), FLAG_EXACT)
+        assert np.array_equal(x.to_numpy(), O.triangular_solve(t, b, upper=upper, trans=trans)), meth
+    z = t.copy()
+    z[10, 10] = 0.0
+    assert DeviceMatrix.from_numpy(z).solve_lower_triangular(DeviceMatrix.from_numpy(b)) is None
