@@ -197,6 +197,30 @@ int nacu_dpotrs_ragged(int count, int n_max, const int32_t* ns, const int64_t* a
 int nacu_dposv(int n, double* A, int nrhs, double* B, int32_t* info, double* logdet, double substitute,
                int flags, nacu_stream_t stream);
 
+/* ---- Cholesky factor updates (batched, n <= 128) ---------------------------- */
+
+/* Cholesky::rank_one_update (src/linalg/cholesky.rs:277-285, 410-449): the
+ * factor L_s = L + s*strideL (n x n, lower part) becomes the factor of
+ * L_s L_s^T + sigma[s] x_s x_s^T, in place; X + s*strideX (n values) is read
+ * only (nalgebra updates a clone).  sigma: device array of batch values. */
+int nacu_dchol_rank1_update_batched(int n, double* L, int64_t strideL, const double* X, int64_t strideX,
+                                    const double* sigma, int batch, int flags, nacu_stream_t stream);
+
+/* Cholesky::remove_column (src/linalg/cholesky.rs:365-399): Lout_s
+ * ((n-1) x (n-1)) = the factor of A_s without row and column j, from L_s (its
+ * strict upper part copied block by block, as nalgebra copies its views). */
+int nacu_dchol_remove_column_batched(int n, const double* L, int64_t strideL, int j, double* Lout, int64_t strideOut,
+                                     int batch, int flags, nacu_stream_t stream);
+
+/* Cholesky::insert_column (src/linalg/cholesky.rs:287-357): Lout_s
+ * ((n+1) x (n+1)) = the factor of A_s with col_s (n+1 values, col + s*strideCol)
+ * inserted as row and column j (n <= 127).  info[s] (nullable) = 1 where the
+ * lower solve of the new row meets a zero diagonal (nalgebra's assertion),
+ * else 0. */
+int nacu_dchol_insert_column_batched(int n, const double* L, int64_t strideL, int j, const double* col,
+                                     int64_t strideCol, double* Lout, int64_t strideOut, int32_t* info, int batch,
+                                     int flags, nacu_stream_t stream);
+
 /* ---- Cholesky, mixed precision (FP32 factor, FP64 refinement) ------------- */
 
 /* Workspace bytes of nacu_dposv_ragged_mixed: queue heads and a fallback

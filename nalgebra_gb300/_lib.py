@@ -43,6 +43,9 @@ SIGNATURES = {
     "nacu_dpotrs_ragged": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_dgetri_batched": (_i, [_i, _vp, _i64, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dtrsv_batched": (_i, [_i, _i, _i, _i, _i, _d, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_dchol_rank1_update_batched": (_i, [_i, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_dchol_remove_column_batched": (_i, [_i, _vp, _i64, _i, _vp, _i64, _i, _i, _vp]),
+    "nacu_dchol_insert_column_batched": (_i, [_i, _vp, _i64, _i, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dposv": (_i, [_i, _vp, _i, _vp, _vp, _vp, _d, _i, _vp]),
     "nacu_dposv_ragged_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _d, _i, _vp]),
     "nacu_mixed_workspace_bytes": (_sz, [_i, _i64]),

@@ -52,6 +52,9 @@ def lib():
             "orc_dgetrs": (C.c_int, [_i64, _dp, _i64, _i32p, _dp, _i64, _i64]),
             "orc_dlu_determinant": (C.c_double, [_i64, _dp, _i64, _i64]),
             "orc_dtrsv": (C.c_int, [_i64, _dp, _i64, _dp, _i64, _i64, C.c_int, C.c_int, C.c_int, C.c_double]),
+            "orc_dchol_rank1": (None, [_i64, _dp, _i64, _dp, C.c_double]),
+            "orc_dchol_remove_column": (None, [_i64, _dp, _i64, _i64, _dp, _i64]),
+            "orc_dchol_insert_column": (C.c_int, [_i64, _dp, _i64, _i64, _dp, _dp, _i64]),
             "orc_dpotrf": (C.c_int, [_i64, _dp, _i64, C.c_int, C.c_double]),
             "orc_spotrf": (C.c_int, [_i64, _fp, _i64, C.c_int, C.c_float]),
             "orc_dpotrs": (None, [_i64, _dp, _i64, _dp, _i64, _i64]),
@@ -120,6 +123,36 @@ def lu_solve(lu_, ipiv, b):
     ok = lib().orc_dgetrs(n, _p(lu_), max(n, 1), _p(np.ascontiguousarray(ipiv, dtype=np.int32), _i32p),
                           _p(x2), max(n, 1), x2.shape[1])
     return x if ok else None
+
+
+def cholesky_rank_one_update(l, x, sigma):
+    """Cholesky::rank_one_update (src/linalg/cholesky.rs:277-285, 410-449) on a
+    copy of the factor l (n x n, lower part used); returns the new factor."""
+    out = np.array(l, dtype=np.float64, order="F", copy=True)
+    xv = np.array(x, dtype=np.float64, copy=True)
+    n = out.shape[0]
+    lib().orc_dchol_rank1(n, _p(out), max(n, 1), _p(xv), float(sigma))
+    return out
+
+
+def cholesky_remove_column(l, j):
+    """Cholesky::remove_column (src/linalg/cholesky.rs:365-399)."""
+    l = _f64(l)
+    n = l.shape[0]
+    out = np.zeros((n - 1, n - 1), order="F")
+    lib().orc_dchol_remove_column(n, _p(l), max(n, 1), j, _p(out), max(n - 1, 1))
+    return out
+
+
+def cholesky_insert_column(l, j, col):
+    """Cholesky::insert_column (src/linalg/cholesky.rs:287-357); None when
+    nalgebra's lower solve assertion would fail."""
+    l = _f64(l)
+    n = l.shape[0]
+    out = np.zeros((n + 1, n + 1), order="F")
+    c = np.ascontiguousarray(col, dtype=np.float64)
+    ok = lib().orc_dchol_insert_column(n, _p(l), max(n, 1), j, _p(c), _p(out), n + 1)
+    return out if ok else None
 
 
 def triangular_solve(t, b, upper=False, trans=False, diag=None):

@@ -75,6 +75,20 @@ int orc_dtrsv(int64_t n, const double* t, int64_t lda, double* b, int64_t ldb, i
   return orc::triangular_solve<double>(n, t, lda, b, ldb, nrhs, uplo != 0, trans != 0, has_diag != 0, diag) ? 1 : 0;
 }
 
+// Cholesky updates (cholesky.rs:277-449): the rank-one update in place (x is
+// overwritten), remove_column into out ((n-1)^2), insert_column into out
+// ((n+1)^2; 0 when the lower solve fails).
+void orc_dchol_rank1(int64_t n, double* l, int64_t lda, double* x, double sigma) {
+  orc::chol_rank_one_update<double>(n, l, lda, x, sigma);
+}
+void orc_dchol_remove_column(int64_t n, const double* l, int64_t lda, int64_t j, double* out, int64_t ldo) {
+  orc::chol_remove_column<double>(n, l, lda, j, out, ldo);
+}
+int orc_dchol_insert_column(int64_t n, const double* l, int64_t lda, int64_t j, const double* col, double* out,
+                            int64_t ldo) {
+  return orc::chol_insert_column<double>(n, l, lda, j, col, out, ldo) ? 1 : 0;
+}
+
 // ---- batched drivers (the CPU baseline) -----------------------------------
 // `batch` dense n x n systems packed back to back (stride n*n), one n x nrhs
 // right-hand side each (stride n*nrhs).  Factor in place, solve in place.

@@ -14,6 +14,7 @@
 // element (r, c) of an nrows x ncols matrix at a[r + c * lda].
 #pragma once
 #include <cmath>
+#include <vector>
 #include <cstddef>
 #include <cstdint>
 
@@ -321,6 +322,81 @@ inline void cholesky_solve(std::size_t n, const T* l, std::size_t lda, T* b, std
       bc[ii] = (bc[ii] - d) / l[ii + ii * lda];
     }
   }
+}
+
+// Cholesky::xx_rank_one_update (cholesky.rs:410-449): L (n x n, lower part)
+// becomes the factor of L L^T + sigma x x^T; x is overwritten (nalgebra works
+// on a clone of the caller's vector).  Operation order as in Rust, no FMA.
+template <class T>
+inline void chol_rank_one_update(std::size_t n, T* l, std::size_t lda, T* x, T sigma) {
+  T beta = T(1);
+  for (std::size_t j = 0; j < n; ++j) {
+    const T diag = l[j + j * lda];
+    const T diag2 = diag * diag;
+    const T xj = x[j];
+    const T sigma_xj2 = sigma * (xj * xj);
+    const T gamma = diag2 * beta + sigma_xj2;
+    const T new_diag = std::sqrt(diag2 + sigma_xj2 / beta);
+    l[j + j * lda] = new_diag;
+    beta += sigma_xj2 / diag2;
+    T* col = l + (j + 1) + j * lda;
+    T* xp = x + j + 1;
+    axpy(n - j - 1, -xj / diag, col, T(1), xp);  // x[j+1..] += (-xj / diag) L[j+1.., j]
+    if (gamma != T(0)) axpy(n - j - 1, new_diag * sigma / gamma * xj, xp, new_diag / diag, col);
+  }
+}
+
+// Cholesky::remove_column (cholesky.rs:365-399): out ((n-1) x (n-1), ldo) is
+// L without row and column j (the strict upper part copied block by block, as
+// nalgebra copies its views), then the rank-one update of the bottom-right
+// corner by L[j+1.., j] with sigma = 1.
+template <class T>
+inline void chol_remove_column(std::size_t n, const T* l, std::size_t lda, std::size_t j, T* out, std::size_t ldo) {
+  for (std::size_t c = 0; c + 1 < n; ++c)
+    for (std::size_t r = 0; r + 1 < n; ++r)
+      out[r + c * ldo] = l[(r < j ? r : r + 1) + (c < j ? c : c + 1) * lda];
+  std::vector<T> w(l + (j + 1) + j * lda, l + n + j * lda);
+  chol_rank_one_update<T>(n - 1 - j, out + j + j * ldo, ldo, w.data(), T(1));
+}
+
+// Cholesky::insert_column (cholesky.rs:287-357): out ((n+1) x (n+1), ldo)
+// holds L with an empty row and column j, then row j from the lower solve of
+// the top-left corner with col[..j], the centre sqrt(col[j] - |row j|^2), the
+// new column (col[j+1..] - bottom-left L[j.., ..j] row_j) / centre through
+// gemv's axcpy order (blas_uninit.rs:127-176), and the rank-one downdate of the
+// bottom-right corner by that column.  False when the lower solve fails
+// (nalgebra's assert).
+template <class T>
+inline bool chol_insert_column(std::size_t n, const T* l, std::size_t lda, std::size_t j, const T* col, T* out,
+                               std::size_t ldo) {
+  const std::size_t m = n + 1;
+  for (std::size_t c = 0; c < m; ++c)
+    for (std::size_t r = 0; r < m; ++r) {
+      if (r == j || c == j) out[r + c * ldo] = T(0);
+      else out[r + c * ldo] = l[(r < j ? r : r - 1) + (c < j ? c : c - 1) * lda];
+    }
+  std::vector<T> row(col, col + j);             // new_rowj_adjoint
+  std::vector<T> ncol(col + j + 1, col + m);    // new_colj
+  if (!triangular_solve<T>(j, l, lda, row.data(), j, 1, false, false, false, T(0))) return false;
+  for (std::size_t k = 0; k < j; ++k) out[j + k * ldo] = row[k];
+  const T center = std::sqrt(col[j] - dot(j, row.data(), row.data()));
+  out[j + j * ldo] = center;
+  // new_colj.gemm(-1/center, L[j.., ..j], row, 1/center), one output column: gemv
+  const T alpha = -T(1) / center, beta = T(1) / center;
+  const std::size_t len = n - j;
+  if (j == 0) {
+    for (std::size_t r = 0; r < len; ++r) ncol[r] *= beta;
+  } else {
+    for (std::size_t k = 0; k < j; ++k) {
+      const T* lc = l + j + k * lda;  // column k of the bottom-left corner
+      const T val = row[k];
+      const T b = (k == 0) ? beta : T(1);
+      for (std::size_t r = 0; r < len; ++r) ncol[r] = alpha * lc[r] * val + b * ncol[r];
+    }
+  }
+  for (std::size_t r = 0; r < len; ++r) out[(j + 1 + r) + j * ldo] = ncol[r];
+  chol_rank_one_update<T>(len, out + (j + 1) + (j + 1) * ldo, ldo, ncol.data(), T(-1));
+  return true;
 }
 
 // Cholesky::ln_determinant (cholesky.rs:172-185): sum of ln(L_ii * L_ii).
