@@ -757,6 +757,110 @@ def bench_trsv_ours(args, rank, world):
     return res
 
 
+def bench_chol_update_ours(args, rank, world):
+    """Batched Cholesky::rank_one_update (cholesky.rs:277-285, 410-449) on 4096
+    factors of order 128 per step (sigma = 1), with remove_column and
+    insert_column (j = 64) timed beside it.  Work: 2 n^2 flops per update (two
+    multiply-adds on each of the n^2/2 entries below the diagonal); FP64
+    roofline."""
+    import time
+
+    import torch
+
+    import oracle as O
+    from nalgebra_gb300 import _lib
+
+    L_ = _lib.load()
+    count, n, j = 4096, 128, 64
+    rng = np.random.default_rng(rank)
+    b = rng.standard_normal((16, n, n))
+    base = []
+    for k in range(16):
+        l, _ = O.cholesky(b[k] @ b[k].T + n * np.eye(n))
+        base.append(np.asfortranarray(l).ravel(order="F"))
+    facs = np.stack([base[k % 16] for k in range(count)])
+    L0 = torch.from_numpy(facs).cuda()
+    Lw = L0.clone()
+    X = torch.from_numpy(rng.standard_normal((count, n))).cuda()
+    S = torch.ones(count, dtype=torch.float64, device="cuda")
+    # insert_column puts an n-th row and column back into the order n-1 factors
+    # that remove_column writes; A's eigenvalues are >= n, so col[j] above
+    # |col|^2 + n keeps the new diagonal positive.
+    cols = rng.standard_normal((count, n))
+    cols[:, j] = (cols * cols).sum(axis=1) + n + 1.0
+    C = torch.from_numpy(cols).cuda()
+    out_rm = torch.empty((count, (n - 1) ** 2), dtype=torch.float64, device="cuda")
+    out_in = torch.empty((count, n * n), dtype=torch.float64, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    flags = 1 if args.exact else 0
+    calls = {
+        "rank_one_update": lambda: _lib.call("nacu_dchol_rank1_update_batched", n, Lw.data_ptr(), n * n, X.data_ptr(), n,
+                                             S.data_ptr(), count, flags, sp),
+        "remove_column": lambda: _lib.call("nacu_dchol_remove_column_batched", n, L0.data_ptr(), n * n, j,
+                                           out_rm.data_ptr(), (n - 1) ** 2, count, flags, sp),
+        "insert_column": lambda: _lib.call("nacu_dchol_insert_column_batched", n - 1, out_rm.data_ptr(), (n - 1) ** 2,
+                                           j, C.data_ptr(), n, out_in.data_ptr(), n * n, info.data_ptr(),
+                                           count, flags, sp),
+    }
+    calls["remove_column"]()  # the inputs of insert_column
+    torch.cuda.synchronize()
+    forms = {}
+    for name, fn in calls.items():
+        for _ in range(args.warmup):
+            Lw.copy_(L0); fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            for i in range(args.steps):
+                Lw.copy_(L0); flush.zero_()
+                ev[i][0].record(stream)
+                fn()
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()
+        ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+        forms[name] = {"ms": ms, "updates_per_s": count / (ms * 1e-3), "clocks": clk.summary()}
+    # accuracy on a sample of the rank-one updates
+    Lw.copy_(L0); calls["rank_one_update"](); torch.cuda.synchronize()
+    g = Lw.cpu().numpy()
+    worst = 0.0
+    for s in range(0, count, 1024):
+        lo = np.tril(g[s].reshape(n, n).T)
+        x = X[s].cpu().numpy()
+        a = base[s % 16].reshape(n, n).T
+        a = np.tril(a) @ np.tril(a).T + np.outer(x, x)
+        worst = max(worst, float(np.abs(lo @ lo.T - a).max() / np.abs(a).max()))
+    head = forms["rank_one_update"]
+    flops = count * 4.0 * n * n / 2
+    peak = ctypes_probe(L_)
+    res = {"metric": "updates/s (batched Cholesky::rank_one_update, 4096 factors of order 128, f64)",
+           "value": head["updates_per_s"], "unit": "updates/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (factors of B B^T + n I, x ~ N(0,1), sigma = 1)",
+           "config": {"workload": "chol_update", "count": count, "n": n, "j": j, "exact": bool(args.exact),
+                      "l2": "256 MB flush between steps"},
+           "forms": forms, "max_rel_error_sample": worst,
+           "roofline": {"bound": "fp64", "achieved": flops / (head["ms"] * 1e-3) / 1e12, "peak": peak / 1e12,
+                        "unit": "TFLOP/s", "frac": flops / (head["ms"] * 1e-3) / peak, "traffic": None,
+                        "peak_source": fp64_peak_source(),
+                        "note": "2 n^2 flops per update (two multiply-adds per entry below the diagonal, three FP64 "
+                                "instructions); the per-column scalar chain (a square root and a reciprocal after the "
+                                "diagonal's reciprocals are formed in bulk) runs in one lane of each 8-lane group and "
+                                "costs a full warp instruction per step"},
+           "gpu_launches": 3 * args.steps, "clocks": head["clocks"]}
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = 200
+        t0 = time.perf_counter()
+        for s in range(sample):
+            O.cholesky_rank_one_update(facs[s].reshape(n, n).T, X[s].cpu().numpy(), 1.0)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": sample / dt, "unit": "updates/s", "cores": 1, "kind": "port",
+                               "sample": f"{sample} of the {count} factors, oracle rank_one_update, one thread"}
+    return res
+
+
 # ----------------------------------------------------------------------------- QR least squares
 
 def bench_ls_ours(args, rank, world):
@@ -1076,7 +1180,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
-                                                                  "mixed_lu", "lu_inverse", "trsv_batched"])
+                                                                  "mixed_lu", "lu_inverse", "trsv_batched", "chol_update"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--single-launch", action="store_true",
                     help="ragged_cholesky: one launch over a host-sorted order with the default tile "
@@ -1112,10 +1216,12 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
-    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse", "trsv_batched"):
+    if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse", "trsv_batched",
+                         "chol_update"):
         res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
                "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours,
-               "lu_inverse": bench_lu_inverse_ours, "trsv_batched": bench_trsv_ours}[args.workload](args, rank, world)
+               "lu_inverse": bench_lu_inverse_ours, "trsv_batched": bench_trsv_ours,
+               "chol_update": bench_chol_update_ours}[args.workload](args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

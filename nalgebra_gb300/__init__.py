@@ -335,9 +335,6 @@ class Cholesky:
         _lib.call("nacu_dposv", m.nrows, m.data.data_ptr(), 0, 0, self.info.data_ptr(), self.logdet.data_ptr(),
                   self.substitute, self.flags, _stream_ptr())
 
-    def _ok(self) -> bool:
-        return int(self.info.item()) == 0
-
     def solve_mut(self, b: DeviceMatrix) -> None:
         """Cholesky::solve_mut (src/linalg/cholesky.rs:122-129)."""
         torch = _torch()
@@ -354,9 +351,65 @@ class Cholesky:
         self.solve_mut(res)
         return res
 
+    @classmethod
+    def _from_factor(cls, factor: DeviceMatrix, flags: int) -> "Cholesky":
+        obj = cls.__new__(cls)
+        obj.chol, obj.flags, obj.substitute = factor, flags, 0.0
+        obj.info, obj.logdet = None, None
+        return obj
+
+    def _ok(self) -> bool:
+        return self.info is None or int(self.info.item()) == 0
+
     def ln_determinant(self) -> float:
-        """Cholesky::ln_determinant (src/linalg/cholesky.rs:172-185)."""
-        return float(self.logdet.item())
+        """Cholesky::ln_determinant (src/linalg/cholesky.rs:172-185): the sum of
+        ln L_ii, in row order, times two; read from the device after a factor
+        update."""
+        if self.logdet is not None:
+            return float(self.logdet.item())
+        d = np.diag(self.chol.to_numpy())
+        acc = 0.0
+        for v in d:
+            acc += float(np.log(abs(v)))
+        return acc * 2.0
+
+    def rank_one_update(self, x: DeviceMatrix, sigma: float) -> None:
+        """Cholesky::rank_one_update (src/linalg/cholesky.rs:277-285): the factor
+        becomes that of L L^T + sigma x x^T, in place (n <= 128); x is read only."""
+        torch = _torch()
+        n = self.chol.nrows
+        assert x.nrows == n and x.ncols == 1
+        s = torch.full((1,), float(sigma), dtype=torch.float64, device="cuda")
+        _lib.call("nacu_dchol_rank1_update_batched", n, self.chol.data.data_ptr(), n * n, x.data.data_ptr(), n,
+                  s.data_ptr(), 1, self.flags & FLAG_EXACT, _stream_ptr())
+        self.logdet = None
+
+    def remove_column(self, j: int) -> "Cholesky":
+        """Cholesky::remove_column (src/linalg/cholesky.rs:365-399): the factor
+        of the matrix without row and column j (n <= 128)."""
+        torch = _torch()
+        n = self.chol.nrows
+        assert 0 <= j < n
+        out = DeviceMatrix(torch.zeros((n - 1) * (n - 1), dtype=torch.float64, device="cuda"), n - 1, n - 1)
+        _lib.call("nacu_dchol_remove_column_batched", n, self.chol.data.data_ptr(), n * n, j, out.data.data_ptr(),
+                  max((n - 1) * (n - 1), 0), 1, self.flags & FLAG_EXACT, _stream_ptr())
+        return Cholesky._from_factor(out, self.flags & FLAG_EXACT)
+
+    def insert_column(self, j: int, col: DeviceMatrix) -> "Cholesky":
+        """Cholesky::insert_column (src/linalg/cholesky.rs:287-357): the factor of
+        the matrix with col (n+1 values) inserted as row and column j (n <= 127).
+        Raises ValueError where nalgebra's assertion on the lower solve fails."""
+        torch = _torch()
+        n = self.chol.nrows
+        assert 0 <= j <= n and col.nrows == n + 1 and col.ncols == 1
+        out = DeviceMatrix(torch.zeros((n + 1) * (n + 1), dtype=torch.float64, device="cuda"), n + 1, n + 1)
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _lib.call("nacu_dchol_insert_column_batched", n, self.chol.data.data_ptr(), n * n, j, col.data.data_ptr(),
+                  n + 1, out.data.data_ptr(), (n + 1) * (n + 1), info.data_ptr(), 1, self.flags & FLAG_EXACT,
+                  _stream_ptr())
+        if int(info.item()) != 0:
+            raise ValueError("insert_column: the lower triangular solve met a zero diagonal")
+        return Cholesky._from_factor(out, self.flags & FLAG_EXACT)
 
     def l(self) -> np.ndarray:
         return np.tril(self.chol.to_numpy())

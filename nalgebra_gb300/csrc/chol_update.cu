@@ -1,19 +1,32 @@
 // Batched updates of Cholesky factors (n <= 128), the GPU form of nalgebra's
 // Cholesky::rank_one_update, remove_column and insert_column
-// (src/linalg/cholesky.rs:277-449): many factors, one warp each.
+// (src/linalg/cholesky.rs:277-449): many factors, a group of G lanes each.
 //
 // The rank-one update is the column recurrence of xx_rank_one_update
-// (cholesky.rs:410-449): per column j, lane 0 carries the scalar chain (the new
-// diagonal, beta, the two axpy coefficients) and the lanes update the rows
-// below j of x and of the factor's column j, 4 rows per lane.  remove_column
-// copies the factor without row and column j and updates the bottom-right
-// corner by the removed column (sigma = 1); insert_column copies it with an
-// empty row and column j, solves the new row with the top-left corner (the
-// lower solve of solve.rs:74-101), forms the centre and the new column (gemv's
-// axcpy order, blas_uninit.rs:127-176) and downdates the bottom-right corner
-// (sigma = -1).  EXACT (NACU_FLAG_EXACT) rounds every operation as Rust does
-// (bit-identical to the oracle's restatement); the default form contracts to
-// FMA.
+// (cholesky.rs:410-449): per column j, the group's first lane carries the
+// scalar chain (the new diagonal, beta, the two axpy coefficients) and the G
+// lanes update the rows below j of x and of the factor's column j.
+// remove_column copies the factor without row and column j and updates the
+// bottom-right corner by the removed column (sigma = 1); insert_column copies
+// it with an empty row and column j, solves the new row with the top-left
+// corner (the lower solve of solve.rs:74-101), forms the centre and the new
+// column (gemv's axcpy order, blas_uninit.rs:127-176) and downdates the
+// bottom-right corner (sigma = -1).  EXACT (NACU_FLAG_EXACT) rounds every
+// operation as Rust does (bit-identical to the oracle's restatement); the
+// default form contracts to FMA.
+//
+// Why groups: the scalar chain is serial per factor (a square root and
+// divisions, each on beta from the previous column), and on this part an FP64
+// instruction costs the same pipe time whether one lane runs it or 32.  With
+// a warp per factor the chain held most of the FP64 pipe; with G lanes per
+// factor one chain instruction serves 32/G factors, while the rows' updates
+// cost the same per factor and a group's loads still fill whole 32-byte
+// sectors.  Measured on 4096 factors of order 128 (ms, G = 32 / 8 / 4 / 2):
+// rank_one_update 1.22 / 0.73 / 1.20 / 1.63, remove_column 0.97 / 1.18 / 1.87 /
+// 2.98, insert_column 1.18 / 1.57 / 2.82 / 5.52 (fewer warps hide less of the
+// chain's latency and of the copies').  So rank_one_update runs G = 8 from
+// kGroupMinBatch factors up and G = 32 below; remove_column and insert_column
+// run G = 32.
 #include <algorithm>
 
 #include "common.cuh"
@@ -21,8 +34,11 @@
 namespace nacu {
 namespace {
 
-constexpr int kUpdWarps = 8;
 constexpr int kUpdMaxN = 128;
+constexpr int kFacPerCta = 16;  // factors per CTA: 16 G threads, 32 KB of vectors
+constexpr int kGroupSmall = 8;
+constexpr int kGroupMinBatch = 1024;
+constexpr unsigned kFull = 0xffffffffu;
 
 template <bool EXACT>
 __device__ __forceinline__ double mul(double a, double b) { return EXACT ? __dmul_rn(a, b) : a * b; }
@@ -31,161 +47,256 @@ __device__ __forceinline__ double add(double a, double b) { return EXACT ? __dad
 template <bool EXACT>
 __device__ __forceinline__ double dvd(double a, double b) { return EXACT ? __ddiv_rn(a, b) : a / b; }
 
-// L (m x m, lower part, leading dimension ld) becomes the factor of
-// L L^T + sigma x x^T; x (the warp's shared-memory slot) is overwritten.
-template <bool EXACT>
-__device__ void warp_rank_one(int m, double* L, int64_t ld, double* x, double sigma, int lane) {
-  double beta = 1.0;  // lane 0 only
+__device__ __forceinline__ void prefetch_l2(const double* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Called by every lane of the warp (the loop bounds are the same for all its
+// groups).  If active, the group's factor L (m x m, lower part, leading
+// dimension ld) becomes the factor of L L^T + sigma x x^T; x (the group's
+// shared-memory slot) is overwritten; rd (another slot) holds 1 / L_jj in the
+// FMA form.  gl: the lane's index in its group.
+template <bool EXACT, int G>
+__device__ void group_rank_one(int m, double* L, int64_t ld, double* x, double* rd, double sigma, int gl,
+                               bool active) {
+  if constexpr (!EXACT) {
+    // the reciprocals of the diagonal (unchanged until step j) G at a time;
+    // gamma = L_jj^2 beta_{j+1} then turns the chain's remaining divisions
+    // into one reciprocal of beta_{j+1}
+    if (active)
+      for (int j = gl; j < m; j += G) rd[j] = 1.0 / L[j + (size_t)j * ld];
+    __syncwarp();
+  }
+  double beta = 1.0, ib = 1.0;  // the group's first lane: beta_j and 1 / beta_j
   for (int j = 0; j < m; ++j) {
+    double* col = L + (size_t)j * ld;
     double a1 = 0.0, a2 = 0.0, b2 = 0.0;
     int upd = 0;
-    if (lane == 0) {
-      const double diag = L[j + j * ld];
-      const double diag2 = mul<EXACT>(diag, diag);
-      const double xj = x[j];
-      const double sigma_xj2 = mul<EXACT>(sigma, mul<EXACT>(xj, xj));
-      const double gamma = add<EXACT>(mul<EXACT>(diag2, beta), sigma_xj2);
-      const double new_diag = __dsqrt_rn(add<EXACT>(diag2, dvd<EXACT>(sigma_xj2, beta)));
-      L[j + j * ld] = new_diag;
-      beta = add<EXACT>(beta, dvd<EXACT>(sigma_xj2, diag2));
-      a1 = dvd<EXACT>(-xj, diag);
-      a2 = mul<EXACT>(dvd<EXACT>(mul<EXACT>(new_diag, sigma), gamma), xj);
-      b2 = dvd<EXACT>(new_diag, diag);
-      upd = (gamma != 0.0);
+    if (active) {
+      for (int r = j + 1 + 16 * gl; r < m; r += 16 * G) prefetch_l2(col + ld + r);  // column j+1, a line per lane
+      if (gl == 0) {
+        const double diag = col[j];
+        const double xj = x[j];
+        if constexpr (EXACT) {
+          const double diag2 = mul<EXACT>(diag, diag);
+          const double sigma_xj2 = mul<EXACT>(sigma, mul<EXACT>(xj, xj));
+          const double gamma = add<EXACT>(mul<EXACT>(diag2, beta), sigma_xj2);
+          const double new_diag = __dsqrt_rn(add<EXACT>(diag2, dvd<EXACT>(sigma_xj2, beta)));
+          col[j] = new_diag;
+          beta = add<EXACT>(beta, dvd<EXACT>(sigma_xj2, diag2));
+          a1 = dvd<EXACT>(-xj, diag);
+          a2 = mul<EXACT>(dvd<EXACT>(mul<EXACT>(new_diag, sigma), gamma), xj);
+          b2 = dvd<EXACT>(new_diag, diag);
+          upd = (gamma != 0.0);
+        } else {
+          const double r = rd[j], r2 = r * r;
+          const double sx = sigma * xj * xj;
+          const double new_diag = sqrt(fma(sx, ib, diag * diag));
+          const double beta1 = fma(sx, r2, beta);
+          const double ib1 = 1.0 / beta1;
+          col[j] = new_diag;
+          a1 = -xj * r;
+          a2 = new_diag * sigma * xj * r2 * ib1;
+          b2 = new_diag * r;
+          upd = (beta1 != 0.0);
+          beta = beta1;
+          ib = ib1;
+        }
+      }
     }
-    a1 = __shfl_sync(0xffffffffu, a1, 0);
-    a2 = __shfl_sync(0xffffffffu, a2, 0);
-    b2 = __shfl_sync(0xffffffffu, b2, 0);
-    upd = __shfl_sync(0xffffffffu, upd, 0);
-    double* col = L + (size_t)j * ld;
-    for (int r = j + 1 + lane; r < m; r += 32) {
-      const double lr = col[r];
-      // x[j+1..] += a1 * L[j+1.., j]; then L[j+1.., j] = a2 * x[j+1..] + b2 * L[j+1.., j]
-      const double xr = EXACT ? __dadd_rn(__dmul_rn(a1, lr), x[r]) : fma(a1, lr, x[r]);
-      x[r] = xr;
-      if (upd) col[r] = EXACT ? __dadd_rn(__dmul_rn(a2, xr), __dmul_rn(b2, lr)) : fma(a2, xr, b2 * lr);
+    a1 = __shfl_sync(kFull, a1, 0, G);
+    a2 = __shfl_sync(kFull, a2, 0, G);
+    b2 = __shfl_sync(kFull, b2, 0, G);
+    upd = __shfl_sync(kFull, upd, 0, G);
+    if (active) {
+      for (int r = j + 1 + gl; r < m; r += G) {
+        const double lr = col[r];
+        // x[j+1..] += a1 * L[j+1.., j]; then L[j+1.., j] = a2 * x[j+1..] + b2 * L[j+1.., j]
+        const double xr = EXACT ? __dadd_rn(__dmul_rn(a1, lr), x[r]) : fma(a1, lr, x[r]);
+        x[r] = xr;
+        if (upd) col[r] = EXACT ? __dadd_rn(__dmul_rn(a2, xr), __dmul_rn(b2, lr)) : fma(a2, xr, b2 * lr);
+      }
     }
     __syncwarp();
   }
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(kUpdWarps * 32) rank1_kernel(int n, double* L, int64_t strideL, const double* X,
-                                                              int64_t strideX, const double* sigma, int batch) {
-  __shared__ double xs_all[kUpdWarps][kUpdMaxN];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kUpdWarps + warp;
-  if (s >= batch) return;
-  double* xs = xs_all[warp];
-  for (int r = lane; r < n; r += 32) xs[r] = X[(size_t)s * strideX + r];  // nalgebra updates a clone of x
-  __syncwarp();
-  warp_rank_one<EXACT>(n, L + (size_t)s * strideL, n, xs, sigma[s], lane);
+// The first factor of this warp; a warp whose first group has no factor has
+// none at all (its factors are consecutive), so it leaves at once.
+template <int G>
+__device__ __forceinline__ bool warp_idle(int batch) {
+  return blockIdx.x * kFacPerCta + (int)(threadIdx.x >> 5) * (32 / G) >= batch;
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(kUpdWarps * 32) remove_kernel(int n, const double* L, int64_t strideL, int j,
-                                                               double* Lout, int64_t strideOut, int batch) {
-  __shared__ double xs_all[kUpdWarps][kUpdMaxN];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kUpdWarps + warp;
-  if (s >= batch) return;
-  const double* l = L + (size_t)s * strideL;
-  double* out = Lout + (size_t)s * strideOut;
+template <bool EXACT, int G>
+__global__ void __launch_bounds__(kFacPerCta * G) rank1_kernel(int n, double* L, int64_t strideL, const double* X,
+                                                               int64_t strideX, const double* sigma, int batch) {
+  __shared__ double xs_all[kFacPerCta][kUpdMaxN];
+  __shared__ double rd_all[kFacPerCta][kUpdMaxN];
+  if (warp_idle<G>(batch)) return;
+  const int g = threadIdx.x / G, gl = threadIdx.x % G;
+  const int s = blockIdx.x * kFacPerCta + g;
+  const bool active = s < batch;
+  double* xs = xs_all[g];
+  if (active)
+    for (int r = gl; r < n; r += G) xs[r] = X[(size_t)s * strideX + r];  // nalgebra updates a clone of x
+  __syncwarp();
+  group_rank_one<EXACT, G>(n, L + (size_t)(active ? s : 0) * strideL, n, xs, rd_all[g], active ? sigma[s] : 0.0, gl,
+                           active);
+}
+
+template <bool EXACT, int G>
+__global__ void __launch_bounds__(kFacPerCta * G) remove_kernel(int n, const double* L, int64_t strideL, int j,
+                                                                double* Lout, int64_t strideOut, int batch) {
+  __shared__ double xs_all[kFacPerCta][kUpdMaxN];
+  __shared__ double rd_all[kFacPerCta][kUpdMaxN];
+  if (warp_idle<G>(batch)) return;
+  const int g = threadIdx.x / G, gl = threadIdx.x % G;
+  const int s = blockIdx.x * kFacPerCta + g;
+  const bool active = s < batch;
   const int m = n - 1;
-  for (int e = lane; e < m * m; e += 32) {
-    const int c = e / m, r = e - c * m;
-    out[e] = l[(r < j ? r : r + 1) + (size_t)(c < j ? c : c + 1) * n];
+  double* out = Lout + (size_t)(active ? s : 0) * strideOut;
+  double* xs = xs_all[g];
+  if (active) {
+    const double* l = L + (size_t)s * strideL;
+    for (int c = 0; c < m; ++c) {
+      const double* src = l + (size_t)(c < j ? c : c + 1) * n;
+      double* dst = out + (size_t)c * m;
+      for (int r = gl; r < m; r += G) dst[r] = src[r < j ? r : r + 1];
+    }
+    for (int r = j + 1 + gl; r < n; r += G) xs[r - j - 1] = l[r + (size_t)j * n];  // the removed column's tail
   }
-  double* xs = xs_all[warp];
-  for (int r = j + 1 + lane; r < n; r += 32) xs[r - j - 1] = l[r + (size_t)j * n];  // the removed column's tail
   __syncwarp();
-  warp_rank_one<EXACT>(m - j, out + j + (size_t)j * m, m, xs, 1.0, lane);
+  group_rank_one<EXACT, G>(m - j, out + j + (size_t)j * m, m, xs, rd_all[g], 1.0, gl, active);
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(kUpdWarps * 32) insert_kernel(int n, const double* L, int64_t strideL, int j,
-                                                               const double* Col, int64_t strideCol, double* Lout,
-                                                               int64_t strideOut, int32_t* info, int batch) {
-  __shared__ double row_all[kUpdWarps][kUpdMaxN];
-  __shared__ double ncol_all[kUpdWarps][kUpdMaxN];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kUpdWarps + warp;
-  if (s >= batch) return;
-  const double* l = L + (size_t)s * strideL;
-  const double* col = Col + (size_t)s * strideCol;
-  double* out = Lout + (size_t)s * strideOut;
+template <bool EXACT, int G>
+__global__ void __launch_bounds__(kFacPerCta * G) insert_kernel(int n, const double* L, int64_t strideL, int j,
+                                                                const double* Col, int64_t strideCol, double* Lout,
+                                                                int64_t strideOut, int32_t* info, int batch) {
+  __shared__ double vs_all[kFacPerCta][kUpdMaxN];  // [0, j): the new row; [j, n): the new column below the centre
+  __shared__ double rd_all[kFacPerCta][kUpdMaxN];
+  if (warp_idle<G>(batch)) return;
+  const int g = threadIdx.x / G, gl = threadIdx.x % G;
+  const int s = blockIdx.x * kFacPerCta + g;
+  const bool active = s < batch;
   const int m = n + 1, len = n - j;
-  for (int e = lane; e < m * m; e += 32) {
-    const int c = e / m, r = e - c * m;
-    out[e] = (r == j || c == j) ? 0.0 : l[(r < j ? r : r - 1) + (size_t)(c < j ? c : c - 1) * n];
+  const double* l = L + (size_t)(active ? s : 0) * strideL;
+  const double* col = Col + (size_t)(active ? s : 0) * strideCol;
+  double* out = Lout + (size_t)(active ? s : 0) * strideOut;
+  double* row = vs_all[g];
+  double* ncol = vs_all[g] + j;
+  if (active) {
+    for (int c = 0; c < m; ++c) {
+      double* dst = out + (size_t)c * m;
+      if (c == j) {
+        for (int r = gl; r < m; r += G) dst[r] = 0.0;
+      } else {
+        const double* src = l + (size_t)(c < j ? c : c - 1) * n;
+        for (int r = gl; r < m; r += G) dst[r] = (r == j) ? 0.0 : src[r < j ? r : r - 1];
+      }
+    }
+    for (int r = gl; r < n; r += G) row[r] = col[r < j ? r : r + 1];
   }
-  double* row = row_all[warp];
-  double* ncol = ncol_all[warp];
-  for (int r = lane; r < j; r += 32) row[r] = col[r];
-  for (int r = lane; r < len; r += 32) ncol[r] = col[j + 1 + r];
   __syncwarp();
   // row j: the lower solve with the top-left corner (solve.rs:74-101)
-  int fail = 0;
+  bool ok = active;
   for (int i = 0; i < j; ++i) {
-    const double d = l[i + (size_t)i * n];
-    if (d == 0.0) {
-      fail = 1;
-      break;
-    }
+    const double* lc = l + (size_t)i * n;
     double coeff = 0.0;
-    if (lane == 0) {
-      coeff = dvd<EXACT>(row[i], d);
-      row[i] = coeff;
+    if (ok) {
+      const double d = lc[i];  // every lane of the group reads it: the group agrees
+      if (d == 0.0) {
+        ok = false;  // nalgebra's assertion
+      } else if (gl == 0) {
+        coeff = dvd<EXACT>(row[i], d);
+        row[i] = coeff;
+      }
     }
-    coeff = __shfl_sync(0xffffffffu, coeff, 0);
-    for (int r = i + 1 + lane; r < j; r += 32)
-      row[r] = EXACT ? __dadd_rn(__dmul_rn(-coeff, l[r + (size_t)i * n]), row[r]) : fma(-coeff, l[r + (size_t)i * n], row[r]);
+    coeff = __shfl_sync(kFull, coeff, 0, G);
+    if (ok)
+      for (int r = i + 1 + gl; r < j; r += G)
+        row[r] = EXACT ? __dadd_rn(__dmul_rn(-coeff, lc[r]), row[r]) : fma(-coeff, lc[r], row[r]);
     __syncwarp();
   }
-  if (fail) {
-    if (lane == 0 && info) info[s] = 1;  // nalgebra's assertion
-    return;
-  }
-  for (int k = lane; k < j; k += 32) out[j + (size_t)k * m] = row[k];
-  // centre: sqrt(col_j - |row|^2), |row|^2 by dotx (blas.rs:96-165)
-  double nrm2;
+  if (active && gl == 0 && info) info[s] = ok ? 0 : 1;
+  if (ok)
+    for (int k = gl; k < j; k += G) out[j + (size_t)k * m] = row[k];
+  // centre: sqrt(col_j - |row|^2), |row|^2 in dotx's order (blas.rs:96-165)
+  double nrm2 = 0.0;
   if constexpr (EXACT) {
-    const int nb = j >> 3;
-    double acc = 0.0;
-    if (lane < 8)
-      for (int b = 0; b < nb; ++b) acc = __dadd_rn(acc, __dmul_rn(row[8 * b + lane], row[8 * b + lane]));
-    const double pair = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, 4));
-    double res = 0.0;
+    if (ok && gl == 0) {
+      double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      const int nb = j >> 3;
+      for (int b = 0; b < nb; ++b)
 #pragma unroll
-    for (int q = 0; q < 4; ++q) res = __dadd_rn(res, __shfl_sync(0xffffffffu, pair, q));
-    for (int e = 8 * nb; e < j; ++e) res = __dadd_rn(res, __dmul_rn(row[e], row[e]));
-    nrm2 = res;
+        for (int q = 0; q < 8; ++q) a[q] = __dadd_rn(a[q], __dmul_rn(row[8 * b + q], row[8 * b + q]));
+      double res = 0.0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) res = __dadd_rn(res, __dadd_rn(a[q], a[q + 4]));
+      for (int e = 8 * nb; e < j; ++e) res = __dadd_rn(res, __dmul_rn(row[e], row[e]));
+      nrm2 = res;
+    }
+    nrm2 = __shfl_sync(kFull, nrm2, 0, G);
   } else {
     double part = 0.0;
-    for (int e = lane; e < j; e += 32) part = fma(row[e], row[e], part);
-    nrm2 = warp_sum(part);
+    if (ok)
+      for (int e = gl; e < j; e += G) part = fma(row[e], row[e], part);
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) part += __shfl_xor_sync(kFull, part, off, G);
+    nrm2 = part;
   }
-  const double center = __dsqrt_rn(add<EXACT>(col[j], -nrm2));
-  if (lane == 0) out[j + (size_t)j * m] = center;
+  const double center = __dsqrt_rn(add<EXACT>(ok ? col[j] : 1.0, -nrm2));
+  if (ok && gl == 0) out[j + (size_t)j * m] = center;
   // new column: gemv(alpha = -1/centre, bottom-left L[j.., ..j], row, beta = 1/centre)
   const double alpha = dvd<EXACT>(-1.0, center), beta = dvd<EXACT>(1.0, center);
-  if (j == 0) {
-    for (int r = lane; r < len; r += 32) ncol[r] = mul<EXACT>(ncol[r], beta);
-  } else {
-    for (int k = 0; k < j; ++k) {
-      const double* lc = l + j + (size_t)k * n;
-      const double val = row[k];
-      const double b = (k == 0) ? beta : 1.0;
-      for (int r = lane; r < len; r += 32)
-        ncol[r] = EXACT ? __dadd_rn(__dmul_rn(__dmul_rn(alpha, lc[r]), val), __dmul_rn(b, ncol[r]))
-                        : fma(alpha * lc[r], val, b * ncol[r]);
+  if (ok) {
+    if (j == 0) {
+      for (int r = gl; r < len; r += G) ncol[r] = mul<EXACT>(ncol[r], beta);
+    } else {
+      for (int k = 0; k < j; ++k) {
+        const double* lc = l + j + (size_t)k * n;
+        const double val = row[k];
+        const double b = (k == 0) ? beta : 1.0;
+        for (int r = gl; r < len; r += G)
+          ncol[r] = EXACT ? __dadd_rn(__dmul_rn(__dmul_rn(alpha, lc[r]), val), __dmul_rn(b, ncol[r]))
+                          : fma(alpha * lc[r], val, b * ncol[r]);
+      }
     }
+    for (int r = gl; r < len; r += G) out[j + 1 + r + (size_t)j * m] = ncol[r];
   }
   __syncwarp();
-  for (int r = lane; r < len; r += 32) out[j + 1 + r + (size_t)j * m] = ncol[r];
-  __syncwarp();
-  warp_rank_one<EXACT>(len, out + (j + 1) + (size_t)(j + 1) * m, m, ncol, -1.0, lane);
-  if (lane == 0 && info) info[s] = 0;
+  group_rank_one<EXACT, G>(len, out + (j + 1) + (size_t)(j + 1) * m, m, ncol, rd_all[g], -1.0, gl, ok);
+}
+
+template <int G>
+void rank1_launch(bool exact, int n, double* L, int64_t strideL, const double* X, int64_t strideX,
+                  const double* sigma, int batch, cudaStream_t st) {
+  const int grid = (batch + kFacPerCta - 1) / kFacPerCta;
+  if (exact)
+    rank1_kernel<true, G><<<grid, kFacPerCta * G, 0, st>>>(n, L, strideL, X, strideX, sigma, batch);
+  else
+    rank1_kernel<false, G><<<grid, kFacPerCta * G, 0, st>>>(n, L, strideL, X, strideX, sigma, batch);
+}
+
+template <int G>
+void remove_launch(bool exact, int n, const double* L, int64_t strideL, int j, double* Lout, int64_t strideOut,
+                   int batch, cudaStream_t st) {
+  const int grid = (batch + kFacPerCta - 1) / kFacPerCta;
+  if (exact)
+    remove_kernel<true, G><<<grid, kFacPerCta * G, 0, st>>>(n, L, strideL, j, Lout, strideOut, batch);
+  else
+    remove_kernel<false, G><<<grid, kFacPerCta * G, 0, st>>>(n, L, strideL, j, Lout, strideOut, batch);
+}
+
+template <int G>
+void insert_launch(bool exact, int n, const double* L, int64_t strideL, int j, const double* col, int64_t strideCol,
+                   double* Lout, int64_t strideOut, int32_t* info, int batch, cudaStream_t st) {
+  const int grid = (batch + kFacPerCta - 1) / kFacPerCta;
+  if (exact)
+    insert_kernel<true, G><<<grid, kFacPerCta * G, 0, st>>>(n, L, strideL, j, col, strideCol, Lout, strideOut,
+                                                             info, batch);
+  else
+    insert_kernel<false, G><<<grid, kFacPerCta * G, 0, st>>>(n, L, strideL, j, col, strideCol, Lout, strideOut,
+                                                              info, batch);
 }
 
 }  // namespace
@@ -202,11 +313,11 @@ int nacu_dchol_rank1_update_batched(int n, double* L, int64_t strideL, const dou
   if (batch == 0 || n == 0) return NACU_SUCCESS;
   if (!L || !X || !sigma) return record_arg_error(-2, "chol rank1 update: null L, X or sigma");
   if (strideL < (int64_t)n * n || strideX < n) return record_arg_error(-3, "chol rank1 update: stride too small");
-  const int grid = (batch + kUpdWarps - 1) / kUpdWarps;
-  if (flags & NACU_FLAG_EXACT)
-    rank1_kernel<true><<<grid, kUpdWarps * 32, 0, (cudaStream_t)stream>>>(n, L, strideL, X, strideX, sigma, batch);
+  const bool exact = flags & NACU_FLAG_EXACT;
+  if (batch >= kGroupMinBatch)
+    rank1_launch<kGroupSmall>(exact, n, L, strideL, X, strideX, sigma, batch, (cudaStream_t)stream);
   else
-    rank1_kernel<false><<<grid, kUpdWarps * 32, 0, (cudaStream_t)stream>>>(n, L, strideL, X, strideX, sigma, batch);
+    rank1_launch<32>(exact, n, L, strideL, X, strideX, sigma, batch, (cudaStream_t)stream);
   return check_launch("nacu_dchol_rank1_update_batched");
 }
 
@@ -220,11 +331,7 @@ int nacu_dchol_remove_column_batched(int n, const double* L, int64_t strideL, in
   if (strideL < (int64_t)n * n || strideOut < (int64_t)(n - 1) * (n - 1))
     return record_arg_error(-3, "chol remove column: stride too small");
   if (n == 1) return NACU_SUCCESS;
-  const int grid = (batch + kUpdWarps - 1) / kUpdWarps;
-  if (flags & NACU_FLAG_EXACT)
-    remove_kernel<true><<<grid, kUpdWarps * 32, 0, (cudaStream_t)stream>>>(n, L, strideL, j, Lout, strideOut, batch);
-  else
-    remove_kernel<false><<<grid, kUpdWarps * 32, 0, (cudaStream_t)stream>>>(n, L, strideL, j, Lout, strideOut, batch);
+  remove_launch<32>(flags & NACU_FLAG_EXACT, n, L, strideL, j, Lout, strideOut, batch, (cudaStream_t)stream);
   return check_launch("nacu_dchol_remove_column_batched");
 }
 
@@ -238,13 +345,8 @@ int nacu_dchol_insert_column_batched(int n, const double* L, int64_t strideL, in
   if ((n > 0 && !L) || !col || !Lout) return record_arg_error(-2, "chol insert column: null L, col or Lout");
   if (strideL < (int64_t)n * n || strideCol < n + 1 || strideOut < (int64_t)(n + 1) * (n + 1))
     return record_arg_error(-3, "chol insert column: stride too small");
-  const int grid = (batch + kUpdWarps - 1) / kUpdWarps;
-  if (flags & NACU_FLAG_EXACT)
-    insert_kernel<true><<<grid, kUpdWarps * 32, 0, (cudaStream_t)stream>>>(n, L, strideL, j, col, strideCol, Lout,
-                                                                         strideOut, info, batch);
-  else
-    insert_kernel<false><<<grid, kUpdWarps * 32, 0, (cudaStream_t)stream>>>(n, L, strideL, j, col, strideCol, Lout,
-                                                                          strideOut, info, batch);
+  insert_launch<32>(flags & NACU_FLAG_EXACT, n, L, strideL, j, col, strideCol, Lout, strideOut, info, batch,
+                    (cudaStream_t)stream);
   return check_launch("nacu_dchol_insert_column_batched");
 }
 
