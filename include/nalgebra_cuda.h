@@ -98,6 +98,28 @@ int nacu_dgetrf_batched(int n, double* A, int64_t strideA, int32_t* ipiv, int32_
 int nacu_dgetrs_batched(int n, int nrhs, double* LU, int64_t strideA, int32_t* ipiv, double* B,
                         int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
 
+/* ---- LU with full pivoting (batched, n <= 128) ------------------------------ */
+
+/* FullPivLU::new (src/linalg/full_piv_lu.rs:56-91) on A + s*strideA (n x n,
+ * in place: the packed L\U factors), and with nrhs > 0 (<= 16)
+ * FullPivLU::solve_mut (:185-211) on B + s*strideB (n x nrhs).  ipiv[s*n+i]
+ * / jpiv[s*n+i]: the row / column swapped with i at step i (i when none);
+ * the pairs with ipiv[i] != i (jpiv[i] != i), in order, are nalgebra's p (q).
+ * Steps stop where the remaining submatrix is zero, as nalgebra's do.
+ * info[s] = 0 when U[n-1][n-1] != 0 (is_invertible, :242-250; B solved),
+ * else 1 + the step that found the remaining submatrix zero (B untouched).
+ * NACU_FLAG_EXACT: factors, pivots and solutions bit-identical to nalgebra. */
+int nacu_dfullpivlu_batched(int n, int nrhs, double* A, int64_t strideA, int32_t* ipiv, int32_t* jpiv, double* B,
+                            int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
+
+/* FullPivLU::solve_mut from factors written by nacu_dfullpivlu_batched (read
+ * only); `lu.try_inverse()` (:216-233) with B = the identity, 16 columns per
+ * call.  info[s] = 0 (solved) or 1 + the first zero U_ii (not invertible: B
+ * untouched). */
+int nacu_dfullpivlu_solve_batched(int n, int nrhs, const double* LU, int64_t strideA, const int32_t* ipiv,
+                                  const int32_t* jpiv, double* B, int64_t strideB, int32_t* info, int batch,
+                                  int flags, nacu_stream_t stream);
+
 /* Inverse from getrf factors: `lu.try_inverse()` (src/linalg/lu.rs:266-297:
  * out = I, then solve_mut(out)), and with nacu_dgetrf_batched before it
  * `m.try_inverse()` for n > 4 (src/linalg/inverse.rs:135-137).  Ainv + s*strideInv

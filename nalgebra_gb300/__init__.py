@@ -35,7 +35,7 @@ from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 __all__ = [
     "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch", "solve_refined", "gemm",
     "PosvLogdet", "cholesky_solve_refined_host",
-    "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE",
+    "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE", "FullPivLU",
 ]
 
 
@@ -153,6 +153,11 @@ class DeviceMatrix:
             raise NotImplementedError("rectangular LU is not on the GPU path")
         return LU(self, flags)
 
+    def full_piv_lu(self, flags: int = 0) -> "FullPivLU":
+        """Matrix::full_piv_lu (src/linalg/decomposition.rs:39-45): factors in
+        place (n <= 128)."""
+        return FullPivLU(self, flags)
+
     def cholesky(self, flags: int = 0, substitute: float | None = None):
         """Matrix::cholesky (decomposition.rs:257-262): Cholesky or None."""
         assert self.is_square(), "The input matrix must be square."
@@ -232,6 +237,81 @@ class LU:
         _lib.call("nacu_dgetri_batched", n, self.lu.data.data_ptr(), n * n, self.ipiv.data_ptr(), out.data.data_ptr(),
                   n * n, info.data_ptr(), 1, self.flags, _stream_ptr())
         return out if int(info.item()) == 0 else None
+
+    def l(self) -> np.ndarray:
+        lu = self.lu.to_numpy()
+        return np.tril(lu, -1) + np.eye(lu.shape[0])
+
+    def u(self) -> np.ndarray:
+        return np.triu(self.lu.to_numpy())
+
+
+class FullPivLU:
+    """LU with full pivoting of one square matrix (n <= 128): packed L\\U in
+    the matrix buffer, row and column pivots on the device."""
+
+    def __init__(self, m: DeviceMatrix, flags: int = 0):
+        torch = _torch()
+        assert m.is_square(), "the batched full-pivot kernel takes square matrices"
+        n = m.nrows
+        self.lu, self.flags = m, flags
+        self.ipiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
+        self.jpiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
+        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _lib.call("nacu_dfullpivlu_batched", n, 0, m.data.data_ptr(), n * n, self.ipiv.data_ptr(),
+                  self.jpiv.data_ptr(), 0, 0, self.info.data_ptr(), 1, flags, _stream_ptr())
+
+    def _solve_cols(self, b: DeviceMatrix) -> bool:
+        torch = _torch()
+        n = self.lu.nrows
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        for c0 in range(0, b.ncols, 16):
+            k = min(16, b.ncols - c0)
+            _lib.call("nacu_dfullpivlu_solve_batched", n, k, self.lu.data.data_ptr(), n * n, self.ipiv.data_ptr(),
+                      self.jpiv.data_ptr(), b.data.data_ptr() + c0 * n * 8, n * k, info.data_ptr(), 1, self.flags,
+                      _stream_ptr())
+        return int(info.item()) == 0
+
+    def solve_mut(self, b: DeviceMatrix) -> bool:
+        """FullPivLU::solve_mut (src/linalg/full_piv_lu.rs:185-211)."""
+        assert b.nrows == self.lu.nrows, "FullPivLU solve matrix dimension mismatch."
+        return self._solve_cols(b)
+
+    def solve(self, b: DeviceMatrix):
+        """FullPivLU::solve (full_piv_lu.rs:168-183): a new matrix, or None."""
+        res = b.clone_owned()
+        return res if self.solve_mut(res) else None
+
+    def try_inverse(self):
+        """FullPivLU::try_inverse (full_piv_lu.rs:216-233): solve_mut on the
+        identity, 16 columns per launch; None when not invertible."""
+        torch = _torch()
+        n = self.lu.nrows
+        out = DeviceMatrix(torch.eye(n, dtype=torch.float64, device="cuda").t().contiguous().reshape(-1), n, n)
+        return out if self._solve_cols(out) else None
+
+    def is_invertible(self) -> bool:
+        """FullPivLU::is_invertible (full_piv_lu.rs:242-250): U[n-1][n-1] != 0."""
+        return int(self.info.item()) == 0
+
+    def p(self):
+        piv = self.ipiv.cpu().numpy()[: self.lu.nrows]
+        return [(i, int(q)) for i, q in enumerate(piv) if q != i]
+
+    def q(self):
+        piv = self.jpiv.cpu().numpy()[: self.lu.nrows]
+        return [(i, int(q)) for i, q in enumerate(piv) if q != i]
+
+    def determinant(self) -> float:
+        """FullPivLU::determinant (full_piv_lu.rs:254-267)."""
+        lu = self.lu.to_numpy()
+        n = lu.shape[0]
+        res = float(lu[n - 1, n - 1])
+        if res == 0.0:
+            return 0.0
+        for i in range(n - 1):
+            res *= float(lu[i, i])
+        return res * (-1.0 if (len(self.p()) + len(self.q())) % 2 else 1.0)
 
     def l(self) -> np.ndarray:
         lu = self.lu.to_numpy()

@@ -42,6 +42,8 @@ SIGNATURES = {
     "nacu_dpotrf_ragged": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _d, _i, _vp]),
     "nacu_dpotrs_ragged": (_i, [_i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _sz, _i, _vp]),
     "nacu_dgetri_batched": (_i, [_i, _vp, _i64, _vp, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_dfullpivlu_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_dfullpivlu_solve_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dtrsv_batched": (_i, [_i, _i, _i, _i, _i, _d, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dchol_rank1_update_batched": (_i, [_i, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dchol_remove_column_batched": (_i, [_i, _vp, _i64, _i, _vp, _i64, _i, _i, _vp]),

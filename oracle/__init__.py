@@ -51,6 +51,8 @@ def lib():
             "orc_sgetrf": (_i64, [_i64, _i64, _fp, _i64, _i32p]),
             "orc_dgetrs": (C.c_int, [_i64, _dp, _i64, _i32p, _dp, _i64, _i64]),
             "orc_dlu_determinant": (C.c_double, [_i64, _dp, _i64, _i64]),
+            "orc_dfullpivlu": (_i64, [_i64, _i64, _dp, _i64, _i32p, _i32p]),
+            "orc_dfullpivlu_solve": (C.c_int, [_i64, _dp, _i64, _i32p, _i32p, _dp, _i64, _i64]),
             "orc_dtrsv": (C.c_int, [_i64, _dp, _i64, _dp, _i64, _i64, C.c_int, C.c_int, C.c_int, C.c_double]),
             "orc_dchol_rank1": (None, [_i64, _dp, _i64, _dp, C.c_double]),
             "orc_dchol_remove_column": (None, [_i64, _dp, _i64, _i64, _dp, _i64]),
@@ -123,6 +125,47 @@ def lu_solve(lu_, ipiv, b):
     ok = lib().orc_dgetrs(n, _p(lu_), max(n, 1), _p(np.ascontiguousarray(ipiv, dtype=np.int32), _i32p),
                           _p(x2), max(n, 1), x2.shape[1])
     return x if ok else None
+
+
+def full_piv_lu(a):
+    """FullPivLU::new (src/linalg/full_piv_lu.rs:56-91).
+
+    Returns (packed L\\U, ipiv, jpiv, steps): ipiv[i] / jpiv[i] are the row /
+    column swapped with i at step i (i when none); steps < min(m, n) when the
+    remaining submatrix was zero (nalgebra's `break`).
+    """
+    a = np.array(a, dtype=np.float64, order="F", copy=True)
+    m, n = a.shape
+    ipiv = np.zeros(min(m, n), dtype=np.int32)
+    jpiv = np.zeros(min(m, n), dtype=np.int32)
+    steps = lib().orc_dfullpivlu(m, n, _p(a), max(m, 1), _p(ipiv, _i32p), _p(jpiv, _i32p))
+    return a, ipiv, jpiv, int(steps)
+
+
+def full_piv_lu_solve(lu_, ipiv, jpiv, b):
+    """FullPivLU::solve (src/linalg/full_piv_lu.rs:168-211).  Returns x, or None
+    when lu[n-1][n-1] == 0 (is_invertible, :242-250)."""
+    lu_ = _f64(lu_)
+    n = lu_.shape[0]
+    x = np.array(b, dtype=np.float64, order="F", copy=True)
+    x2 = x.reshape(n, -1, order="F")
+    ok = lib().orc_dfullpivlu_solve(n, _p(lu_), max(n, 1), _p(np.ascontiguousarray(ipiv, dtype=np.int32), _i32p),
+                                    _p(np.ascontiguousarray(jpiv, dtype=np.int32), _i32p), _p(x2), max(n, 1),
+                                    x2.shape[1])
+    return x if ok else None
+
+
+def full_piv_lu_determinant(lu_, ipiv, jpiv):
+    """FullPivLU::determinant (src/linalg/full_piv_lu.rs:254-267): U[n-1][n-1]
+    times the other diagonal entries in order, times the signs of p and q."""
+    n = lu_.shape[0]
+    res = float(lu_[n - 1, n - 1])
+    if res == 0.0:
+        return 0.0
+    for i in range(n - 1):
+        res *= float(lu_[i, i])
+    swaps = int(np.sum(np.asarray(ipiv) != np.arange(n))) + int(np.sum(np.asarray(jpiv) != np.arange(n)))
+    return res * (-1.0 if swaps % 2 else 1.0)
 
 
 def cholesky_rank_one_update(l, x, sigma):

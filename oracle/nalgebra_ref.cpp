@@ -40,6 +40,13 @@ int orc_dgetrs(int64_t n, const double* lu, int64_t lda, const int32_t* ipiv, do
                int64_t nrhs) {
   return orc::lu_solve<double>(n, lu, lda, ipiv, b, ldb, nrhs) ? 1 : 0;
 }
+int64_t orc_dfullpivlu(int64_t m, int64_t n, double* a, int64_t lda, int32_t* ipiv, int32_t* jpiv) {
+  return (int64_t)orc::full_piv_lu_factor<double>(m, n, a, lda, ipiv, jpiv);
+}
+int orc_dfullpivlu_solve(int64_t n, const double* lu, int64_t lda, const int32_t* ipiv, const int32_t* jpiv,
+                         double* b, int64_t ldb, int64_t nrhs) {
+  return orc::full_piv_lu_solve<double>(n, lu, lda, ipiv, jpiv, b, ldb, nrhs) ? 1 : 0;
+}
 double orc_dlu_determinant(int64_t n, const double* lu, int64_t lda, int64_t len) {
   return orc::lu_determinant<double>(n, lu, lda, len);
 }

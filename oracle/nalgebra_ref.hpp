@@ -168,6 +168,120 @@ inline std::size_t lu_factor(std::size_t m, std::size_t n, T* a, std::size_t lda
   return len;
 }
 
+// ---------------------------------------------------------------------------
+// LU with full pivoting (src/linalg/full_piv_lu.rs)
+// ---------------------------------------------------------------------------
+
+// Matrix::icamax_full for a real m x n matrix (src/base/min_max.rs:146-167):
+// columns in order, rows within each, strict `>` from (0, 0), so ties keep the
+// earlier position in that order and a NaN never wins unless it is at (0, 0).
+template <class T>
+inline void icamax_full(std::size_t m, std::size_t n, const T* a, std::size_t lda, std::size_t* ri,
+                        std::size_t* ci) {
+  T the_max = std::fabs(a[0]);
+  std::size_t bi = 0, bj = 0;
+  for (std::size_t j = 0; j < n; ++j)
+    for (std::size_t i = 0; i < m; ++i) {
+      const T v = std::fabs(a[i + j * lda]);
+      if (v > the_max) {
+        the_max = v;
+        bi = i;
+        bj = j;
+      }
+    }
+  *ri = bi;
+  *ci = bj;
+}
+
+// FullPivLU::new (full_piv_lu.rs:56-91): per step i the pivot of the trailing
+// submatrix (icamax_full), a stop when it is zero (the rest of the matrix is
+// zero), the column swap, then the same rows swap and gauss_step as LU::new.
+// Writes ipiv[i] / jpiv[i] (the row / column swapped with i at step i, i when
+// none or after the stop) and returns the number of steps taken.  The pairs
+// with ipiv[i] != i (jpiv[i] != i), in order, are nalgebra's p (q).
+template <class T>
+inline std::size_t full_piv_lu_factor(std::size_t m, std::size_t n, T* a, std::size_t lda, int32_t* ipiv,
+                                      int32_t* jpiv) {
+  const std::size_t mn = m < n ? m : n;
+  for (std::size_t i = 0; i < mn; ++i) ipiv[i] = jpiv[i] = (int32_t)i;
+  for (std::size_t i = 0; i < mn; ++i) {
+    std::size_t r, c;
+    icamax_full(m - i, n - i, a + i + i * lda, lda, &r, &c);
+    const std::size_t row_piv = r + i, col_piv = c + i;
+    const T diag = a[row_piv + col_piv * lda];
+    if (diag == T(0)) return i;
+    if (col_piv != i)
+      for (std::size_t k = 0; k < m; ++k) {  // swap_columns(i, col_piv)
+        T t = a[k + i * lda];
+        a[k + i * lda] = a[k + col_piv * lda];
+        a[k + col_piv * lda] = t;
+      }
+    jpiv[i] = (int32_t)col_piv;
+    if (row_piv != i) {
+      ipiv[i] = (int32_t)row_piv;
+      for (std::size_t k = 0; k < i; ++k) {  // columns_range_mut(..i).swap_rows(i, row_piv)
+        T t = a[i + k * lda];
+        a[i + k * lda] = a[row_piv + k * lda];
+        a[row_piv + k * lda] = t;
+      }
+    }
+    gauss_step(m, n, a, lda, diag, i, row_piv);
+  }
+  return mn;
+}
+
+// FullPivLU::solve_mut (full_piv_lu.rs:185-211) for an n x n factor: false (b
+// untouched) unless lu[n-1][n-1] != 0 (is_invertible, :242-250); then
+// p.permute_rows, the unit-lower solve, the upper solve (whose result nalgebra
+// ignores: a zero U_ii stops it there, later columns of b unsolved), and
+// q.inv_permute_rows (permutation_sequence.rs:108-116).
+template <class T>
+inline bool full_piv_lu_solve(std::size_t n, const T* lu, std::size_t lda, const int32_t* ipiv,
+                              const int32_t* jpiv, T* b, std::size_t ldb, std::size_t nrhs) {
+  if (n == 0) return true;
+  if (lu[(n - 1) + (n - 1) * lda] == T(0)) return false;
+  for (std::size_t i = 0; i < n; ++i) {
+    const std::size_t p = (std::size_t)ipiv[i];
+    if (p != i)
+      for (std::size_t c = 0; c < nrhs; ++c) {
+        T t = b[i + c * ldb];
+        b[i + c * ldb] = b[p + c * ldb];
+        b[p + c * ldb] = t;
+      }
+  }
+  for (std::size_t c = 0; c < nrhs; ++c) {  // solve_lower_triangular_with_diag_mut(b, 1)
+    T* bc = b + c * ldb;
+    for (std::size_t i = 0; i + 1 < n; ++i) {
+      const T coeff = bc[i] / T(1);
+      axpy(n - i - 1, -coeff, lu + (i + 1) + i * lda, T(1), bc + i + 1);
+    }
+  }
+  bool stop = false;
+  for (std::size_t c = 0; c < nrhs && !stop; ++c) {  // solve_upper_triangular_mut(b)
+    T* bc = b + c * ldb;
+    for (std::size_t ii = n; ii-- > 0;) {
+      const T diag = lu[ii + ii * lda];
+      if (diag == T(0)) {
+        stop = true;
+        break;
+      }
+      const T coeff = bc[ii] / diag;
+      bc[ii] = coeff;
+      axpy(ii, -coeff, lu + ii * lda, T(1), bc);
+    }
+  }
+  for (std::size_t k = n; k-- > 0;) {  // q.inv_permute_rows(b)
+    const std::size_t q = (std::size_t)jpiv[k];
+    if (q != k)
+      for (std::size_t c = 0; c < nrhs; ++c) {
+        T t = b[k + c * ldb];
+        b[k + c * ldb] = b[q + c * ldb];
+        b[q + c * ldb] = t;
+      }
+  }
+  return true;
+}
+
 // LU::solve_mut (lu.rs:242-260): permute_rows, then the unit-lower forward
 // solve (solve.rs:106-133), then the upper back substitution (solve.rs:137-182).
 // Returns false when some U_ii == 0 (columns before the failing one are solved).

@@ -286,3 +286,113 @@ def test_triangular_solve_properties(seed):
         assert np.allclose((tri.T if trans else tri) @ x, b, atol=1e-7, rtol=0)
     x = O.triangular_solve(a, b, diag=1.0)
     assert np.allclose((np.tril(a, -1) + np.eye(4)) @ x, b, atol=1e-7, rtol=0)
+
+
+def _inv_permute_columns(m, jpiv):
+    """PermutationSequence::inv_permute_columns (permutation_sequence.rs:131-140)."""
+    m = m.copy()
+    for i in reversed(range(len(jpiv))):
+        q = jpiv[i]
+        if q != i:
+            m[:, [i, q]] = m[:, [q, i]]
+    return m
+
+
+@pytest.mark.parametrize("case", ["full_piv_lu_simple", "full_piv_lu_simple_with_pivot"])
+def test_full_piv_lu_known_answers(case):
+    """tests/linalg/full_piv_lu.rs:3-40: the exact determinant and P, L, U, Q
+    reconstructing m."""
+    k = _known()[case]
+    m = _rows(k["rows"])
+    lu, ipiv, jpiv, steps = O.full_piv_lu(m)
+    assert steps == 3
+    assert O.full_piv_lu_determinant(lu, ipiv, jpiv) == k["determinant"]
+    l, u = _unpack(lu, ipiv)
+    rec = _inv_permute_columns(_inv_permute_rows(l @ u, ipiv), jpiv)
+    assert np.allclose(rec, m, atol=k["reconstruction_epsilon"], rtol=0)
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 17, 40])
+def test_full_piv_lu_properties(n):
+    """The reference's property tests (tests/linalg/full_piv_lu.rs:62-100):
+    P L U Q reconstructs m, |L| <= 1, solve gives m x = b, the determinant."""
+    rng = np.random.default_rng(900 + n)
+    m = rng.standard_normal((n, n))
+    lu, ipiv, jpiv, steps = O.full_piv_lu(m)
+    assert steps == n
+    l, u = _unpack(lu, ipiv)
+    rec = _inv_permute_columns(_inv_permute_rows(l @ u, ipiv), jpiv)
+    assert np.allclose(rec, m, atol=1e-12 * n, rtol=0)
+    assert np.all(np.abs(np.tril(lu, -1)) <= 1.0)
+    b = rng.standard_normal((n, 3))
+    x = O.full_piv_lu_solve(lu, ipiv, jpiv, b)
+    assert np.allclose(m @ x, b, atol=1e-10, rtol=0)
+    det = O.full_piv_lu_determinant(lu, ipiv, jpiv)
+    assert np.isclose(det, np.linalg.det(m), rtol=1e-10, atol=0)
+
+
+def test_full_piv_lu_rank_deficient_stops():
+    """A rank-1 4x4 matrix: one step, then the remaining submatrix is zero
+    (full_piv_lu.rs:73-76), so the solve returns None."""
+    m = np.outer([1.0, 2.0, 4.0, 0.5], [3.0, -1.0, 2.0, 5.0])  # rank 1, every elimination exact
+    lu, ipiv, jpiv, steps = O.full_piv_lu(m)
+    assert steps == 1 and ipiv[0] == 2 and jpiv[0] == 3
+    assert list(ipiv[steps:]) == list(range(steps, 4)) and list(jpiv[steps:]) == list(range(steps, 4))
+    assert O.full_piv_lu_solve(lu, ipiv, jpiv, np.ones(4)) is None
+    assert O.full_piv_lu_determinant(lu, ipiv, jpiv) == 0.0
+    lz, _, _, sz = O.full_piv_lu(np.zeros((3, 3)))
+    assert sz == 0 and np.all(lz == 0)
+
+
+def test_full_piv_lu_pivot_rule_ties_and_nan():
+    """icamax_full (min_max.rs:146-167): the first maximum in column-major order;
+    a NaN wins only at (0, 0)."""
+    m = np.array([[1.0, 4.0], [4.0, 2.0]])  # equal maxima at (1, 0) and (0, 1): (1, 0) first
+    _, ipiv, jpiv, _ = O.full_piv_lu(m)
+    assert ipiv[0] == 1 and jpiv[0] == 0
+    m = np.array([[np.nan, 5.0], [1.0, 2.0]])
+    _, ipiv, jpiv, _ = O.full_piv_lu(m)
+    assert ipiv[0] == 0 and jpiv[0] == 0
+    m = np.array([[1.0, np.nan], [3.0, 2.0]])
+    _, ipiv, jpiv, _ = O.full_piv_lu(m)
+    assert ipiv[0] == 1 and jpiv[0] == 0
+
+
+def _pure_python_full_piv_lu(a):
+    """Independent pure-Python restatement of FullPivLU::new for tiny matrices."""
+    a = [list(map(float, r)) for r in a]
+    n = len(a)
+    ipiv, jpiv, steps = list(range(n)), list(range(n)), n
+    for i in range(n):
+        best, br, bc = abs(a[i][i]), i, i
+        for c in range(i, n):
+            for r in range(i, n):
+                if abs(a[r][c]) > best:
+                    best, br, bc = abs(a[r][c]), r, c
+        diag = a[br][bc]
+        if diag == 0.0:
+            steps = i
+            break
+        for r in range(n):
+            a[r][i], a[r][bc] = a[r][bc], a[r][i]
+        jpiv[i], ipiv[i] = bc, br
+        a[i], a[br] = a[br], a[i]
+        inv = 1.0 / diag
+        for r in range(i + 1, n):
+            a[r][i] = a[r][i] * inv
+        for c in range(i + 1, n):
+            p = a[i][c]
+            for r in range(i + 1, n):
+                a[r][c] = (-p) * a[r][i] + a[r][c]
+    return np.array(a), np.array(ipiv), np.array(jpiv), steps
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 8])
+def test_full_piv_lu_matches_pure_python_restatement_bitwise(n):
+    rng = np.random.default_rng(40 + n)
+    a = rng.uniform(-100, 100, size=(n, n))
+    lu, ipiv, jpiv, steps = O.full_piv_lu(a)
+    lu2, ipiv2, jpiv2, steps2 = _pure_python_full_piv_lu(a)
+    assert steps == steps2
+    assert np.array_equal(ipiv, ipiv2) and np.array_equal(jpiv, jpiv2)
+    assert np.array_equal(lu, lu2)
