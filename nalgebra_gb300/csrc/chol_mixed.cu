@@ -52,9 +52,7 @@ struct MixedArgs {
   double subst;
 };
 
-__device__ __forceinline__ unsigned long long abs_bits(double x) {
-  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
-}
+__device__ __forceinline__ unsigned long long abs_bits(double x) { return abs_bits_f64(x); }
 
 // max over the CTA of per-thread values (non-negative doubles compared as
 // integers: no FP64 instructions); red: kRhsChunk x 4 warps scratch.

@@ -63,13 +63,27 @@ __device__ __forceinline__ T axpy1(T y, T a, T x) {
 // unsigned integer (valid for non-negative IEEE values); a NaN wins only at
 // the first position of the scan (where nalgebra's running max starts), and is
 // ignored elsewhere.  Ties resolve to the lowest index by the reduction.
+// |x| as its bit image (for non-negative doubles the integer order is the
+// numeric order), taken through an opaque mov: a plain mask of the
+// reinterpreted bits is recognised as fabs and then costs an FP64 add.
+__device__ __forceinline__ unsigned long long abs_bits_f64(double x) {
+  unsigned lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+  return ((unsigned long long)(hi & 0x7fffffffu) << 32) | lo;
+}
+
+// The bit image is taken through an opaque mov: a plain mask of the
+// reinterpreted bits is recognised as fabs and then costs an FP64 add (an
+// FP64 pipe slot) per key, where the key is taken for every updated element.
 __device__ __forceinline__ uint64_t pivot_key(double x, bool first) {
-  uint64_t b = (uint64_t)__double_as_longlong(x) & 0x7fffffffffffffffull;
+  const uint64_t b = abs_bits_f64(x);
   if (b > 0x7ff0000000000000ull) return first ? ~0ull : 0ull;
   return b;
 }
 __device__ __forceinline__ uint64_t pivot_key(float x, bool first) {
-  uint32_t b = (uint32_t)__float_as_uint(x) & 0x7fffffffu;
+  unsigned u;
+  asm("mov.b32 %0, %1;" : "=r"(u) : "f"(x));
+  const uint32_t b = u & 0x7fffffffu;
   if (b > 0x7f800000u) return first ? ~0ull : 0ull;
   return (uint64_t)b;
 }

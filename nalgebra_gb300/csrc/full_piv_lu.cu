@@ -2,25 +2,28 @@
 // FullPivLU::new (src/linalg/full_piv_lu.rs:56-91), FullPivLU::solve_mut
 // (:185-211) and, on identity right-hand sides, try_inverse (:216-233).
 //
-// One CTA per system; the matrix lives in shared memory (column-major, odd
-// leading dimension so row walks hit no bank conflicts).  Per step i:
-//   - warp 0 reduces the per-warp pivot candidates to icamax_full's choice
-//     (src/base/min_max.rs:146-167: largest |a| of the trailing submatrix,
-//     the first in column-major order on ties, a NaN only at its first
-//     position), stops when that pivot is zero (the rest of the matrix is
-//     zero: nalgebra's `break`), and swaps columns i and q;
-//   - all threads swap rows i and p in every other column and form the
-//     multipliers of column i (gauss_step_swap's order, lu.rs:362-389);
-//   - all threads apply the rank-1 update of the trailing submatrix over a
-//     flattened index, each tracking the largest |a| it wrote (the integer
-//     image of |a|, no FP64 issue slots), so the next step's pivot search
-//     needs no pass of its own.
-// Three CTA barriers per step.  The solve then runs nalgebra's steps in
-// nalgebra's order, one warp per right-hand side: permute rows, unit-lower
-// solve, upper solve (stopping where nalgebra's would), inverse column
-// permutation.  EXACT (NACU_FLAG_EXACT) rounds every product and sum
-// separately and divides where nalgebra divides (bit-identical results); the
-// default form contracts to FMA and multiplies by reciprocals.
+// One CTA per system; the matrix and the right-hand sides live in shared
+// memory (column-major, odd leading dimension so row walks hit no bank
+// conflicts).  Per step i:
+//   - every warp reduces the per-warp pivot candidates (key, position, value)
+//     to icamax_full's choice (src/base/min_max.rs:146-167: the largest |a| of
+//     the trailing submatrix, the first in column-major order on ties, a NaN
+//     only at its first position) and stops when that pivot is zero (the rest
+//     of the matrix is zero: nalgebra's `break`);
+//   - warp 0 rewrites columns i and q from registers (the column swap, the row
+//     swap of rows i and p, the multipliers of column i in gauss_step_swap's
+//     order, lu.rs:362-389) while the other warps swap rows i and p in every
+//     other column, the right-hand sides included;
+//   - all threads apply the rank-1 update of the trailing columns (the
+//     right-hand sides ride along: the forward solve in nalgebra's order),
+//     each tracking the largest |a| it wrote (the integer image of |a|, no
+//     FP64 issue slots), so the next pivot search needs no pass of its own.
+// Two CTA barriers per step.  The back substitution (stopping where nalgebra's
+// would) and the inverse column permutation then run one warp per right-hand
+// side; solving from given factors runs the permutation and the forward solve
+// there too.  EXACT (NACU_FLAG_EXACT) rounds every product and sum separately
+// and divides where nalgebra divides (bit-identical results); the default
+// form contracts to FMA and multiplies by reciprocals.
 #include <algorithm>
 
 #include "common.cuh"
@@ -34,7 +37,7 @@ constexpr int kFpMaxN = 128;
 constexpr int kFpMaxRhs = 16;
 
 struct FpLayout {
-  size_t sa, scal, key, idx, piv, ipiv, jpiv, rd, total;
+  size_t sa, key, val, idx, piv, ipiv, jpiv, rd, total;
 };
 
 __host__ __device__ inline size_t fp_align(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -43,9 +46,9 @@ __host__ __device__ inline FpLayout fp_layout(int n, int nrhs) {
   const int ld = n | 1;
   FpLayout l;
   l.sa = 0;
-  l.scal = fp_align(l.sa + (size_t)ld * (n + nrhs) * sizeof(double));
-  l.key = fp_align(l.scal + 4 * sizeof(double));
-  l.idx = fp_align(l.key + kFpWarps * sizeof(uint64_t));
+  l.key = fp_align(l.sa + (size_t)ld * (n + nrhs) * sizeof(double));
+  l.val = fp_align(l.key + kFpWarps * sizeof(uint64_t));
+  l.idx = fp_align(l.val + kFpWarps * sizeof(double));
   l.piv = fp_align(l.idx + kFpWarps * sizeof(int));
   l.ipiv = fp_align(l.piv + 4 * sizeof(int));
   l.jpiv = fp_align(l.ipiv + (size_t)n * sizeof(int));
@@ -54,17 +57,47 @@ __host__ __device__ inline FpLayout fp_layout(int n, int nrhs) {
   return l;
 }
 
+// A warp's best (key, index, value) into its candidate slot.
+__device__ __forceinline__ void fp_publish(uint64_t key, int idx, double val, uint64_t* s_key, int* s_idx,
+                                           double* s_val, int warp, int lane) {
+  uint64_t k = key;
+  int i = idx;
+  warp_argmax(k, i);
+  const unsigned who = __ballot_sync(0xffffffffu, key == k && idx == i);
+  const double v = __shfl_sync(0xffffffffu, val, __ffs(who) - 1);
+  if (lane == 0) {
+    s_key[warp] = k;
+    s_idx[warp] = i;
+    s_val[warp] = v;
+  }
+}
+
+// The pivot of the step from the warps' candidates: icamax_full's choice
+// (the largest key, the lowest column-major index on ties); returns its value.
+__device__ __forceinline__ double fp_pick(const uint64_t* s_key, const int* s_idx, const double* s_val, int lane,
+                                          int& idx) {
+  const uint64_t key = lane < kFpWarps ? s_key[lane] : 0ull;
+  const int id = lane < kFpWarps ? s_idx[lane] : 0x7fffffff;
+  const double val = lane < kFpWarps ? s_val[lane] : 0.0;
+  uint64_t k = key;
+  int i = id;
+  warp_argmax(k, i);
+  const unsigned who = __ballot_sync(0xffffffffu, lane < kFpWarps && key == k && id == i);
+  idx = i;
+  return __shfl_sync(0xffffffffu, val, __ffs(who) - 1);
+}
+
 // mode: 0 = factor, 1 = factor + solve, 2 = solve from given factors.
 template <bool EXACT>
-__global__ void __launch_bounds__(kFpThreads) fullpiv_kernel(int n, int nrhs, double* __restrict__ A, int64_t strideA,
+__global__ void __launch_bounds__(kFpThreads, 5) fullpiv_kernel(int n, int nrhs, double* __restrict__ A, int64_t strideA,
                                                              int32_t* __restrict__ ipiv, int32_t* __restrict__ jpiv,
                                                              double* __restrict__ B, int64_t strideB,
                                                              int32_t* __restrict__ info, int batch, int mode) {
   extern __shared__ __align__(16) unsigned char fp_smem[];
   const FpLayout lay = fp_layout(n, nrhs);
   double* sa = reinterpret_cast<double*>(fp_smem + lay.sa);
-  double* s_scal = reinterpret_cast<double*>(fp_smem + lay.scal);  // [0] 1/pivot, [1] pivot, [2] a_ii after the column swap
   uint64_t* s_key = reinterpret_cast<uint64_t*>(fp_smem + lay.key);
+  double* s_val = reinterpret_cast<double*>(fp_smem + lay.val);
   int* s_idx = reinterpret_cast<int*>(fp_smem + lay.idx);
   int* s_piv = reinterpret_cast<int*>(fp_smem + lay.piv);  // [0] row, [1] column pivot, [2] steps, [3] zero-diagonal row
   int* s_ipiv = reinterpret_cast<int*>(fp_smem + lay.ipiv);
@@ -94,82 +127,85 @@ __global__ void __launch_bounds__(kFpThreads) fullpiv_kernel(int n, int nrhs, do
     }
     __syncthreads();
 
-    int inf = 0;
+    int inf = 0, steps = n;
+    const int ncols = n + solve_cols;  // the right-hand sides ride along the elimination
     if (mode != 2) {
       // the first search, over the whole matrix
       uint64_t bkey = 0;
       int bidx = 0x7fffffff;
+      double bval = 0.0;
       for (int e = tid; e < n * n; e += kFpThreads) {
         const int c = e / n, r = e - c * n;
-        const uint64_t k = pivot_key(sa[(size_t)c * ld + r], e == 0);
+        const double v = sa[(size_t)c * ld + r];
+        const uint64_t k = pivot_key(v, e == 0);
         if (bidx == 0x7fffffff || k > bkey) {
           bkey = k;
           bidx = e;
+          bval = v;
         }
       }
-      warp_argmax(bkey, bidx);
-      if (lane == 0) {
-        s_key[warp] = bkey;
-        s_idx[warp] = bidx;
-      }
+      fp_publish(bkey, bidx, bval, s_key, s_idx, s_val, warp, lane);
       __syncthreads();
-      int steps = n;
       for (int i = 0; i < n; ++i) {
+        // every warp reduces the candidates to the same pivot (no barrier)
         const int msz = n - i;
-        if (warp == 0) {
-          uint64_t key = lane < kFpWarps ? s_key[lane] : 0ull;
-          int idx = lane < kFpWarps ? s_idx[lane] : 0x7fffffff;
-          warp_argmax(key, idx);
-          const int rp = i + idx % msz, cp = i + idx / msz;
-          const double diag = sa[(size_t)cp * ld + rp];
-          if (diag != 0.0) {
-            if (cp != i)  // swap_columns(i, cp)
-              for (int r = lane; r < n; r += 32) {
-                const double t = sa[(size_t)i * ld + r];
-                sa[(size_t)i * ld + r] = sa[(size_t)cp * ld + r];
-                sa[(size_t)cp * ld + r] = t;
-              }
-            __syncwarp();
-            if (lane == 0) {
-              s_piv[0] = rp;
-              s_scal[0] = 1.0 / diag;  // gauss_step's inv_diag: one division per step
-              s_scal[2] = sa[(size_t)i * ld + i];
-              s_ipiv[i] = rp;
-              s_jpiv[i] = cp;
-            }
-          }
-          if (lane == 0) s_scal[1] = diag;
-        }
-        __syncthreads();
-        const double diag = s_scal[1];
-        if (diag == 0.0) {  // full_piv_lu.rs:73-76
+        int idx;
+        const double diag = fp_pick(s_key, s_idx, s_val, lane, idx);
+        if (diag == 0.0) {  // full_piv_lu.rs:73-76: the rest of the matrix is zero
           steps = i;
           break;
         }
-        const int piv = s_piv[0];
-        const double inv_diag = s_scal[0], old_ii = s_scal[2];
-        double* coli = sa + (size_t)i * ld;
-        if (piv != i)
-          for (int c = tid; c < n; c += kFpThreads) {
-            if (c == i) continue;
+        const int rp = i + idx % msz, cp = i + idx / msz;
+        if (warp == 0) {
+          // columns i and cp at once, from registers: the column swap, the
+          // row swap of rows i and rp, and the multipliers of column i
+          const double inv_diag = 1.0 / diag;  // gauss_step's inv_diag
+          double* ci = sa + (size_t)i * ld;
+          double* cq = sa + (size_t)cp * ld;
+          const double a_ii = ci[i], a_rpi = ci[rp], a_icp = cq[i];
+          double vi[kFpMaxN / 32], vq[kFpMaxN / 32];
+#pragma unroll
+          for (int q = 0; q < kFpMaxN / 32; ++q) {
+            const int r = lane + 32 * q;
+            if (r < n) {
+              vi[q] = ci[r];
+              vq[q] = cq[r];
+            }
+          }
+          __syncwarp();
+#pragma unroll
+          for (int q = 0; q < kFpMaxN / 32; ++q) {
+            const int r = lane + 32 * q;
+            if (r < n) {
+              if (cp != i) cq[r] = (r == i) ? a_rpi : (r == rp ? a_ii : vi[q]);
+              double u = (r == i) ? diag : (r == rp ? a_icp : vq[q]);
+              if (r > i) u = EXACT ? __dmul_rn(u, inv_diag) : u * inv_diag;
+              ci[r] = u;
+            }
+          }
+          if (lane == 0) {
+            s_ipiv[i] = rp;
+            s_jpiv[i] = cp;
+          }
+        } else if (rp != i) {
+          for (int c = tid - 32; c < ncols; c += kFpThreads - 32) {
+            if (c == i || c == cp) continue;
             double* col = sa + (size_t)c * ld;
             const double t = col[i];
-            col[i] = col[piv];
-            col[piv] = t;
+            col[i] = col[rp];
+            col[rp] = t;
           }
-        for (int r = i + 1 + tid; r < n; r += kFpThreads) {
-          const double v = (r == piv) ? old_ii : coli[r];
-          coli[r] = EXACT ? __dmul_rn(v, inv_diag) : v * inv_diag;
         }
-        if (tid == 0) coli[i] = diag;
         __syncthreads();
-        // rank-1 update of rows i+1.. of columns i+1.., tracking the next pivot
+        // rank-1 update of rows i+1.. of columns i+1.. (right-hand sides
+        // included), tracking the next pivot over the matrix columns
         const int m = n - 1 - i;
         uint64_t bk = 0;
         int bi = 0x7fffffff;
+        double bv = 0.0;
         if (m > 0) {
-          const int total = m * m;
-          const double* lcol = coli + i + 1;
+          const int total = m * (ncols - 1 - i), mm = m * m;
+          const double* lcol = sa + (size_t)i * ld + i + 1;
           int e = tid;
           int cq = e / m;
           int rr = e - cq * m;
@@ -179,10 +215,13 @@ __global__ void __launch_bounds__(kFpThreads) fullpiv_kernel(int n, int nrhs, do
             double* col = base + (size_t)cq * ld;
             const double v = axpy1<EXACT>(col[i + 1 + rr], -col[i], lcol[rr]);
             col[i + 1 + rr] = v;
-            const uint64_t k = pivot_key(v, e == 0);
-            if (bi == 0x7fffffff || k > bk) {  // e increases: the first of equal keys stays
-              bk = k;
-              bi = e;
+            if (e < mm) {  // a matrix column: e = cq * m + rr, column-major in the next submatrix
+              const uint64_t k = pivot_key(v, e == 0);
+              if (bi == 0x7fffffff || k > bk) {  // e increases: the first of equal keys stays
+                bk = k;
+                bi = e;
+                bv = v;
+              }
             }
             rr += dr;
             cq += dq;
@@ -192,11 +231,7 @@ __global__ void __launch_bounds__(kFpThreads) fullpiv_kernel(int n, int nrhs, do
             }
           }
         }
-        warp_argmax(bk, bi);
-        if (lane == 0) {
-          s_key[warp] = bk;
-          s_idx[warp] = bi;
-        }
+        fp_publish(bk, bi, bv, s_key, s_idx, s_val, warp, lane);
         __syncthreads();
       }
       // is_invertible (full_piv_lu.rs:242-250): U[n-1][n-1] != 0; else report
@@ -224,7 +259,10 @@ __global__ void __launch_bounds__(kFpThreads) fullpiv_kernel(int n, int nrhs, do
       const int z = s_piv[3];
       for (int c = warp; c < solve_cols; c += kFpWarps) {
         double* bc = sb + (size_t)c * ld;
-        if (lane == 0)  // p.permute_rows (permutation_sequence.rs:97-104)
+        // p.permute_rows (permutation_sequence.rs:97-104) and the unit-lower
+        // solve rode along the elimination for its steps; from factors (and
+        // after a stop) they run here, in nalgebra's order
+        if (mode == 2 && lane == 0)
           for (int i = 0; i < n; ++i) {
             const int p = s_ipiv[i];
             if (p != i) {
@@ -234,7 +272,7 @@ __global__ void __launch_bounds__(kFpThreads) fullpiv_kernel(int n, int nrhs, do
             }
           }
         __syncwarp();
-        for (int i = 0; i + 1 < n; ++i) {  // solve_lower_triangular_with_diag_mut(b, 1)
+        for (int i = (mode == 2) ? 0 : steps; i + 1 < n; ++i) {  // solve_lower_triangular_with_diag_mut(b, 1)
           const double coeff = bc[i];
           const double* lc = sa + (size_t)i * ld;
           for (int r = i + 1 + lane; r < n; r += 32) bc[r] = axpy1<EXACT>(bc[r], -coeff, lc[r]);
@@ -274,7 +312,7 @@ __global__ void __launch_bounds__(kFpThreads) fullpiv_kernel(int n, int nrhs, do
         jpiv[(size_t)s * n + i] = s_jpiv[i];
       }
     }
-    if (solve_cols > 0) {
+    if (solve_cols > 0 && inf == 0) {  // not invertible: B stays as given (the ride-along copy is dropped)
       double* b = B + (size_t)s * strideB;
       for (int e = tid; e < n * solve_cols; e += kFpThreads) {
         const int c = e / n, r = e - c * n;

@@ -1123,9 +1123,7 @@ __global__ void to_fp32_kernel(int n, const double* __restrict__ A, int64_t lda,
   }
 }
 
-__device__ __forceinline__ unsigned long long dabs_bits(double x) {
-  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
-}
+__device__ __forceinline__ unsigned long long dabs_bits(double x) { return abs_bits_f64(x); }
 
 // part[cb * n + i] = sum over the column chunk cb of A[i][j] * x[j] (or |A[i][j]| when abs_mode).
 constexpr int kGemvChunks = 16;
