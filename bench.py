@@ -937,6 +937,82 @@ def bench_full_piv_lu_ours(args, rank, world):
     return res
 
 
+def bench_col_piv_qr_ours(args, rank, world):
+    """Batched ColPivQR::new + solve (src/linalg/col_piv_qr.rs:59-92,
+    227-247) on the plain-LU workload: 4096 dense 64x64 systems, one RHS
+    (nacu_dcolpivqr_batched).  Work: 4/3 n^3 (Householder QR of a square
+    matrix) + 3 n^2 (Q^T b and the upper solve) flops per system; FP64
+    roofline."""
+    import time
+
+    import torch
+
+    import oracle as O
+    from nalgebra_gb300 import _lib
+    from nalgebra_gb300 import workloads as W
+
+    L = _lib.load()
+    count, n = 4096, 64
+    a, b = W.dense_lu(count, n, 1, seed=rank)
+    a0 = torch.from_numpy(a).cuda().reshape(-1)
+    b0 = torch.from_numpy(b).cuda().reshape(-1)
+    A, B = a0.clone(), b0.clone()
+    diag = torch.zeros(count * n, dtype=torch.float64, device="cuda")
+    jpiv = torch.zeros(count * n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    flags = 1 if args.exact else 0
+
+    def launch():
+        _lib.call("nacu_dcolpivqr_batched", n, 1, A.data_ptr(), n * n, diag.data_ptr(), jpiv.data_ptr(),
+                  B.data_ptr(), n, info.data_ptr(), count, flags, sp)
+
+    for _ in range(args.warmup):
+        A.copy_(a0); B.copy_(b0); launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            A.copy_(a0); B.copy_(b0); flush.zero_()
+            ev[i][0].record(stream)
+            launch()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+    x = B.cpu().numpy().reshape(count, n)
+    am = a.reshape(count, n, n)
+    bm = b.reshape(count, n)
+    berr = 0.0
+    for s in range(0, count, 256):
+        m = am[s].T  # column-major storage
+        berr = max(berr, float(np.abs(m @ x[s] - bm[s]).max() / (np.abs(m).max() * np.abs(x[s]).max() * n)))
+    flops = count * (4.0 / 3 * n ** 3 + 3.0 * n ** 2)
+    peak = ctypes_probe(L)
+    res = {"metric": "solves/s (batched ColPivQR factor+solve, 4096 x 64x64 f64)", "value": count / (ms * 1e-3),
+           "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (the plain-LU workload: N(0,1) entries plus 64 on the diagonal)",
+           "config": {"workload": "col_piv_qr", "count": count, "n": n, "exact": bool(args.exact),
+                      "l2": "256 MB flush between steps"},
+           "gflops": flops / (ms * 1e-3) / 1e9, "backward_error_sample_in_eps": berr / np.finfo(float).eps,
+           "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak / 1e12,
+                        "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / peak, "traffic": None,
+                        "peak_source": fp64_peak_source()},
+           "gpu_launches": args.steps, "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = 400
+        t0 = time.perf_counter()
+        for s in range(sample):
+            qr, d, jp = O.col_piv_qr(am[s].T)
+            O.col_piv_qr_solve(qr, d, jp, bm[s])
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": sample / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                               "sample": f"{sample} of the {count} systems, oracle ColPivQR new + solve, one thread"}
+    return res
+
+
 # ----------------------------------------------------------------------------- QR least squares
 
 def bench_ls_ours(args, rank, world):
@@ -1257,7 +1333,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
                                                                   "mixed_lu", "lu_inverse", "trsv_batched", "chol_update",
-                                                                        "full_piv_lu"])
+                                                                        "full_piv_lu", "col_piv_qr"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--single-launch", action="store_true",
                     help="ragged_cholesky: one launch over a host-sorted order with the default tile "
@@ -1294,12 +1370,13 @@ def main():
         torch.distributed.barrier()
 
     if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse", "trsv_batched",
-                         "chol_update", "full_piv_lu"):
+                         "chol_update", "full_piv_lu", "col_piv_qr"):
         res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
                "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours,
                "lu_inverse": bench_lu_inverse_ours, "trsv_batched": bench_trsv_ours,
                "chol_update": bench_chol_update_ours,
-               "full_piv_lu": bench_full_piv_lu_ours}[args.workload](args, rank, world)
+               "full_piv_lu": bench_full_piv_lu_ours,
+               "col_piv_qr": bench_col_piv_qr_ours}[args.workload](args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

@@ -120,6 +120,27 @@ int nacu_dfullpivlu_solve_batched(int n, int nrhs, const double* LU, int64_t str
                                   const int32_t* jpiv, double* B, int64_t strideB, int32_t* info, int batch,
                                   int flags, nacu_stream_t stream);
 
+/* ---- QR with column pivoting (batched, n <= 128) --------------------------- */
+
+/* ColPivQR::new (src/linalg/col_piv_qr.rs:59-92) on A + s*strideA (n x n, in
+ * place: the Householder axes at and below the diagonal, R above it),
+ * diag[s*n+i] (QR::new's signed diagonal; R's is |diag|), jpiv[s*n+i] (the
+ * column swapped with i at step i: the column of the trailing submatrix's
+ * largest |a|); with nrhs > 0 (<= 16) ColPivQR::solve_mut (:227-247) on B +
+ * s*strideB (n x nrhs; written even when the solve fails, as nalgebra's b
+ * is).  info[s] = 0 when every diag entry is non-zero (is_invertible,
+ * :307-320; B solved), else 1 + the first zero one.  NACU_FLAG_EXACT:
+ * factors, pivots and solutions bit-identical to nalgebra. */
+int nacu_dcolpivqr_batched(int n, int nrhs, double* A, int64_t strideA, double* diag, int32_t* jpiv, double* B,
+                           int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
+
+/* ColPivQR::solve_mut from factors written by nacu_dcolpivqr_batched (read
+ * only); `qr.try_inverse()` (:288-303) with B = the identity, 16 columns per
+ * call.  info as above. */
+int nacu_dcolpivqr_solve_batched(int n, int nrhs, const double* QR, int64_t strideA, const double* diag,
+                                 const int32_t* jpiv, double* B, int64_t strideB, int32_t* info, int batch, int flags,
+                                 nacu_stream_t stream);
+
 /* Inverse from getrf factors: `lu.try_inverse()` (src/linalg/lu.rs:266-297:
  * out = I, then solve_mut(out)), and with nacu_dgetrf_batched before it
  * `m.try_inverse()` for n > 4 (src/linalg/inverse.rs:135-137).  Ainv + s*strideInv

@@ -35,7 +35,7 @@ from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 __all__ = [
     "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch", "solve_refined", "gemm",
     "PosvLogdet", "cholesky_solve_refined_host",
-    "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE", "FullPivLU",
+    "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE", "FullPivLU", "ColPivQR",
 ]
 
 
@@ -157,6 +157,11 @@ class DeviceMatrix:
         """Matrix::full_piv_lu (src/linalg/decomposition.rs:39-45): factors in
         place (n <= 128)."""
         return FullPivLU(self, flags)
+
+    def col_piv_qr(self, flags: int = 0) -> "ColPivQR":
+        """Matrix::col_piv_qr (src/linalg/decomposition.rs:65-75): factors in
+        place (n <= 128)."""
+        return ColPivQR(self, flags)
 
     def cholesky(self, flags: int = 0, substitute: float | None = None):
         """Matrix::cholesky (decomposition.rs:257-262): Cholesky or None."""
@@ -319,6 +324,76 @@ class FullPivLU:
 
     def u(self) -> np.ndarray:
         return np.triu(self.lu.to_numpy())
+
+
+class ColPivQR:
+    """QR with column pivoting of one square matrix (n <= 128): Householder
+    axes and R in the matrix buffer, the signed diagonal and the column pivots
+    on the device."""
+
+    def __init__(self, m: DeviceMatrix, flags: int = 0):
+        torch = _torch()
+        assert m.is_square(), "the batched column-pivot kernel takes square matrices"
+        n = m.nrows
+        self.qr, self.flags = m, flags
+        self.diag = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
+        self.jpiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
+        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _lib.call("nacu_dcolpivqr_batched", n, 0, m.data.data_ptr(), n * n, self.diag.data_ptr(),
+                  self.jpiv.data_ptr(), 0, 0, self.info.data_ptr(), 1, flags, _stream_ptr())
+
+    def _solve_cols(self, b: DeviceMatrix) -> bool:
+        torch = _torch()
+        n = self.qr.nrows
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        for c0 in range(0, b.ncols, 16):
+            k = min(16, b.ncols - c0)
+            _lib.call("nacu_dcolpivqr_solve_batched", n, k, self.qr.data.data_ptr(), n * n, self.diag.data_ptr(),
+                      self.jpiv.data_ptr(), b.data.data_ptr() + c0 * n * 8, n * k, info.data_ptr(), 1, self.flags,
+                      _stream_ptr())
+        return int(info.item()) == 0
+
+    def solve_mut(self, b: DeviceMatrix) -> bool:
+        """ColPivQR::solve_mut (src/linalg/col_piv_qr.rs:227-247): b is
+        overwritten even when it returns False."""
+        assert b.nrows == self.qr.nrows, "ColPivQR solve matrix dimension mismatch."
+        return self._solve_cols(b)
+
+    def solve(self, b: DeviceMatrix):
+        """ColPivQR::solve (col_piv_qr.rs:205-221): a new matrix, or None."""
+        res = b.clone_owned()
+        return res if self.solve_mut(res) else None
+
+    def try_inverse(self):
+        """ColPivQR::try_inverse (col_piv_qr.rs:288-303)."""
+        torch = _torch()
+        n = self.qr.nrows
+        out = DeviceMatrix(torch.eye(n, dtype=torch.float64, device="cuda").reshape(-1).clone(), n, n)
+        return out if self._solve_cols(out) else None
+
+    def is_invertible(self) -> bool:
+        """ColPivQR::is_invertible (col_piv_qr.rs:307-320)."""
+        return int(self.info.item()) == 0
+
+    def p(self):
+        piv = self.jpiv.cpu().numpy()[: self.qr.nrows]
+        return [(i, int(q)) for i, q in enumerate(piv) if q != i]
+
+    def determinant(self) -> float:
+        """ColPivQR::determinant (col_piv_qr.rs:324-338): the product of diag
+        in order, times the sign of p."""
+        res = 1.0
+        for d in self.diag.cpu().numpy()[: self.qr.nrows]:
+            res *= float(d)
+        return res * (-1.0 if len(self.p()) % 2 else 1.0)
+
+    def r(self) -> np.ndarray:
+        """ColPivQR::r (col_piv_qr.rs:97-110): the upper triangle, |diag| on
+        its diagonal."""
+        n = self.qr.nrows
+        r = np.triu(self.qr.to_numpy())
+        r[np.arange(n), np.arange(n)] = np.abs(self.diag.cpu().numpy()[:n])
+        return r
 
 
 def solve_refined(a: DeviceMatrix, b: DeviceMatrix, tol_units: float = 1.0, max_iter: int = 0):

@@ -44,6 +44,8 @@ SIGNATURES = {
     "nacu_dgetri_batched": (_i, [_i, _vp, _i64, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dfullpivlu_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dfullpivlu_solve_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_dcolpivqr_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_dcolpivqr_solve_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dtrsv_batched": (_i, [_i, _i, _i, _i, _i, _d, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dchol_rank1_update_batched": (_i, [_i, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dchol_remove_column_batched": (_i, [_i, _vp, _i64, _i, _vp, _i64, _i, _i, _vp]),

@@ -1,0 +1,365 @@
+// Batched QR with column pivoting (n <= 128): the GPU form of nalgebra's
+// ColPivQR::new (src/linalg/col_piv_qr.rs:59-92), ColPivQR::solve_mut
+// (:227-247) and, on identity right-hand sides, try_inverse (:288-303).
+//
+// One CTA per system; the matrix and the right-hand sides live in shared
+// memory (column-major, odd leading dimension).  Per step i:
+//   - warp 0 reduces the per-warp candidates to icamax_full's column (the
+//     column of the trailing submatrix's largest |a|, src/base/min_max.rs:
+//     146-167; not the largest column norm), swaps it with column i and turns
+//     column i into the Householder axis (householder::reflection_axis_mut,
+//     householder.rs:19-53: norm, sign rule, two normalisations);
+//   - one warp per trailing column applies the reflection
+//     (reflection.rs:70-83: a dot with the axis, then an axpy with the sign
+//     of the diagonal entry), each lane tracking the largest |a| it wrote for
+//     the next step's pivot; the right-hand sides ride along (q_tr_mul
+//     applies every reflection, even where the column was zero).
+// Two CTA barriers per step.  The upper solve (divide by |diag_i|, stopping
+// where nalgebra's would) and the inverse column permutation then run one
+// warp per right-hand side.  EXACT (NACU_FLAG_EXACT) rounds every operation
+// as Rust does, the dots in dotx's order (src/base/blas.rs:96-165):
+// bit-identical factors, pivots and solutions.  The default form contracts to
+// FMA and reduces the dots across the warp.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace nacu {
+namespace {
+
+constexpr int kCqThreads = 256;
+constexpr int kCqWarps = kCqThreads / 32;
+constexpr int kCqMaxN = 128;
+constexpr int kCqMaxRhs = 16;
+
+struct CqLayout {
+  size_t sa, key, idx, diag, rd, jpiv, flag, total;
+};
+
+__host__ __device__ inline size_t cq_align(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline CqLayout cq_layout(int n, int nrhs) {
+  const int ld = n | 1;
+  CqLayout l;
+  l.sa = 0;
+  l.key = cq_align((size_t)ld * (n + nrhs) * sizeof(double));
+  l.idx = cq_align(l.key + kCqWarps * sizeof(uint64_t));
+  l.diag = cq_align(l.idx + kCqWarps * sizeof(int));
+  l.rd = cq_align(l.diag + (size_t)n * sizeof(double));
+  l.jpiv = cq_align(l.rd + (size_t)n * sizeof(double));
+  l.flag = cq_align(l.jpiv + (size_t)n * sizeof(int));
+  l.total = cq_align(l.flag + 4 * sizeof(int));
+  return l;
+}
+
+template <bool EXACT>
+__device__ __forceinline__ double cq_mul(double a, double b) { return EXACT ? __dmul_rn(a, b) : a * b; }
+template <bool EXACT>
+__device__ __forceinline__ double cq_add(double a, double b) { return EXACT ? __dadd_rn(a, b) : a + b; }
+
+// simba's to_exp for a real: (x, 1) when x >= 0, else (-x, -1) (NaN: -1).
+__device__ __forceinline__ void cq_to_exp(double x, double& modulus, double& sign) {
+  if (x >= 0.0) {
+    modulus = x;
+    sign = 1.0;
+  } else {
+    modulus = -x;
+    sign = -1.0;
+  }
+}
+
+// Rust's f64::signum: +1 for +0 and positives, -1 for -0 and negatives, NaN for NaN.
+__device__ __forceinline__ double cq_signum(double x) { return isnan(x) ? x : (signbit(x) ? -1.0 : 1.0); }
+
+// sum_{e < len} x[e] y[e] in dotx's order (EXACT: eight accumulators over
+// blocks of 8, combined (a0+a4), (a1+a5), (a2+a6), (a3+a7) into 0, then the
+// tail one product at a time) or as a warp reduction; valid in every lane.
+template <bool EXACT>
+__device__ double cq_dot(int len, const double* x, const double* y, int lane) {
+  if constexpr (EXACT) {
+    const int nb = len >> 3;
+    double acc = 0.0;
+    if (lane < 8)
+      for (int b = 0; b < nb; ++b) acc = __dadd_rn(acc, __dmul_rn(x[8 * b + lane], y[8 * b + lane]));
+    const double pair = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, 4));
+    double res = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) res = __dadd_rn(res, __shfl_sync(0xffffffffu, pair, q));
+    for (int e = 8 * nb; e < len; ++e) res = __dadd_rn(res, __dmul_rn(x[e], y[e]));
+    return res;
+  } else {
+    double part = 0.0;
+    for (int e = lane; e < len; e += 32) part = fma(x[e], y[e], part);
+    return warp_sum(part);
+  }
+}
+
+// mode: 0 = factor, 1 = factor + solve, 2 = solve from given factors.
+template <bool EXACT>
+__global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, double* __restrict__ A, int64_t strideA,
+                                                              double* __restrict__ diag, int32_t* __restrict__ jpiv,
+                                                              double* __restrict__ B, int64_t strideB,
+                                                              int32_t* __restrict__ info, int batch, int mode) {
+  extern __shared__ __align__(16) unsigned char cq_smem[];
+  const CqLayout lay = cq_layout(n, nrhs);
+  double* sa = reinterpret_cast<double*>(cq_smem + lay.sa);
+  uint64_t* s_key = reinterpret_cast<uint64_t*>(cq_smem + lay.key);
+  int* s_idx = reinterpret_cast<int*>(cq_smem + lay.idx);
+  double* s_diag = reinterpret_cast<double*>(cq_smem + lay.diag);
+  double* s_rd = reinterpret_cast<double*>(cq_smem + lay.rd);
+  int* s_jpiv = reinterpret_cast<int*>(cq_smem + lay.jpiv);
+  int* s_flag = reinterpret_cast<int*>(cq_smem + lay.flag);  // [0] the step's reflection is not empty
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ld = n | 1;
+  const int solve_cols = (mode == 0) ? 0 : nrhs;
+  const int ncols = n + ((mode == 1) ? nrhs : 0);  // right-hand sides ride along the factorization
+  double* sb = sa + (size_t)ld * n;
+
+  for (int s = blockIdx.x; s < batch; s += gridDim.x) {
+    double* a = A + (size_t)s * strideA;
+    for (int e = tid; e < n * n; e += kCqThreads) {
+      const int c = e / n, r = e - c * n;
+      sa[(size_t)c * ld + r] = a[e];
+    }
+    if (solve_cols > 0) {
+      const double* b = B + (size_t)s * strideB;
+      for (int e = tid; e < n * solve_cols; e += kCqThreads) {
+        const int c = e / n, r = e - c * n;
+        sb[(size_t)c * ld + r] = b[e];
+      }
+    }
+    if (mode == 2)
+      for (int i = tid; i < n; i += kCqThreads) {
+        s_diag[i] = diag[(size_t)s * n + i];
+        s_jpiv[i] = jpiv[(size_t)s * n + i];
+      }
+    __syncthreads();
+
+    if (mode != 2) {
+      uint64_t bkey = 0;
+      int bidx = 0x7fffffff;
+      for (int e = tid; e < n * n; e += kCqThreads) {  // the first search, over the whole matrix
+        const int c = e / n, r = e - c * n;
+        const uint64_t k = pivot_key(sa[(size_t)c * ld + r], e == 0);
+        if (bidx == 0x7fffffff || k > bkey) {
+          bkey = k;
+          bidx = e;
+        }
+      }
+      warp_argmax(bkey, bidx);
+      if (lane == 0) {
+        s_key[warp] = bkey;
+        s_idx[warp] = bidx;
+      }
+      __syncthreads();
+      for (int i = 0; i < n; ++i) {
+        const int L = n - i;
+        if (warp == 0) {
+          uint64_t key = lane < kCqWarps ? s_key[lane] : 0ull;
+          int idx = lane < kCqWarps ? s_idx[lane] : 0x7fffffff;
+          warp_argmax(key, idx);
+          const int cp = i + idx / L;
+          if (cp != i)  // swap_columns(i, cp)
+            for (int r = lane; r < n; r += 32) {
+              const double t = sa[(size_t)i * ld + r];
+              sa[(size_t)i * ld + r] = sa[(size_t)cp * ld + r];
+              sa[(size_t)cp * ld + r] = t;
+            }
+          __syncwarp();
+          // reflection_axis_mut on rows i.. of column i
+          double* x = sa + (size_t)i * ld + i;
+          const double sq = cq_add<EXACT>(0.0, cq_dot<EXACT>(L, x, x, lane));
+          const double nrm = __dsqrt_rn(sq);
+          double modulus, sign;
+          cq_to_exp(x[0], modulus, sign);
+          const double signed_norm = cq_mul<EXACT>(sign, nrm);
+          const double factor = cq_mul<EXACT>(cq_add<EXACT>(sq, cq_mul<EXACT>(modulus, nrm)), 2.0);
+          __syncwarp();
+          if (lane == 0) x[0] = cq_add<EXACT>(x[0], signed_norm);
+          __syncwarp();
+          const bool nz = (factor != 0.0);
+          double rnorm = signed_norm;
+          if (nz) {
+            const double sf = __dsqrt_rn(factor);
+            for (int k = lane; k < L; k += 32) x[k] = __ddiv_rn(x[k], sf);  // unscale_mut
+            __syncwarp();
+            const double n2 = __dsqrt_rn(cq_add<EXACT>(0.0, cq_dot<EXACT>(L, x, x, lane)));  // normalize_mut
+            __syncwarp();
+            for (int k = lane; k < L; k += 32) x[k] = __ddiv_rn(x[k], n2);
+            rnorm = -signed_norm;
+          }
+          if (lane == 0) {
+            s_diag[i] = rnorm;
+            s_jpiv[i] = cp;
+            s_flag[0] = nz ? 1 : 0;
+          }
+        }
+        __syncthreads();
+        // the reflection of the trailing columns, one warp per column
+        const bool nz = s_flag[0] != 0;
+        const double sgn = cq_signum(s_diag[i]);
+        const double m_two = cq_mul<EXACT>(sgn, -2.0);
+        const double* v = sa + (size_t)i * ld + i;
+        const int lm = L - 1;  // the next submatrix is lm x lm
+        uint64_t bk = 0;
+        int bi = 0x7fffffff;
+        for (int c = i + 1 + warp; c < ncols; c += kCqWarps) {
+          double* col = sa + (size_t)c * ld + i;
+          const bool rhs = c >= n;
+          if (nz || rhs) {
+            const double f = cq_mul<EXACT>(cq_dot<EXACT>(L, v, col, lane), m_two);
+            __syncwarp();  // the dot has read the column
+            for (int k = lane; k < L; k += 32)
+              col[k] = EXACT ? __dadd_rn(__dmul_rn(f, v[k]), __dmul_rn(sgn, col[k])) : fma(f, v[k], sgn * col[k]);
+          }
+          if (!rhs) {  // rows i+1.. of this column (each lane reads what it wrote), column-major in the next submatrix
+            const int cl = c - i - 1;
+            for (int k = lane; k < L; k += 32) {
+              if (k == 0) continue;
+              const int e = cl * lm + (k - 1);
+              const uint64_t kk = pivot_key(col[k], e == 0);
+              if (bi == 0x7fffffff || kk > bk) {  // e increases: the first of equal keys stays
+                bk = kk;
+                bi = e;
+              }
+            }
+          }
+          __syncwarp();
+        }
+        warp_argmax(bk, bi);
+        if (lane == 0) {
+          s_key[warp] = bk;
+          s_idx[warp] = bi;
+        }
+        __syncthreads();
+      }
+    }
+
+    // is_invertible (col_piv_qr.rs:307-320): every diag entry non-zero; info =
+    // 1 + the first zero one
+    int inf = 0;
+    for (int i = n - 1; i >= 0; --i)
+      if (s_diag[i] == 0.0) inf = i + 1;
+
+    if (solve_cols > 0) {
+      if constexpr (!EXACT)
+        for (int i = tid; i < n; i += kCqThreads) s_rd[i] = 1.0 / fabs(s_diag[i]);
+      __syncthreads();
+      int zb = -1;  // the first zero |diag_i| from the bottom stops nalgebra's upper solve
+      for (int i = 0; i < n; ++i)
+        if (s_diag[i] == 0.0) zb = i;
+      for (int c = warp; c < solve_cols; c += kCqWarps) {
+        double* bc = sb + (size_t)c * ld;
+        if (mode == 2)  // q_tr_mul (col_piv_qr.rs:180-192): every reflection
+          for (int i = 0; i < n; ++i) {
+            const double sgn = cq_signum(s_diag[i]);
+            const double* v = sa + (size_t)i * ld + i;
+            double* y = bc + i;
+            const double f = cq_mul<EXACT>(cq_dot<EXACT>(n - i, v, y, lane), cq_mul<EXACT>(sgn, -2.0));
+            __syncwarp();
+            for (int k = lane; k < n - i; k += 32)
+              y[k] = EXACT ? __dadd_rn(__dmul_rn(f, v[k]), __dmul_rn(sgn, y[k])) : fma(f, v[k], sgn * y[k]);
+            __syncwarp();
+          }
+        const int lo = (zb < 0) ? 0 : (c == 0 ? zb + 1 : n);
+        for (int i = n - 1; i >= lo; --i) {  // col_piv_qr.rs:250-285
+          const double* uc = sa + (size_t)i * ld;
+          if (lane == 0) bc[i] = EXACT ? __ddiv_rn(bc[i], fabs(s_diag[i])) : bc[i] * s_rd[i];
+          __syncwarp();
+          const double coeff = bc[i];
+          for (int r = lane; r < i; r += 32) bc[r] = axpy1<EXACT>(bc[r], -coeff, uc[r]);
+          __syncwarp();
+        }
+        if (lane == 0)  // p.inv_permute_rows, whatever the upper solve returned
+          for (int k = n - 1; k >= 0; --k) {
+            const int q = s_jpiv[k];
+            if (q != k) {
+              const double t = bc[k];
+              bc[k] = bc[q];
+              bc[q] = t;
+            }
+          }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    if (mode != 2) {
+      for (int e = tid; e < n * n; e += kCqThreads) {
+        const int c = e / n, r = e - c * n;
+        a[e] = sa[(size_t)c * ld + r];
+      }
+      for (int i = tid; i < n; i += kCqThreads) {
+        diag[(size_t)s * n + i] = s_diag[i];
+        jpiv[(size_t)s * n + i] = s_jpiv[i];
+      }
+    }
+    if (solve_cols > 0) {  // nalgebra overwrites b even when the upper solve fails
+      double* b = B + (size_t)s * strideB;
+      for (int e = tid; e < n * solve_cols; e += kCqThreads) {
+        const int c = e / n, r = e - c * n;
+        b[e] = sb[(size_t)c * ld + r];
+      }
+    }
+    if (tid == 0 && info) info[s] = inf;
+    __syncthreads();
+  }
+}
+
+int colpivqr_launch(int n, int nrhs, double* A, int64_t strideA, double* diag, int32_t* jpiv, double* B,
+                    int64_t strideB, int32_t* info, int batch, int flags, int mode, cudaStream_t stream,
+                    const char* name) {
+  const size_t smem = cq_layout(n, nrhs).total;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  auto kern = (flags & NACU_FLAG_EXACT) ? colpivqr_kernel<true> : colpivqr_kernel<false>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return record_cuda_error(e, name);
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCqThreads, smem);
+  // persistent: as many CTAs as fit at once, each taking systems grid-stride
+  const int grid = std::max(1, std::min(batch, std::max(1, per_sm) * std::max(1, nsm)));
+  kern<<<grid, kCqThreads, smem, stream>>>(n, nrhs, A, strideA, diag, jpiv, B, strideB, info, batch, mode);
+  return check_launch(name);
+}
+
+}  // namespace
+}  // namespace nacu
+
+using namespace nacu;
+
+extern "C" {
+
+int nacu_dcolpivqr_batched(int n, int nrhs, double* A, int64_t strideA, double* diag, int32_t* jpiv, double* B,
+                           int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream) {
+  const char* name = "nacu_dcolpivqr_batched";
+  if (n < 0 || n > kCqMaxN) return record_arg_error(-1, "col-pivot QR batched: n out of range [0, 128]");
+  if (nrhs < 0 || nrhs > kCqMaxRhs) return record_arg_error(-2, "col-pivot QR batched: nrhs out of range [0, 16]");
+  if (batch < 0) return record_arg_error(-10, "col-pivot QR batched: negative batch");
+  if (batch == 0 || n == 0) return NACU_SUCCESS;
+  if (!A || !diag || !jpiv || (nrhs > 0 && !B)) return record_arg_error(-3, "col-pivot QR batched: null pointer");
+  if (strideA < (int64_t)n * n) return record_arg_error(-4, "col-pivot QR batched: strideA < n*n");
+  if (nrhs > 0 && strideB < (int64_t)n * nrhs) return record_arg_error(-8, "col-pivot QR batched: strideB < n*nrhs");
+  return colpivqr_launch(n, nrhs, A, strideA, diag, jpiv, B, strideB, info, batch, flags, nrhs > 0 ? 1 : 0,
+                         (cudaStream_t)stream, name);
+}
+
+int nacu_dcolpivqr_solve_batched(int n, int nrhs, const double* QR, int64_t strideA, const double* diag,
+                                 const int32_t* jpiv, double* B, int64_t strideB, int32_t* info, int batch, int flags,
+                                 nacu_stream_t stream) {
+  const char* name = "nacu_dcolpivqr_solve_batched";
+  if (n < 0 || n > kCqMaxN) return record_arg_error(-1, "col-pivot QR solve: n out of range [0, 128]");
+  if (nrhs < 0 || nrhs > kCqMaxRhs) return record_arg_error(-2, "col-pivot QR solve: nrhs out of range [0, 16]");
+  if (batch < 0) return record_arg_error(-10, "col-pivot QR solve: negative batch");
+  if (batch == 0 || n == 0 || nrhs == 0) return NACU_SUCCESS;
+  if (!QR || !diag || !jpiv || !B) return record_arg_error(-3, "col-pivot QR solve: null pointer");
+  if (strideA < (int64_t)n * n) return record_arg_error(-4, "col-pivot QR solve: strideA < n*n");
+  if (strideB < (int64_t)n * nrhs) return record_arg_error(-8, "col-pivot QR solve: strideB < n*nrhs");
+  // mode 2 reads the factors, diag and pivots and writes only B and info
+  return colpivqr_launch(n, nrhs, const_cast<double*>(QR), strideA, const_cast<double*>(diag),
+                         const_cast<int32_t*>(jpiv), B, strideB, info, batch, flags, 2, (cudaStream_t)stream, name);
+}
+
+}  // extern "C"

@@ -52,6 +52,8 @@ def lib():
             "orc_dgetrs": (C.c_int, [_i64, _dp, _i64, _i32p, _dp, _i64, _i64]),
             "orc_dlu_determinant": (C.c_double, [_i64, _dp, _i64, _i64]),
             "orc_dfullpivlu": (_i64, [_i64, _i64, _dp, _i64, _i32p, _i32p]),
+            "orc_dcolpivqr": (None, [_i64, _i64, _dp, _i64, _dp, _i32p]),
+            "orc_dcolpivqr_solve": (C.c_int, [_i64, _dp, _i64, _dp, _i32p, _dp, _i64, _i64]),
             "orc_dfullpivlu_solve": (C.c_int, [_i64, _dp, _i64, _i32p, _i32p, _dp, _i64, _i64]),
             "orc_dtrsv": (C.c_int, [_i64, _dp, _i64, _dp, _i64, _i64, C.c_int, C.c_int, C.c_int, C.c_double]),
             "orc_dchol_rank1": (None, [_i64, _dp, _i64, _dp, C.c_double]),
@@ -166,6 +168,43 @@ def full_piv_lu_determinant(lu_, ipiv, jpiv):
         res *= float(lu_[i, i])
     swaps = int(np.sum(np.asarray(ipiv) != np.arange(n))) + int(np.sum(np.asarray(jpiv) != np.arange(n)))
     return res * (-1.0 if swaps % 2 else 1.0)
+
+
+def col_piv_qr(a):
+    """ColPivQR::new (src/linalg/col_piv_qr.rs:59-92).  Returns (packed factor:
+    reflector axes at and below the diagonal, R above it; diag; jpiv)."""
+    a = np.array(a, dtype=np.float64, order="F", copy=True)
+    m, n = a.shape
+    diag = np.zeros(min(m, n))
+    jpiv = np.zeros(min(m, n), dtype=np.int32)
+    lib().orc_dcolpivqr(m, n, _p(a), max(m, 1), _p(diag), _p(jpiv, _i32p))
+    return a, diag, jpiv
+
+
+def col_piv_qr_solve(qr_, diag, jpiv, b):
+    """ColPivQR::solve_mut (col_piv_qr.rs:227-247) on a copy of b.  Returns
+    (x, solved): nalgebra overwrites b even when it returns false."""
+    qr_ = _f64(qr_)
+    n = qr_.shape[0]
+    x = np.array(b, dtype=np.float64, order="F", copy=True)
+    x2 = x.reshape(n, -1, order="F")
+    ok = lib().orc_dcolpivqr_solve(n, _p(qr_), max(n, 1), _p(np.ascontiguousarray(diag, dtype=np.float64)),
+                                   _p(np.ascontiguousarray(jpiv, dtype=np.int32), _i32p), _p(x2), max(n, 1),
+                                   x2.shape[1])
+    return x, bool(ok)
+
+
+def col_piv_qr_q_r(qr_, diag):
+    """(Q, R) of ColPivQR::unpack (col_piv_qr.rs:97-173): Q from q_tr_mul on the
+    identity, R the upper triangle with |diag| on its diagonal."""
+    qr_ = _f64(qr_)
+    m, n = qr_.shape
+    qt = np.asfortranarray(np.eye(m))
+    lib().orc_dqr_q_tr_mul(m, n, _p(qr_), max(m, 1), _p(np.ascontiguousarray(diag, dtype=np.float64)), _p(qt),
+                           max(m, 1), m)
+    r = np.triu(qr_[: min(m, n), :])
+    r[np.arange(len(diag)), np.arange(len(diag))] = np.abs(diag)
+    return qt.T[:, : min(m, n)], r
 
 
 def cholesky_rank_one_update(l, x, sigma):

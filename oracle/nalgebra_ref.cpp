@@ -47,6 +47,13 @@ int orc_dfullpivlu_solve(int64_t n, const double* lu, int64_t lda, const int32_t
                          double* b, int64_t ldb, int64_t nrhs) {
   return orc::full_piv_lu_solve<double>(n, lu, lda, ipiv, jpiv, b, ldb, nrhs) ? 1 : 0;
 }
+void orc_dcolpivqr(int64_t m, int64_t n, double* a, int64_t lda, double* diag, int32_t* jpiv) {
+  orc::col_piv_qr_factor<double>(m, n, a, lda, diag, jpiv);
+}
+int orc_dcolpivqr_solve(int64_t n, const double* qr, int64_t lda, const double* diag, const int32_t* jpiv,
+                        double* b, int64_t ldb, int64_t nrhs) {
+  return orc::col_piv_qr_solve<double>(n, qr, lda, diag, jpiv, b, ldb, nrhs) ? 1 : 0;
+}
 double orc_dlu_determinant(int64_t n, const double* lu, int64_t lda, int64_t len) {
   return orc::lu_determinant<double>(n, lu, lda, len);
 }

@@ -588,6 +588,68 @@ inline void qr_q_tr_mul(std::size_t m, std::size_t n, const T* qr, std::size_t l
     reflect_with_sign(m - i, qr + i + i * lda, nrhs, b + i, ldb, signum(diag[i]));
 }
 
+// ColPivQR::new (src/linalg/col_piv_qr.rs:59-92): per step the column of
+// icamax_full over the trailing submatrix (its largest |a|, min_max.rs:146-167),
+// the column swap, then clear_column_unchecked as QR::new.  jpiv[i] is the
+// column swapped with i at step i (i when none); diag as QR::new's.
+template <class T>
+inline void col_piv_qr_factor(std::size_t m, std::size_t n, T* a, std::size_t lda, T* diag, int32_t* jpiv) {
+  const std::size_t mn = m < n ? m : n;
+  for (std::size_t i = 0; i < mn; ++i) {
+    std::size_t r, c;
+    icamax_full(m - i, n - i, a + i + i * lda, lda, &r, &c);
+    const std::size_t col_piv = c + i;
+    if (col_piv != i)
+      for (std::size_t k = 0; k < m; ++k) {  // swap_columns(i, col_piv)
+        T t = a[k + i * lda];
+        a[k + i * lda] = a[k + col_piv * lda];
+        a[k + col_piv * lda] = t;
+      }
+    jpiv[i] = (int32_t)col_piv;
+    bool not_zero;
+    T* axis = a + i + i * lda;
+    const T rnorm = reflection_axis(m - i, axis, &not_zero);
+    if (not_zero) reflect_with_sign(m - i, axis, n - i - 1, axis + lda, lda, signum(rnorm));
+    diag[i] = rnorm;
+  }
+}
+
+// ColPivQR::solve_mut (col_piv_qr.rs:227-247) for an n x n factor: q_tr_mul
+// (:180-192, every reflection, with the sign of its diag entry), the upper
+// solve of :250-285 (divide by |diag_i|; a zero one returns false at once,
+// that column partly and the later ones not solved), then p.inv_permute_rows
+// whatever the upper solve returned.  Returns the upper solve's result.
+template <class T>
+inline bool col_piv_qr_solve(std::size_t n, const T* qr, std::size_t lda, const T* diag, const int32_t* jpiv, T* b,
+                             std::size_t ldb, std::size_t nrhs) {
+  for (std::size_t i = 0; i < n; ++i)
+    reflect_with_sign(n - i, qr + i + i * lda, nrhs, b + i, ldb, signum(diag[i]));
+  bool solved = true;
+  for (std::size_t c = 0; c < nrhs && solved; ++c) {
+    T* bc = b + c * ldb;
+    for (std::size_t ii = n; ii-- > 0;) {
+      const T d = std::fabs(diag[ii]);
+      if (d == T(0)) {
+        solved = false;
+        break;
+      }
+      const T coeff = bc[ii] / d;
+      bc[ii] = coeff;
+      axpy(ii, -coeff, qr + ii * lda, T(1), bc);
+    }
+  }
+  for (std::size_t k = n; k-- > 0;) {
+    const std::size_t q = (std::size_t)jpiv[k];
+    if (q != k)
+      for (std::size_t c = 0; c < nrhs; ++c) {
+        T t = b[k + c * ldb];
+        b[k + c * ldb] = b[q + c * ldb];
+        b[q + c * ldb] = t;
+      }
+  }
+  return solved;
+}
+
 // Least squares x = argmin ||A x - b|| for m >= n from the factors: Q^T b
 // (qr.rs:157-171), then the back substitution of qr.rs:224-256 (divide by
 // |diag_i|, axpy with the strict upper part of R) restricted to the top n rows,

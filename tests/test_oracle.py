@@ -396,3 +396,58 @@ def test_full_piv_lu_matches_pure_python_restatement_bitwise(n):
     assert steps == steps2
     assert np.array_equal(ipiv, ipiv2) and np.array_equal(jpiv, jpiv2)
     assert np.array_equal(lu, lu2)
+
+
+def _colpiv_reconstruct(qr, diag, jpiv):
+    q, r = O.col_piv_qr_q_r(qr, diag)
+    return q, _inv_permute_columns(q @ r, jpiv)
+
+
+def test_col_piv_qr_known_answer():
+    """tests/linalg/col_piv_qr.rs:5-21: the (singular) 4x4 matrix has a zero
+    determinant to 1e-7 and Q R P^-1 reconstructs it."""
+    k = _known()["col_piv_qr"]
+    m = _rows(k["rows"])
+    qr, diag, jpiv = O.col_piv_qr(m)
+    det = float(np.prod(diag)) * (-1.0 if int(np.sum(jpiv != np.arange(4))) % 2 else 1.0)
+    assert abs(det - k["determinant"]) <= k["determinant_epsilon"]
+    q, rec = _colpiv_reconstruct(qr, diag, jpiv)
+    assert np.allclose(rec, m, atol=k["reconstruction_epsilon"], rtol=0)
+    assert np.allclose(q.T @ q, np.eye(4), atol=1e-7, rtol=0)
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (5, 5), (9, 4), (4, 9), (30, 30)])
+def test_col_piv_qr_properties(m, n):
+    """tests/linalg/col_piv_qr.rs:40-80: Q R P^-1 = m and Q orthogonal (1e-7);
+    for square systems solve gives m x = b."""
+    rng = np.random.default_rng(600 + 7 * m + n)
+    a = rng.uniform(-100, 100, size=(m, n))
+    qr, diag, jpiv = O.col_piv_qr(a)
+    q, rec = _colpiv_reconstruct(qr, diag, jpiv)
+    assert np.allclose(rec, a, atol=1e-7, rtol=0)
+    assert np.allclose(q.T @ q, np.eye(min(m, n)), atol=1e-7, rtol=0)
+    if m == n:
+        b = rng.standard_normal((n, 2))
+        x, ok = O.col_piv_qr_solve(qr, diag, jpiv, b)
+        assert ok and np.allclose(a @ x, b, atol=1e-9, rtol=0)
+
+
+def test_col_piv_qr_pivots_on_the_largest_entry():
+    """The pivot column holds the trailing submatrix's largest |a| (icamax_full),
+    not the largest column norm: column 1 has the larger norm, column 0 the
+    larger entry."""
+    a = np.array([[5.0, 3.0], [0.0, 3.0]])
+    _, _, jpiv = O.col_piv_qr(a)
+    assert jpiv[0] == 0
+    a = np.array([[1.0, 3.0], [1.0, 3.0]])
+    _, _, jpiv = O.col_piv_qr(a)
+    assert jpiv[0] == 1
+
+
+def test_col_piv_qr_zero_column_and_failed_solve():
+    """A zero matrix: no reflection (diag = +/-0), the solve returns false after
+    q_tr_mul and the inverse permutation, with b still overwritten."""
+    qr, diag, jpiv = O.col_piv_qr(np.zeros((3, 3)))
+    assert np.all(diag == 0)
+    x, ok = O.col_piv_qr_solve(qr, diag, jpiv, np.array([1.0, 2.0, 3.0]))
+    assert not ok
