@@ -9,12 +9,14 @@
 //     146-167; not the largest column norm), swaps it with column i and turns
 //     column i into the Householder axis (householder::reflection_axis_mut,
 //     householder.rs:19-53: norm, sign rule, two normalisations);
-//   - one warp per trailing column applies the reflection
-//     (reflection.rs:70-83: a dot with the axis, then an axpy with the sign
-//     of the diagonal entry), each lane tracking the largest |a| it wrote for
-//     the next step's pivot; the right-hand sides ride along (q_tr_mul
-//     applies every reflection, even where the column was zero).
-// Two CTA barriers per step.  The upper solve (divide by |diag_i|, stopping
+//   - the reflection of the trailing columns (reflection.rs:70-83): one
+//     thread per column forms its factor (a dot with the axis, sequential, so
+//     no warp reductions spend FP64 adds), then all threads apply the axpys
+//     as one flattened update, one FMA per element with the sign folded in,
+//     each tracking the largest |a| it wrote for the next step's pivot; the
+//     right-hand sides ride along (q_tr_mul applies every reflection, even
+//     where the column was zero).
+// Three CTA barriers per step.  The upper solve (divide by |diag_i|, stopping
 // where nalgebra's would) and the inverse column permutation then run one
 // warp per right-hand side.  EXACT (NACU_FLAG_EXACT) rounds every operation
 // as Rust does, the dots in dotx's order (src/base/blas.rs:96-165):
@@ -33,7 +35,7 @@ constexpr int kCqMaxN = 128;
 constexpr int kCqMaxRhs = 16;
 
 struct CqLayout {
-  size_t sa, key, idx, diag, rd, jpiv, flag, total;
+  size_t sa, key, idx, diag, rd, f, jpiv, flag, total;
 };
 
 __host__ __device__ inline size_t cq_align(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -46,7 +48,8 @@ __host__ __device__ inline CqLayout cq_layout(int n, int nrhs) {
   l.idx = cq_align(l.key + kCqWarps * sizeof(uint64_t));
   l.diag = cq_align(l.idx + kCqWarps * sizeof(int));
   l.rd = cq_align(l.diag + (size_t)n * sizeof(double));
-  l.jpiv = cq_align(l.rd + (size_t)n * sizeof(double));
+  l.f = cq_align(l.rd + (size_t)n * sizeof(double));
+  l.jpiv = cq_align(l.f + (size_t)(n + nrhs) * sizeof(double));
   l.flag = cq_align(l.jpiv + (size_t)n * sizeof(int));
   l.total = cq_align(l.flag + 4 * sizeof(int));
   return l;
@@ -94,6 +97,45 @@ __device__ double cq_dot(int len, const double* x, const double* y, int lane) {
   }
 }
 
+// The same sum by one thread: dotx's order in EXACT, four interleaved
+// accumulators otherwise.
+template <bool EXACT>
+__device__ __forceinline__ double cq_dot_seq(int len, const double* x, const double* y) {
+  if constexpr (EXACT) {
+    double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const int nb = len >> 3;
+    for (int b = 0; b < nb; ++b)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) a[q] = __dadd_rn(a[q], __dmul_rn(x[8 * b + q], y[8 * b + q]));
+    double res = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) res = __dadd_rn(res, __dadd_rn(a[q], a[q + 4]));
+    for (int e = 8 * nb; e < len; ++e) res = __dadd_rn(res, __dmul_rn(x[e], y[e]));
+    return res;
+  } else {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int e = 0;
+    for (; e + 4 <= len; e += 4) {
+      a0 = fma(x[e], y[e], a0);
+      a1 = fma(x[e + 1], y[e + 1], a1);
+      a2 = fma(x[e + 2], y[e + 2], a2);
+      a3 = fma(x[e + 3], y[e + 3], a3);
+    }
+    for (; e < len; ++e) a0 = fma(x[e], y[e], a0);
+    return (a0 + a1) + (a2 + a3);
+  }
+}
+
+// -x by flipping the sign bit with integer instructions (no FP64 slot).
+__device__ __forceinline__ double neg_bits(double x) {
+  unsigned lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+  hi ^= 0x80000000u;
+  double r;
+  asm("mov.b64 %0, {%1, %2};" : "=d"(r) : "r"(lo), "r"(hi));
+  return r;
+}
+
 // mode: 0 = factor, 1 = factor + solve, 2 = solve from given factors.
 template <bool EXACT>
 __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, double* __restrict__ A, int64_t strideA,
@@ -107,6 +149,7 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
   int* s_idx = reinterpret_cast<int*>(cq_smem + lay.idx);
   double* s_diag = reinterpret_cast<double*>(cq_smem + lay.diag);
   double* s_rd = reinterpret_cast<double*>(cq_smem + lay.rd);
+  double* s_f = reinterpret_cast<double*>(cq_smem + lay.f);  // the step's reflection factor per trailing column
   int* s_jpiv = reinterpret_cast<int*>(cq_smem + lay.jpiv);
   int* s_flag = reinterpret_cast<int*>(cq_smem + lay.flag);  // [0] the step's reflection is not empty
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -195,36 +238,60 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
           }
         }
         __syncthreads();
-        // the reflection of the trailing columns, one warp per column
+        // the reflection of the trailing columns (reflect_with_sign, bias 0):
+        // first every column's factor (its dot with the axis, one thread per
+        // column), then the axpys as one flattened update
         const bool nz = s_flag[0] != 0;
         const double sgn = cq_signum(s_diag[i]);
         const double m_two = cq_mul<EXACT>(sgn, -2.0);
         const double* v = sa + (size_t)i * ld + i;
+        const int ntr = ncols - i - 1;
+        for (int t = tid; t < ntr; t += kCqThreads) {
+          const int c = i + 1 + t;
+          double f = 0.0;
+          if (nz || c >= n) f = cq_mul<EXACT>(cq_dot_seq<EXACT>(L, v, sa + (size_t)c * ld + i), m_two);
+          s_f[t] = f;
+        }
+        __syncthreads();
         const int lm = L - 1;  // the next submatrix is lm x lm
         uint64_t bk = 0;
         int bi = 0x7fffffff;
-        for (int c = i + 1 + warp; c < ncols; c += kCqWarps) {
-          double* col = sa + (size_t)c * ld + i;
-          const bool rhs = c >= n;
-          if (nz || rhs) {
-            const double f = cq_mul<EXACT>(cq_dot<EXACT>(L, v, col, lane), m_two);
-            __syncwarp();  // the dot has read the column
-            for (int k = lane; k < L; k += 32)
-              col[k] = EXACT ? __dadd_rn(__dmul_rn(f, v[k]), __dmul_rn(sgn, col[k])) : fma(f, v[k], sgn * col[k]);
-          }
-          if (!rhs) {  // rows i+1.. of this column (each lane reads what it wrote), column-major in the next submatrix
-            const int cl = c - i - 1;
-            for (int k = lane; k < L; k += 32) {
-              if (k == 0) continue;
-              const int e = cl * lm + (k - 1);
-              const uint64_t kk = pivot_key(col[k], e == 0);
-              if (bi == 0x7fffffff || kk > bk) {  // e increases: the first of equal keys stays
+        if (ntr > 0) {
+          const int total = L * ntr;
+          int e = tid;
+          int cq = e / L;
+          int rr = e - cq * L;
+          const int dq = kCqThreads / L, dr = kCqThreads - dq * L;
+          for (; e < total; e += kCqThreads) {
+            const int c = i + 1 + cq;
+            double* col = sa + (size_t)c * ld + i;
+            double val = col[rr];
+            if (nz || c >= n) {
+              const double f = s_f[cq];
+              if constexpr (EXACT) {
+                val = __dadd_rn(__dmul_rn(f, v[rr]), __dmul_rn(sgn, val));
+              } else {
+                // sgn * col + f * v with the sign folded into one FMA
+                val = (sgn == 1.0) ? fma(f, v[rr], val)
+                                   : (sgn == -1.0 ? neg_bits(fma(-f, v[rr], val)) : fma(f, v[rr], sgn * val));
+              }
+              col[rr] = val;
+            }
+            if (c < n && rr > 0) {  // rows i+1.. of the matrix columns, column-major in the next submatrix
+              const int en = cq * lm + (rr - 1);  // increases with e: the first of equal keys stays
+              const uint64_t kk = pivot_key(val, en == 0);
+              if (bi == 0x7fffffff || kk > bk) {
                 bk = kk;
-                bi = e;
+                bi = en;
               }
             }
+            rr += dr;
+            cq += dq;
+            if (rr >= L) {
+              rr -= L;
+              ++cq;
+            }
           }
-          __syncwarp();
         }
         warp_argmax(bk, bi);
         if (lane == 0) {
