@@ -30,6 +30,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _lib
+from . import factor_format
 from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 
 __all__ = [
@@ -250,6 +251,25 @@ class LU:
     def u(self) -> np.ndarray:
         return np.triu(self.lu.to_numpy())
 
+    def to_json(self) -> str:
+        """nalgebra's serde JSON form of LU (src/linalg/lu.rs:14-38)."""
+        return factor_format.lu_to_json(self.lu.to_numpy(), self.ipiv.cpu().numpy()[: self.lu.nrows])
+
+    @classmethod
+    def from_json(cls, s: str, flags: int = 0) -> "LU":
+        """An LU from nalgebra's serde JSON form, its factors on the device."""
+        torch = _torch()
+        lu, ipiv = factor_format.lu_from_json(s)
+        n = lu.shape[0]
+        obj = cls.__new__(cls)
+        obj.lu, obj.flags, obj.large = DeviceMatrix.from_numpy(lu), flags, n > 128
+        obj.ipiv = torch.from_numpy(np.resize(ipiv.astype(np.int32), max(n, 1))).cuda()
+        zero = np.nonzero(np.diag(lu) == 0)[0]
+        obj.info = torch.tensor([int(zero[0]) + 1 if len(zero) else 0, 0], dtype=torch.int32, device="cuda")
+        if obj.large:
+            obj._ws = torch.empty(_lib.load().nacu_getrf_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+        return obj
+
 
 class FullPivLU:
     """LU with full pivoting of one square matrix (n <= 128): packed L\\U in
@@ -325,6 +345,28 @@ class FullPivLU:
     def u(self) -> np.ndarray:
         return np.triu(self.lu.to_numpy())
 
+    def to_json(self) -> str:
+        """nalgebra's serde JSON form of FullPivLU (src/linalg/full_piv_lu.rs:14-39)."""
+        n = self.lu.nrows
+        return factor_format.full_piv_lu_to_json(self.lu.to_numpy(), self.ipiv.cpu().numpy()[:n],
+                                                 self.jpiv.cpu().numpy()[:n])
+
+    @classmethod
+    def from_json(cls, s: str, flags: int = 0) -> "FullPivLU":
+        """A FullPivLU from nalgebra's serde JSON form; info is 0 when
+        U[n-1][n-1] != 0, else 1 + the first zero U_ii."""
+        torch = _torch()
+        lu, ipiv, jpiv = factor_format.full_piv_lu_from_json(s)
+        n = lu.shape[0]
+        obj = cls.__new__(cls)
+        obj.lu, obj.flags = DeviceMatrix.from_numpy(lu), flags
+        obj.ipiv = torch.from_numpy(np.resize(ipiv.astype(np.int32), max(n, 1))).cuda()
+        obj.jpiv = torch.from_numpy(np.resize(jpiv.astype(np.int32), max(n, 1))).cuda()
+        zero = np.nonzero(np.diag(lu) == 0)[0]
+        inv = n == 0 or lu[n - 1, n - 1] != 0
+        obj.info = torch.tensor([0 if inv else int(zero[0]) + 1], dtype=torch.int32, device="cuda")
+        return obj
+
 
 class ColPivQR:
     """QR with column pivoting of one square matrix (n <= 128): Householder
@@ -394,6 +436,26 @@ class ColPivQR:
         r = np.triu(self.qr.to_numpy())
         r[np.arange(n), np.arange(n)] = np.abs(self.diag.cpu().numpy()[:n])
         return r
+
+    def to_json(self) -> str:
+        """nalgebra's serde JSON form of ColPivQR (src/linalg/col_piv_qr.rs:14-43)."""
+        n = self.qr.nrows
+        return factor_format.col_piv_qr_to_json(self.qr.to_numpy(), self.jpiv.cpu().numpy()[:n],
+                                                self.diag.cpu().numpy()[:n])
+
+    @classmethod
+    def from_json(cls, s: str, flags: int = 0) -> "ColPivQR":
+        """A ColPivQR from nalgebra's serde JSON form."""
+        torch = _torch()
+        qr, jpiv, diag = factor_format.col_piv_qr_from_json(s)
+        n = qr.shape[0]
+        obj = cls.__new__(cls)
+        obj.qr, obj.flags = DeviceMatrix.from_numpy(qr), flags
+        obj.diag = torch.from_numpy(np.resize(diag, max(n, 1))).cuda()
+        obj.jpiv = torch.from_numpy(np.resize(jpiv.astype(np.int32), max(n, 1))).cuda()
+        zero = np.nonzero(diag == 0)[0]
+        obj.info = torch.tensor([int(zero[0]) + 1 if len(zero) else 0], dtype=torch.int32, device="cuda")
+        return obj
 
 
 def solve_refined(a: DeviceMatrix, b: DeviceMatrix, tol_units: float = 1.0, max_iter: int = 0):
@@ -568,6 +630,15 @@ class Cholesky:
 
     def l(self) -> np.ndarray:
         return np.tril(self.chol.to_numpy())
+
+    def to_json(self) -> str:
+        """nalgebra's serde JSON form of Cholesky (src/linalg/cholesky.rs:15-33)."""
+        return factor_format.cholesky_to_json(self.chol.to_numpy())
+
+    @classmethod
+    def from_json(cls, s: str, flags: int = 0) -> "Cholesky":
+        """A Cholesky from nalgebra's serde JSON form, its factor on the device."""
+        return cls._from_factor(DeviceMatrix.from_numpy(factor_format.cholesky_from_json(s)), flags)
 
 
 class DeviceBatch:
