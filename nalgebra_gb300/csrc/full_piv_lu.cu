@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kFpThreads, 5) fullpiv_kernel(int n, int nrhs,
   uint64_t* s_key = reinterpret_cast<uint64_t*>(fp_smem + lay.key);
   double* s_val = reinterpret_cast<double*>(fp_smem + lay.val);
   int* s_idx = reinterpret_cast<int*>(fp_smem + lay.idx);
-  int* s_piv = reinterpret_cast<int*>(fp_smem + lay.piv);  // [0] row, [1] column pivot, [2] steps, [3] zero-diagonal row
+  int* s_piv = reinterpret_cast<int*>(fp_smem + lay.piv);  // [3]: the solve's last zero U_ii from the bottom
   int* s_ipiv = reinterpret_cast<int*>(fp_smem + lay.ipiv);
   int* s_jpiv = reinterpret_cast<int*>(fp_smem + lay.jpiv);
   double* s_rd = reinterpret_cast<double*>(fp_smem + lay.rd);
