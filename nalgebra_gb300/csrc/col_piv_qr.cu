@@ -254,6 +254,8 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
         }
         __syncthreads();
         const int lm = L - 1;  // the next submatrix is lm x lm
+        // the sign's case, decided once: FP64 compares run on the FP64 pipe
+        const int smode = (sgn == 1.0) ? 0 : (sgn == -1.0 ? 1 : 2);
         uint64_t bk = 0;
         int bi = 0x7fffffff;
         if (ntr > 0) {
@@ -272,8 +274,8 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
                 val = __dadd_rn(__dmul_rn(f, v[rr]), __dmul_rn(sgn, val));
               } else {
                 // sgn * col + f * v with the sign folded into one FMA
-                val = (sgn == 1.0) ? fma(f, v[rr], val)
-                                   : (sgn == -1.0 ? neg_bits(fma(-f, v[rr], val)) : fma(f, v[rr], sgn * val));
+                val = (smode == 0) ? fma(f, v[rr], val)
+                                   : (smode == 1 ? neg_bits(fma(-f, v[rr], val)) : fma(f, v[rr], sgn * val));
               }
               col[rr] = val;
             }
