@@ -107,6 +107,27 @@ def dist_env():
     return rank, world, local
 
 
+def combine_over_ranks(res, units, world, device="cuda"):
+    """Whole-job figures of `world` independent replicas that each process
+    `units` per step: the slowest rank's time per step (MAX over ranks), for
+    the device-timed figure and for the end-to-end one, and units * world over
+    that time.  Every rank must call it (a collective)."""
+    if world <= 1:
+        return res
+    import torch
+
+    e2e = res.get("e2e") or {}
+    t = torch.tensor([float(res["ms_per_step"]), float(e2e.get("ms_per_step", 0.0))], dtype=torch.float64,
+                     device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    res["ms_per_step"] = float(t[0])
+    res["value"] = units * world / (res["ms_per_step"] * 1e-3)
+    if e2e.get("ms_per_step"):
+        e2e["ms_per_step"] = float(t[1])
+        e2e["value"] = units * world / (e2e["ms_per_step"] * 1e-3)
+    return res
+
+
 # ----------------------------------------------------------------------------- ragged Cholesky
 
 RAGGED = dict(count=20000, n_lo=8, n_hi=256, nrhs=4, seed=0)
@@ -351,7 +372,7 @@ def bench_ragged_ours(args, rank, world):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": kern_ms,
+        "ms_per_step": head_ms,  # the time of the form `value` reports
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -1385,11 +1406,7 @@ def main():
     if args.profile:
         print(json.dumps(res))
         return
-    if world > 1:
-        t = torch.tensor([res["ms_per_step"]], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        res["ms_per_step"] = float(t.item())
-        res["value"] = RAGGED["count"] * world / (res["ms_per_step"] * 1e-3)
+    res = combine_over_ranks(res, res["config"]["count"], world)
     if rank == 0:
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = cpu_baseline_ragged(data)
