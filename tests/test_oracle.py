@@ -451,3 +451,75 @@ def test_col_piv_qr_zero_column_and_failed_solve():
     assert np.all(diag == 0)
     x, ok = O.col_piv_qr_solve(qr, diag, jpiv, np.array([1.0, 2.0, 3.0]))
     assert not ok
+
+
+def _pure_python_rank_one_update(l, x, sigma):
+    """Independent pure-Python restatement of xx_rank_one_update
+    (src/linalg/cholesky.rs:404-449) on the lower part of l."""
+    import math
+
+    n = len(x)
+    l = [[float(l[r][c]) for c in range(n)] for r in range(n)]
+    x = [float(v) for v in x]
+    beta = 1.0
+    for j in range(n):
+        diag = l[j][j]
+        diag2 = diag * diag
+        xj = x[j]
+        sigma_xj2 = sigma * (xj * xj)
+        gamma = diag2 * beta + sigma_xj2
+        new_diag = math.sqrt(diag2 + sigma_xj2 / beta)
+        l[j][j] = new_diag
+        beta += sigma_xj2 / diag2
+        a1 = -xj / diag
+        for r in range(j + 1, n):
+            x[r] = a1 * l[r][j] + x[r]
+        if gamma != 0.0:
+            a2 = new_diag * sigma / gamma * xj
+            b2 = new_diag / diag
+            for r in range(j + 1, n):
+                l[r][j] = a2 * x[r] + b2 * l[r][j]
+    return np.array(l)
+
+
+@pytest.mark.parametrize("n", [1, 3, 8, 13])
+@pytest.mark.parametrize("sigma", [0.7, -0.2])
+def test_rank_one_update_matches_pure_python_restatement_bitwise(n, sigma):
+    rng = np.random.default_rng(70 + n)
+    b = rng.standard_normal((n, n))
+    l, info = O.cholesky(b @ b.T + n * np.eye(n))
+    assert info == 0
+    x = rng.standard_normal(n) / np.sqrt(n)
+    got = O.cholesky_rank_one_update(l, x, sigma)
+    ref = _pure_python_rank_one_update(l, x, sigma)
+    assert np.array_equal(np.tril(got), np.tril(ref))
+    assert np.array_equal(np.triu(got, 1), np.triu(l, 1))  # the strict upper part is not touched
+
+
+def _random_sdp(rng, n):
+    b = rng.standard_normal((n, n))
+    return b @ b.T + n * np.eye(n)
+
+
+@pytest.mark.parametrize("seed", range(5))
+def test_cholesky_update_properties(seed):
+    """tests/linalg/cholesky.rs:120-173: rank_one_update with sigma in [0, 1),
+    insert_column and remove_column (n <= 10, random j) rebuild the updated
+    matrix to 1e-7."""
+    rng = np.random.default_rng(800 + seed)
+    m = _random_sdp(rng, 4)
+    x = rng.uniform(-1, 1, 4)
+    sigma = float(rng.random())
+    l, _ = O.cholesky(m)
+    lu = np.tril(O.cholesky_rank_one_update(l, x, sigma))
+    assert np.allclose(lu @ lu.T, m + sigma * np.outer(x, x), atol=1e-7, rtol=0)
+    n = int(rng.integers(1, 11))
+    j = int(rng.integers(0, n))
+    m_updated = _random_sdp(rng, n)
+    m_small = np.delete(np.delete(m_updated, j, axis=0), j, axis=1)
+    l_small, _ = O.cholesky(m_small) if n > 1 else (np.zeros((0, 0)), 0)
+    li = np.tril(O.cholesky_insert_column(l_small, j, m_updated[:, j]))
+    assert np.allclose(li @ li.T, m_updated, atol=1e-7, rtol=0)
+    l_full, _ = O.cholesky(m_updated)
+    lr = np.tril(O.cholesky_remove_column(l_full, j))
+    assert np.allclose(lr @ lr.T, m_small, atol=1e-7, rtol=0)
