@@ -523,3 +523,73 @@ def test_cholesky_update_properties(seed):
     l_full, _ = O.cholesky(m_updated)
     lr = np.tril(O.cholesky_remove_column(l_full, j))
     assert np.allclose(lr @ lr.T, m_small, atol=1e-7, rtol=0)
+
+
+def _py_dotx(x, y):
+    """Matrix::dotx (src/base/blas.rs:96-165) in pure Python."""
+    n = len(x)
+    acc = [0.0] * 8
+    i = 0
+    while n - i >= 8:
+        for q in range(8):
+            acc[q] += x[i + q] * y[i + q]
+        i += 8
+    res = 0.0
+    for q in range(4):
+        res += acc[q] + acc[q + 4]
+    for k in range(i, n):
+        res += x[k] * y[k]
+    return res
+
+
+def _pure_python_col_piv_qr(a):
+    """Independent pure-Python restatement of ColPivQR::new
+    (src/linalg/col_piv_qr.rs:59-92, householder.rs:19-85, reflection.rs:70-83)
+    for tiny square matrices; columns as lists."""
+    import math
+
+    n = len(a)
+    cols = [[float(a[r][c]) for r in range(n)] for c in range(n)]
+    diag, jpiv = [0.0] * n, list(range(n))
+    for i in range(n):
+        best, bc = abs(cols[i][i]), i
+        for c in range(i, n):
+            for r in range(i, n):
+                if abs(cols[c][r]) > best:
+                    best, bc = abs(cols[c][r]), c
+        cols[i], cols[bc] = cols[bc], cols[i]
+        jpiv[i] = bc
+        x = cols[i][i:]
+        sq = 0.0 + _py_dotx(x, x)
+        nrm = math.sqrt(sq)
+        modulus, sign = (x[0], 1.0) if x[0] >= 0 else (-x[0], -1.0)
+        signed_norm = sign * nrm
+        factor = (sq + modulus * nrm) * 2.0
+        x[0] += signed_norm
+        if factor != 0.0:
+            sf = math.sqrt(factor)
+            x = [v / sf for v in x]
+            n2 = math.sqrt(0.0 + _py_dotx(x, x))
+            x = [v / n2 for v in x]
+            rnorm = -signed_norm
+            sgn = math.copysign(1.0, rnorm)
+            for c in range(i + 1, n):
+                y = cols[c][i:]
+                f = (_py_dotx(x, y) - 0.0) * (sgn * -2.0)
+                cols[c][i:] = [f * x[k] + sgn * y[k] for k in range(len(y))]
+        else:
+            rnorm = signed_norm
+        cols[i][i:] = x
+        diag[i] = rnorm
+    return np.array(cols).T, np.array(diag), np.array(jpiv)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 9])
+def test_col_piv_qr_matches_pure_python_restatement_bitwise(n):
+    rng = np.random.default_rng(90 + n)
+    a = rng.uniform(-100, 100, size=(n, n))
+    qr, diag, jpiv = O.col_piv_qr(a)
+    qr2, diag2, jpiv2 = _pure_python_col_piv_qr(a)
+    assert np.array_equal(jpiv, jpiv2)
+    assert np.array_equal(diag, diag2)
+    assert np.array_equal(qr, qr2)
