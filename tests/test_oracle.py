@@ -593,3 +593,53 @@ def test_col_piv_qr_matches_pure_python_restatement_bitwise(n):
     assert np.array_equal(jpiv, jpiv2)
     assert np.array_equal(diag, diag2)
     assert np.array_equal(qr, qr2)
+
+
+def _pure_python_trsv(t, b, upper, trans, diag=None):
+    """Independent pure-Python restatement of the vector loops of
+    src/linalg/solve.rs (:74-101, :106-133, :156-182, :374-442) for one column."""
+    n = len(b)
+    x = [float(v) for v in b]
+    if diag is not None:  # solve_lower_triangular_with_diag_mut: b_i is never rewritten
+        if diag == 0.0:
+            return None
+        for i in range(n - 1):
+            coeff = x[i] / diag
+            for r in range(i + 1, n):
+                x[r] = -coeff * t[r][i] + x[r]
+        return x
+    if not trans:
+        order = reversed(range(n)) if upper else range(n)
+        for i in order:
+            d = t[i][i]
+            if d == 0.0:
+                return None
+            coeff = x[i] / d
+            x[i] = coeff
+            rows = range(i) if upper else range(i + 1, n)
+            for r in rows:
+                x[r] = -coeff * t[r][i] + x[r]
+        return x
+    order = range(n) if upper else reversed(range(n))
+    for i in order:
+        rows = list(range(i)) if upper else list(range(i + 1, n))
+        dot = _py_dotx([t[r][i] for r in rows], [x[r] for r in rows])
+        d = t[i][i]
+        if d == 0.0:
+            return None
+        x[i] = (x[i] - dot) / d
+    return x
+
+
+@pytest.mark.parametrize("n", [1, 7, 8, 9, 17])
+def test_triangular_solves_match_pure_python_restatement_bitwise(n):
+    rng = np.random.default_rng(120 + n)
+    t = rng.uniform(-1, 1, size=(n, n)) + 2 * np.eye(n)
+    b = rng.uniform(-1, 1, size=n)
+    for upper in (False, True):
+        for trans in (False, True):
+            got = O.triangular_solve(t, b, upper=upper, trans=trans)
+            ref = _pure_python_trsv(t, b, upper, trans)
+            assert np.array_equal(np.asarray(got).ravel(), np.array(ref)), (upper, trans)
+    got = O.triangular_solve(t, b, diag=2.5)
+    assert np.array_equal(np.asarray(got).ravel(), np.array(_pure_python_trsv(t, b, False, False, diag=2.5)))
