@@ -74,3 +74,16 @@ def test_non_finite_values_follow_serde_json():
     assert json.loads(s)["chol"][0] == [None, None, 0.0, 1.0]
     with pytest.raises(ValueError, match="expected f64"):
         F.cholesky_from_json(s)
+
+
+def test_empty_and_malformed_objects():
+    """A 0 x 0 factor round-trips; a permutation whose len exceeds its vector,
+    or a vector that is not n x 1, is refused."""
+    lu, ipiv = F.lu_from_json(F.lu_to_json(np.zeros((0, 0)), np.zeros(0, dtype=np.int32)))
+    assert lu.shape == (0, 0) and ipiv.shape == (0,)
+    with pytest.raises(ValueError, match="exceeds"):
+        F.permutation_from_obj({"len": 3, "ipiv": [[[0, 1], [0, 0]], 2, 1]})
+    with pytest.raises(ValueError, match="components"):
+        F.permutation_from_obj({"len": 1, "ipiv": [[[0, 1], [0, 0]], 2, 2]})
+    with pytest.raises(ValueError, match="expected"):
+        F.matrix_from_obj({"data": [1.0], "nrows": 1, "ncols": 1})
