@@ -372,11 +372,14 @@ int nacu_dgels_batched(int count, int n, int m_max, const int32_t* ms, const int
  * certified hosts that allocate only at start-up, plugins whose framework owns
  * every allocation).  No counterpart in nalgebra: it exists for callers of
  * this library.  Scratch (the work-queue head and the largest-first order) is
- * a fixed 256 KiB array inside the library's device image, held on every GPU
- * that loads the library until the process exits.  count <= 65536, else the
- * call returns -1 with a message.  The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  All calls share the one array: calls that overlap on
+ * a fixed array of 4 * (1 + 65536) bytes (256 KiB + 4 B) inside the
+ * library's device image, held on every GPU that loads the library until the
+ * process exits.  count <= 65536, else the call returns -1 with a message.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) and caches it for the process; make that first call
+ * before any stream capture.  cudaDeviceReset unloads the module and leaves
+ * that cached address stale: do not call this entry point on a device after
+ * resetting it.  All calls share the one array: calls that overlap on
  * the GPU race on it and must be ordered by the caller.  Arguments and results
  * are those of nacu_dposv_ragged; allocates nothing. */
 int nacu_dposv_ragged_noalloc(int count, int n_max, const int32_t* ns, const int64_t* a_offsets, double* A,

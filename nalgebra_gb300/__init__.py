@@ -263,7 +263,7 @@ class LU:
         n = lu.shape[0]
         obj = cls.__new__(cls)
         obj.lu, obj.flags, obj.large = DeviceMatrix.from_numpy(lu), flags, n > 128
-        obj.ipiv = torch.from_numpy(np.resize(ipiv.astype(np.int32), max(n, 1))).cuda()
+        obj.ipiv = torch.from_numpy(np.append(ipiv.astype(np.int32), np.zeros(max(n, 1) - n, np.int32))).cuda()
         zero = np.nonzero(np.diag(lu) == 0)[0]
         obj.info = torch.tensor([int(zero[0]) + 1 if len(zero) else 0, 0], dtype=torch.int32, device="cuda")
         if obj.large:
@@ -360,8 +360,8 @@ class FullPivLU:
         n = lu.shape[0]
         obj = cls.__new__(cls)
         obj.lu, obj.flags = DeviceMatrix.from_numpy(lu), flags
-        obj.ipiv = torch.from_numpy(np.resize(ipiv.astype(np.int32), max(n, 1))).cuda()
-        obj.jpiv = torch.from_numpy(np.resize(jpiv.astype(np.int32), max(n, 1))).cuda()
+        obj.ipiv = torch.from_numpy(np.append(ipiv.astype(np.int32), np.zeros(max(n, 1) - n, np.int32))).cuda()
+        obj.jpiv = torch.from_numpy(np.append(jpiv.astype(np.int32), np.zeros(max(n, 1) - n, np.int32))).cuda()
         zero = np.nonzero(np.diag(lu) == 0)[0]
         inv = n == 0 or lu[n - 1, n - 1] != 0
         obj.info = torch.tensor([0 if inv else int(zero[0]) + 1], dtype=torch.int32, device="cuda")
@@ -451,8 +451,8 @@ class ColPivQR:
         n = qr.shape[0]
         obj = cls.__new__(cls)
         obj.qr, obj.flags = DeviceMatrix.from_numpy(qr), flags
-        obj.diag = torch.from_numpy(np.resize(diag, max(n, 1))).cuda()
-        obj.jpiv = torch.from_numpy(np.resize(jpiv.astype(np.int32), max(n, 1))).cuda()
+        obj.diag = torch.from_numpy(np.append(diag, np.zeros(max(n, 1) - n))).cuda()
+        obj.jpiv = torch.from_numpy(np.append(jpiv.astype(np.int32), np.zeros(max(n, 1) - n, np.int32))).cuda()
         zero = np.nonzero(diag == 0)[0]
         obj.info = torch.tensor([int(zero[0]) + 1 if len(zero) else 0], dtype=torch.int32, device="cuda")
         return obj

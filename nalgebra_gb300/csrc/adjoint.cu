@@ -284,7 +284,7 @@ int adj_launch_forward(int n, const T* A, int64_t strideA, const T* B, T* X, T* 
   if (!A || !B || !X || !logdet) return record_arg_error(-2, "posv_logdet_forward: null A, B, X or logdet");
   if (strideA < (int64_t)n * n) return record_arg_error(-3, "posv_logdet_forward: strideA < n*n");
   const size_t smem = ((size_t)(n | 1) * n + n) * sizeof(T);
-  cudaError_t e = cudaFuncSetAttribute(adj_forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_dynamic_smem(adj_forward_kernel<T>, smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   adj_forward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, A, strideA, B, X, Lout, logdet, info, batch);
   return check_launch(name);
@@ -299,7 +299,7 @@ int adj_launch_backward(int n, const T* AL, int64_t strideA, int recompute, cons
   if (!AL || !X || !W || !dA || !db) return record_arg_error(-2, "posv_logdet_backward: null argument");
   if (strideA < (int64_t)n * n) return record_arg_error(-3, "posv_logdet_backward: strideA < n*n");
   const size_t smem = ((size_t)(n | 1) * n + 5 * (size_t)n) * sizeof(T);
-  cudaError_t e = cudaFuncSetAttribute(adj_backward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_dynamic_smem(adj_backward_kernel<T>, smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   adj_backward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, AL, strideA, recompute, X, W, G, dA, db, info,
                                                                batch);

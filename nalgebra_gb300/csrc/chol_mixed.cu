@@ -637,9 +637,9 @@ int nacu_dposv_ragged_mixed(int count, int n_max, const int32_t* ns, const int64
   const size_t smem = mixed_smem_bytes(n_max);
   const size_t smem_fb = fallback_smem_bytes(n_max);
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaFuncSetAttribute(chol_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_dynamic_smem(chol_mixed_kernel, smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(chol_mixed_fallback_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_fb);
+    e = ensure_dynamic_smem(chol_mixed_fallback_kernel, smem_fb);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dposv_ragged_mixed");
   int per_sm = 0, per_sm_fb = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chol_mixed_kernel, kCholThreads, smem);

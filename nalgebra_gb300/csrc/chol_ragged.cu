@@ -20,6 +20,7 @@
 // factor is bit-identical to nalgebra's.  The triangular solves are blocked by
 // 32 rows: one warp solves each diagonal block out of registers with shuffles,
 // the whole CTA applies the block to the remaining rows.
+#include <atomic>
 #include <algorithm>
 #include <vector>
 
@@ -186,7 +187,7 @@ int chol_launch_tile(CholArgs g, int tile, bool exact, cudaStream_t stream, bool
   CholKernel kern = chol_kernel(exact, tile);
   const int threads = kCholTiles[tile].threads;
   const size_t smem = chol_smem_bytes(g.n_max, kCholTiles[tile].nb);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_dynamic_smem(kern, smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   int grid = 1;
   if (persistent) {
@@ -380,7 +381,7 @@ int chol_uniform_posv(int n, double* A, int64_t strideA, int nrhs, double* B, in
   if (tile < 0 || tile >= NACU_RAGGED_TILES) tile = kDefaultTile;
   CholKernel kern = chol_kernel(false, tile);
   const size_t smem = chol_smem_bytes(n, kCholTiles[tile].nb);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_dynamic_smem(kern, smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   kern<<<batch, kCholTiles[tile].threads, smem, s>>>(g);
   return check_launch(name);
@@ -493,7 +494,9 @@ constexpr int kNoAllocMaxCount = NACU_RAGGED_NOALLOC_MAX_COUNT;
 // [0]: work-queue head; [1 .. count]: processing order.
 static __device__ __align__(256) int32_t g_ragged_noalloc_scratch[1 + kNoAllocMaxCount];
 
-int32_t* g_noalloc_scratch_ptr[64] = {nullptr};
+// Per-device cache of the array's device address.  Atomic: two host threads
+// making a first call at once both look it up and store the same value.
+std::atomic<int32_t*> g_noalloc_scratch_ptr[64] = {};
 
 // Builds the largest-first order (a counting sort on n, one CTA) into the
 // scratch and clears the queue head, so every call starts from zero.
@@ -533,13 +536,15 @@ int noalloc_scratch(int32_t** out) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dposv_ragged_noalloc: cudaGetDevice");
   if (dev < 0 || dev >= 64) return record_arg_error(-99, "nacu_dposv_ragged_noalloc: device index >= 64");
-  if (g_noalloc_scratch_ptr[dev] == nullptr) {
+  int32_t* cached = g_noalloc_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (cached == nullptr) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_ragged_noalloc_scratch);
     if (e != cudaSuccess) return record_cuda_error(e, "nacu_dposv_ragged_noalloc: cudaGetSymbolAddress");
-    g_noalloc_scratch_ptr[dev] = static_cast<int32_t*>(p);
+    cached = static_cast<int32_t*>(p);
+    g_noalloc_scratch_ptr[dev].store(cached, std::memory_order_release);
   }
-  *out = g_noalloc_scratch_ptr[dev];
+  *out = cached;
   return NACU_SUCCESS;
 }
 

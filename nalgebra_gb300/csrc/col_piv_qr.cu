@@ -383,7 +383,7 @@ int colpivqr_launch(int n, int nrhs, double* A, int64_t strideA, double* diag, i
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   auto kern = (flags & NACU_FLAG_EXACT) ? colpivqr_kernel<true> : colpivqr_kernel<false>;
   if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const cudaError_t e = ensure_dynamic_smem(kern, smem);
     if (e != cudaSuccess) return record_cuda_error(e, name);
   }
   int per_sm = 0;

@@ -35,6 +35,23 @@ inline int check_launch(const char* where) {
   return NACU_SUCCESS;
 }
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes`, never
+// lowering it.  A kernel node recorded in a CUDA graph keeps the size it was
+// captured with, while the function attribute is read again when the node is
+// launched on its own (a profiler replaying a graph node by node does this).
+// Setting the attribute to each call's own size let a later, smaller call on
+// the same kernel push it below an earlier node's size, and that node's
+// launch then failed.
+template <typename K>
+inline cudaError_t ensure_dynamic_smem(K kern, size_t bytes) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, reinterpret_cast<const void*>(kern));
+  if (e != cudaSuccess) return e;
+  if ((size_t)a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+  return cudaFuncSetAttribute(reinterpret_cast<const void*>(kern), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)bytes);
+}
+
 inline int sm_count() {
   static int count = 0;
   if (count == 0) {

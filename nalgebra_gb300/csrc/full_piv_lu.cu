@@ -334,7 +334,7 @@ int fullpiv_launch(int n, int nrhs, double* A, int64_t strideA, int32_t* ipiv, i
   const bool exact = flags & NACU_FLAG_EXACT;
   auto kern = exact ? fullpiv_kernel<true> : fullpiv_kernel<false>;
   if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const cudaError_t e = ensure_dynamic_smem(kern, smem);
     if (e != cudaSuccess) return record_cuda_error(e, name);
   }
   int per_sm = 0;

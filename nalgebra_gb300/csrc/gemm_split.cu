@@ -491,7 +491,7 @@ int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, 
   g.rexp = rexp;
   g.cexp = cexp;
   const size_t smem = (size_t)kStages * kStageBytes + 1024;
-  e = cudaFuncSetAttribute(split_gemm_kernel<TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  e = ensure_dynamic_smem(split_gemm_kernel<TO>, smem);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgemm_split_bf16");
   dim3 grid(L.mp / kTM, L.np / kTN);
   if (g.npairs == 0) {  // k == 0: C = beta * C

@@ -622,7 +622,7 @@ __global__ void __launch_bounds__(64) lu_trsm_generic_kernel(int n, T* A, int64_
 template <typename T, int NB>
 cudaError_t launch_trsm_tiled(int n, T* A, int64_t lda, int j0, int rest, cudaStream_t s) {
   const size_t smem = (size_t)NB * NB * sizeof(T);
-  cudaError_t e = cudaFuncSetAttribute(lu_trsm_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_dynamic_smem(lu_trsm_kernel<T, NB>, smem);
   if (e != cudaSuccess) return e;
   const int per_cta = 8 * kTrsmCols;
   lu_trsm_kernel<T, NB><<<(rest + per_cta - 1) / per_cta, 256, smem, s>>>(n, A, lda, j0);
@@ -635,8 +635,7 @@ cudaError_t launch_trsm(int n, T* A, int64_t lda, int j0, int jb, int rest, cuda
   if (jb == 128) return launch_trsm_tiled<T, 128>(n, A, lda, j0, rest, s);
   const size_t smem = (size_t)jb * jb * sizeof(T) + (size_t)jb * 64 * sizeof(T);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(lu_trsm_generic_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = ensure_dynamic_smem(lu_trsm_generic_kernel<T>, smem);
     if (e != cudaSuccess) return e;
   }
   lu_trsm_generic_kernel<T><<<(rest + 63) / 64, 64, smem, s>>>(n, A, lda, j0, jb);
@@ -927,7 +926,7 @@ int panel_cluster_ctas() {
   if (ctas >= 0) return ctas;
   ctas = 0;
   auto kern = lu_panel_cluster_kernel<T>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelMaxSmem) != cudaSuccess ||
+  if (ensure_dynamic_smem(kern, kPanelMaxSmem) != cudaSuccess ||
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
     cudaGetLastError();
     return ctas;
@@ -965,7 +964,7 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
   cudaError_t e;
   if (nb > kPanelMaxNb) nb = kPanelMaxNb;
   const void* pk = reinterpret_cast<const void*>(lu_panel_grid_kernel<T>);
-  e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelMaxSmem);
+  e = ensure_dynamic_smem(pk, kPanelMaxSmem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   const int cluster = panel_cluster_ctas<T>();
   const int gmax = std::min(kPanelMaxG, sm_count());
@@ -1061,7 +1060,7 @@ int trsv_pair(int n, const T* LU, int64_t lda, T* x, int32_t* info, int* sync, c
   const void* tk = reinterpret_cast<const void*>(trsv_kernel<T>);
   constexpr int BS = TrsvTile<T>::BS;
   const size_t smem = (size_t)BS * (BS + 1) * sizeof(T);
-  cudaError_t e = cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_dynamic_smem(tk, smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   const int nblk = (n + BS - 1) / BS;
   for (int lower = 1; lower >= 0; --lower) {
@@ -1082,8 +1081,7 @@ int getrs_one(int n, const T* LU, int64_t lda, const int32_t* ipiv, T* x, int32_
   const size_t stage = (size_t)n * (sizeof(T) + sizeof(int32_t));
   const int staged = stage <= kStageLimit;
   if (staged && stage > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(apply_pivots_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kStageLimit);
+    cudaError_t e = ensure_dynamic_smem(apply_pivots_kernel<T>, kStageLimit);
     if (e != cudaSuccess) return record_cuda_error(e, name);
   }
   apply_pivots_kernel<T><<<1, 256, staged ? stage : 0, s>>>(n, ipiv, x, staged);
@@ -1286,7 +1284,7 @@ int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, do
   if (hinfo == 0) {
     const int staged = (size_t)n * 8 <= kStageLimit;
     if (staged && (size_t)n * 8 > 48 * 1024) {
-      e = cudaFuncSetAttribute(pivots_to_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageLimit);
+      e = ensure_dynamic_smem(pivots_to_perm_kernel, kStageLimit);
       if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgesv_mixed_ir");
     }
     pivots_to_perm_kernel<<<1, 256, staged ? (size_t)n * 8 : 0, s>>>(n, ipiv, perm, staged);

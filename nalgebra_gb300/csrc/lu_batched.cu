@@ -275,7 +275,7 @@ int lu_launch(int n, int nrhs, T* A, int64_t strideA, int32_t* ipiv, T* B, int64
   const bool exact = (flags & NACU_FLAG_EXACT) != 0;
   auto kern = exact ? lu_batched_kernel<T, true> : lu_batched_kernel<T, false>;
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ensure_dynamic_smem(kern, smem);
     if (e != cudaSuccess) return record_cuda_error(e, name);
   }
   const int grid = batch;  // one CTA per system; the hardware scheduler refills SMs

@@ -370,7 +370,7 @@ int nacu_dgels_batched(int count, int n, int m_max, const int32_t* ms, const int
            reinterpret_cast<int32_t*>(workspace)};
   const size_t smem = (size_t)(m_max | 1) * kQrNB * sizeof(double);
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaFuncSetAttribute(qr_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = ensure_dynamic_smem(qr_batched_kernel, smem);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgels_batched");
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_batched_kernel, kQrThreads, smem);

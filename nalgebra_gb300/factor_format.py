@@ -84,10 +84,36 @@ def permutation_from_obj(o, where: str = "permutation") -> np.ndarray:
         raise ValueError(f"{where}: Expected {dim * int(ncols)} components, found {len(data)}")
     if k > dim:
         raise ValueError(f"{where}: len {k} exceeds the dimension {dim}")
+    if k < 0:
+        raise ValueError(f"{where}: negative len {k}")
     ipiv = np.arange(dim, dtype=np.int32)
-    for i, i2 in data[:k]:
-        ipiv[int(i)] = int(i2)
+    prev = -1
+    for pair in data[:k]:
+        if not (isinstance(pair, list) and len(pair) == 2):
+            raise ValueError(f"{where}: expected [i, i2] pairs")
+        i, i2 = int(pair[0]), int(pair[1])
+        # The factorizations append (i, piv) at step i with i < piv < dim
+        # (lu.rs:103-113, full_piv_lu.rs:79-82, col_piv_qr.rs:74-78,
+        # append_permutation skipping i == piv); only such sequences have the
+        # per-step device form.
+        if not (0 <= i < dim and i <= i2 < dim):
+            raise ValueError(f"{where}: swap ({i}, {i2}) out of range for dimension {dim}")
+        if i <= prev:
+            raise ValueError(f"{where}: swap ({i}, {i2}) out of step order")
+        prev = i
+        ipiv[i] = i2
     return ipiv
+
+
+def _square(m: np.ndarray, where: str) -> int:
+    if m.shape[0] != m.shape[1]:
+        raise ValueError(f"{where}: the factor is {m.shape[0]} x {m.shape[1]}, expected a square matrix")
+    return int(m.shape[0])
+
+
+def _dim(v: np.ndarray, n: int, where: str) -> None:
+    if v.shape[0] != n:
+        raise ValueError(f"{where}: dimension {v.shape[0]} does not match the factor's order {n}")
 
 
 def _dump(obj: dict) -> str:
@@ -100,8 +126,12 @@ def lu_to_json(lu, ipiv) -> str:
 
 
 def lu_from_json(s: str):
+    """(lu, ipiv) of a square LU; a non-square factor or a permutation of
+    another dimension is refused."""
     o = json.loads(s)
-    return matrix_from_obj(o["lu"], "lu"), permutation_from_obj(o["p"], "p")
+    lu, p = matrix_from_obj(o["lu"], "lu"), permutation_from_obj(o["p"], "p")
+    _dim(p, _square(lu, "lu"), "p")
+    return lu, p
 
 
 def full_piv_lu_to_json(lu, ipiv, jpiv) -> str:
@@ -111,8 +141,12 @@ def full_piv_lu_to_json(lu, ipiv, jpiv) -> str:
 
 def full_piv_lu_from_json(s: str):
     o = json.loads(s)
-    return (matrix_from_obj(o["lu"], "lu"), permutation_from_obj(o["p"], "p"),
-            permutation_from_obj(o["q"], "q"))
+    lu, p, q = (matrix_from_obj(o["lu"], "lu"), permutation_from_obj(o["p"], "p"),
+                permutation_from_obj(o["q"], "q"))
+    n = _square(lu, "lu")
+    _dim(p, n, "p")
+    _dim(q, n, "q")
+    return lu, p, q
 
 
 def qr_to_json(qr, diag) -> str:
@@ -121,8 +155,13 @@ def qr_to_json(qr, diag) -> str:
 
 
 def qr_from_json(s: str):
+    """(qr, diag) of an m x n QR; diag holds min(m, n) entries (qr.rs:60-62)."""
     o = json.loads(s)
-    return matrix_from_obj(o["qr"], "qr"), matrix_from_obj(o["diag"], "diag")[:, 0].copy()
+    qr, diag = matrix_from_obj(o["qr"], "qr"), matrix_from_obj(o["diag"], "diag")
+    if diag.shape[1] != 1:
+        raise ValueError("diag: expected a column vector")
+    _dim(diag, min(qr.shape), "diag")
+    return qr, diag[:, 0].copy()
 
 
 def col_piv_qr_to_json(qr, jpiv, diag) -> str:
@@ -133,8 +172,14 @@ def col_piv_qr_to_json(qr, jpiv, diag) -> str:
 
 def col_piv_qr_from_json(s: str):
     o = json.loads(s)
-    return (matrix_from_obj(o["col_piv_qr"], "col_piv_qr"), permutation_from_obj(o["p"], "p"),
-            matrix_from_obj(o["diag"], "diag")[:, 0].copy())
+    qr, p, diag = (matrix_from_obj(o["col_piv_qr"], "col_piv_qr"), permutation_from_obj(o["p"], "p"),
+                   matrix_from_obj(o["diag"], "diag"))
+    n = _square(qr, "col_piv_qr")
+    if diag.shape[1] != 1:
+        raise ValueError("diag: expected a column vector")
+    _dim(p, n, "p")
+    _dim(diag, n, "diag")
+    return qr, p, diag[:, 0].copy()
 
 
 def cholesky_to_json(chol) -> str:
@@ -144,4 +189,6 @@ def cholesky_to_json(chol) -> str:
 
 
 def cholesky_from_json(s: str) -> np.ndarray:
-    return matrix_from_obj(json.loads(s)["chol"], "chol")
+    chol = matrix_from_obj(json.loads(s)["chol"], "chol")
+    _square(chol, "chol")
+    return chol

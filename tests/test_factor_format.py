@@ -87,3 +87,42 @@ def test_empty_and_malformed_objects():
         F.permutation_from_obj({"len": 1, "ipiv": [[[0, 1], [0, 0]], 2, 2]})
     with pytest.raises(ValueError, match="expected"):
         F.matrix_from_obj({"data": [1.0], "nrows": 1, "ncols": 1})
+
+
+def test_out_of_range_swaps_are_refused():
+    """A swap pair outside [0, dim), with i2 < i, out of step order, or a
+    negative len would index outside the device factor: refused."""
+    def perm(pairs, dim, k=None):
+        pad = [[0, 0]] * (dim - len(pairs))
+        return {"len": len(pairs) if k is None else k, "ipiv": [pairs + pad, dim, 1]}
+
+    assert list(F.permutation_from_obj(perm([[0, 2], [1, 2]], 3))) == [2, 2, 2]
+    for bad in (perm([[-1, 2]], 3), perm([[0, 3]], 3), perm([[2, 1]], 3), perm([[1, 2], [0, 1]], 3),
+                perm([[1, 2], [1, 2]], 3), perm([[0, -3]], 3)):
+        with pytest.raises(ValueError, match="out of"):
+            F.permutation_from_obj(bad)
+    with pytest.raises(ValueError, match="negative len"):
+        F.permutation_from_obj(perm([[0, 1]], 3, k=-1))
+
+
+def test_factor_shapes_are_checked():
+    """A tall factor, or a permutation / diag of another dimension than the
+    factor's order, is refused before anything reaches the device."""
+    tall = np.arange(12.0).reshape(4, 3)
+    with pytest.raises(ValueError, match="square"):
+        F.lu_from_json(F.lu_to_json(tall, np.arange(3, dtype=np.int32)))
+    with pytest.raises(ValueError, match="square"):
+        F.cholesky_from_json(F.cholesky_to_json(tall))
+    with pytest.raises(ValueError, match="square"):
+        F.col_piv_qr_from_json(F.col_piv_qr_to_json(tall, np.arange(3), np.ones(3)))
+    sq = np.eye(3)
+    with pytest.raises(ValueError, match="does not match"):
+        F.lu_from_json(F.lu_to_json(sq, np.arange(2, dtype=np.int32)))
+    with pytest.raises(ValueError, match="does not match"):
+        F.full_piv_lu_from_json(F.full_piv_lu_to_json(sq, np.arange(3), np.arange(4)))
+    with pytest.raises(ValueError, match="does not match"):
+        F.col_piv_qr_from_json(F.col_piv_qr_to_json(sq, np.arange(3), np.ones(2)))
+    with pytest.raises(ValueError, match="does not match"):
+        F.qr_from_json(F.qr_to_json(tall, np.ones(4)))
+    q, d = F.qr_from_json(F.qr_to_json(tall, np.ones(3)))
+    assert q.shape == (4, 3) and d.shape == (3,)
