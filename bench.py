@@ -151,41 +151,40 @@ def ragged_bytes(ns, nrhs):
     return float(np.sum(8.0 * ns * (ns + 1) + 2 * 8.0 * nrhs * ns))
 
 
-def backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample):
-    """Normwise backward error of a sample of systems with the residual in
-    extended precision (numpy longdouble), in units of n * eps64."""
-    worst = 0.0
-    for s in sample:
-        n = int(ns[s])
-        a = a_host[aoff[s]:aoff[s] + n * n].reshape(n, n).T.astype(np.longdouble)
-        a = np.tril(a) + np.tril(a, -1).T
-        b = b_host[boff[s]:boff[s] + n * nrhs].reshape(nrhs, n).T.astype(np.longdouble)
-        x = x_host[boff[s]:boff[s] + n * nrhs].reshape(nrhs, n).T.astype(np.longdouble)
-        r = b - a @ x
-        an = np.max(np.sum(np.abs(a), axis=1))
-        be = np.max(np.max(np.abs(r), axis=0) / (an * np.max(np.abs(x), axis=0) + np.max(np.abs(b), axis=0)))
-        worst = max(worst, float(be) / (n * EPS64))
-    return worst
-
-
-def forward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample):
-    """Max over a sample of ||x - x_ref||_inf / ||x_ref||_inf per right-hand
-    side, x_ref the oracle's FP64 solve (nalgebra's Cholesky::solve restated)."""
+def batch_accuracy(ns, aoff, a_host, boff, b_host, x_host, nrhs, x_ref=None):
+    """Accuracy of every system of the batch (host, outside the timed events):
+    the normwise backward error with the residual by Dot2 (the oracle's
+    compensated dot), in units of n * eps64, and -- given the oracle's FP64
+    solutions x_ref -- the forward error ||x - x_ref||_inf / ||x_ref||_inf per
+    right-hand side."""
     import oracle as O
 
-    worst = 0.0
-    for s in sample:
-        n = int(ns[s])
-        a = a_host[aoff[s]:aoff[s] + n * n].reshape(n, n).T
-        b = b_host[boff[s]:boff[s] + n * nrhs].reshape(nrhs, n).T
-        x = x_host[boff[s]:boff[s] + n * nrhs].reshape(nrhs, n).T
-        l, info = O.cholesky(a)
-        if info != 0:
-            continue
-        xr = O.cholesky_solve(l, b)
-        fe = np.max(np.max(np.abs(x - xr), axis=0) / np.max(np.abs(xr), axis=0))
-        worst = max(worst, float(fe))
-    return worst
+    berr = O.ragged_backward_errors(ns, aoff, a_host, boff, b_host, x_host, nrhs)
+    units = berr / (ns.astype(np.float64) * EPS64)
+    out = {"backward_error_max_over_batch_in_n_eps": float(np.max(units)),
+           "systems_above_n_eps": int(np.sum(~(units <= 1.0))), "systems_checked": int(ns.size)}
+    if x_ref is not None:
+        # one segment per (system, right-hand side): rows boff[s] + c*n ... + n
+        ns64 = ns.astype(np.int64)
+        packed = bool(np.all(np.diff(boff) == ns64[:-1] * nrhs)) and int(boff[-1] + ns64[-1] * nrhs) == x_host.size
+        starts = (boff[:, None] + np.arange(nrhs)[None, :] * ns64[:, None]).ravel()[np.repeat(ns, nrhs) > 0]
+        if packed and starts.size:
+            d = np.maximum.reduceat(np.abs(x_host - x_ref), starts)
+            r = np.maximum.reduceat(np.abs(x_ref), starts)
+        else:
+            lens = np.repeat(ns64, nrhs)[np.repeat(ns, nrhs) > 0]
+            d = np.array([np.max(np.abs(x_host[a:a + k] - x_ref[a:a + k])) for a, k in zip(starts, lens)])
+            r = np.array([np.max(np.abs(x_ref[a:a + k])) for a, k in zip(starts, lens)])
+        out["forward_error_max_vs_fp64_oracle_over_batch"] = float(np.max(d / np.where(r > 0, r, 1.0))) if d.size else 0.0
+    return out
+
+
+def oracle_solutions(ns, aoff, a_host, boff, b_host, nrhs):
+    """The oracle's FP64 solutions of the whole batch (nalgebra's
+    Cholesky::solve restated), all host threads."""
+    import oracle as O
+
+    return O.posv_ragged(ns, aoff, a_host, boff, b_host, nrhs)[1]
 
 
 def bench_ragged_ours(args, rank, world):
@@ -266,19 +265,18 @@ def bench_ragged_ours(args, rank, world):
     info = chol.info.cpu().numpy()
     if np.any(info != 0):
         raise RuntimeError(f"{int(np.sum(info != 0))} systems failed to factor")
-    # accuracy of the last step's solutions (sampled)
+    # accuracy of the last step's solutions, every system of the batch
     rng = np.random.default_rng(1)
-    sample = rng.choice(count, size=min(48, count), replace=False)
     a_host = a0.cpu().numpy()
     b_host = b0.cpu().numpy()
     x_host = B.cpu().numpy()
-    berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample)
-    ferr64 = forward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample[:16])
+    x_ref = oracle_solutions(ns, aoff, a_host, boff, b_host, nrhs)
+    acc64 = batch_accuracy(ns, aoff, a_host, boff, b_host, x_host, nrhs, x_ref)
 
     # precision form: FP32 factor + FP64 refinement, same inputs, one launch
-    mixed = bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host)
+    mixed = bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host, x_ref)
     mchol, mrhs, mout = mixed.pop("_objects")
-    use_mixed = mixed["backward_error_max_over_sample_in_n_eps"] <= 1.0 and mixed["ms_per_step"] < kern_ms
+    use_mixed = mixed["systems_above_n_eps"] == 0 and mixed["ms_per_step"] < kern_ms
 
     # e2e through the public API from pinned host buffers (H2D of A and B in,
     # D2H of X, info and the per-matrix status out), inside the timed region.
@@ -352,8 +350,7 @@ def bench_ragged_ours(args, rank, world):
     flops = ragged_flops(ns, nrhs)
     achieved = flops / (kern_ms * 1e-3)
     fp64_form = {"solves_per_s": count / (kern_ms * 1e-3), "gflops": achieved / 1e9, "ms_per_step": kern_ms,
-                 "frac_of_fp64_peak": achieved / peak, "backward_error_max_over_sample_in_n_eps": berr,
-                 "forward_error_max_vs_fp64_oracle_over_sample": ferr64}
+                 "frac_of_fp64_peak": achieved / peak, **acc64}
     mixed["frac_of_fp64_peak_executed"] = mixed["fp64_flops_executed_per_launch"] / (mixed["ms_per_step"] * 1e-3) / peak
     head_ms = mixed["ms_per_step"] if use_mixed else kern_ms
     value = count * world / (head_ms * 1e-3)
@@ -364,7 +361,7 @@ def bench_ragged_ours(args, rank, world):
     else:
         roof_achieved = achieved
         roof_note = "dominant kernel chol_ragged_kernel<false>: n^3/3 + 2 nrhs n^2 per system"
-    berr_head = mixed["backward_error_max_over_sample_in_n_eps"] if use_mixed else berr
+    acc_head = {k: (mixed if use_mixed else acc64)[k] for k in acc64}
     res = {
         "metric": "solves/s at backward err <= n*eps64 (ragged batched SPD solve, chosen forms vs plain FP64)",
         "value": value,
@@ -388,7 +385,7 @@ def bench_ragged_ours(args, rank, world):
                    "l2": "inputs (3.4 GB) larger than L2; input restore outside the timed events",
                    "parallelism": "replicas" if world > 1 else "single"},
         "gflops": flops / (head_ms * 1e-3) / 1e9,
-        "backward_error_max_over_sample_in_n_eps": berr_head,
+        **acc_head,
         "forms": {
             "batched_persistent_fp64": fp64_form,
             "plain_fp64_launch_per_matrix": {"solves_per_s": plain_solves_per_s, "gflops": plain_flops / 1e9,
@@ -400,7 +397,7 @@ def bench_ragged_ours(args, rank, world):
                      "frac": roof_achieved / peak, "traffic": None, "note": roof_note,
                      "peak_source": fp64_peak_source(),
                      "algorithmic_bytes_per_launch": ragged_bytes(ns, nrhs),
-                     "hbm_frac_of_measured": (ragged_bytes(ns, nrhs) / (kern_ms * 1e-3)) / (read_peaks().get("hbm_gbs", 6794.8) * 1e9)},
+                     "hbm_frac_of_measured": (ragged_bytes(ns, nrhs) / (head_ms * 1e-3)) / (read_peaks().get("hbm_gbs", 6794.8) * 1e9)},
         "e2e": {"value": count / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         # per step: the mixed form launches chol_mixed_kernel + chol_mixed_fallback_kernel; the FP64
@@ -415,7 +412,7 @@ def bench_ragged_ours(args, rank, world):
     return res, dict(ns=ns, aoff=aoff, boff=boff, a_host=a_host, b_host=b_host, nrhs=nrhs)
 
 
-def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host):
+def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_host, x_ref=None):
     """The precision form on the same inputs (A and B read-only, X out), one
     graph-replayed launch per step."""
     import torch
@@ -446,19 +443,15 @@ def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_
     it = chol._iters.cpu().numpy()[:count]
     if np.any(chol.info.cpu().numpy()[:count] != 0):
         raise RuntimeError("mixed form: systems reported not SPD")
-    rng = np.random.default_rng(2)
-    sample = rng.choice(count, size=min(48, count), replace=False)
     x_host = out.data.cpu().numpy()
-    berr = backward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample)
-    ferr = forward_errors_sample(ns, aoff, a_host, boff, b_host, x_host, nrhs, sample[:16])
+    acc = batch_accuracy(ns, aoff, a_host, boff, b_host, x_host, nrhs, x_ref)
     n = ns.astype(np.float64)
     fp64_flops = float(np.sum(np.abs(it) * 2.0 * nrhs * n * n))  # FP64 residual work actually executed
     return {"solves_per_s": count / (ms * 1e-3), "ms_per_step": ms,
             "gflops_fp64_equivalent": ragged_flops(ns, nrhs) / (ms * 1e-3) / 1e9,
             "fp64_flops_executed_per_launch": fp64_flops,
             "residuals_per_system_mean": float(np.mean(np.abs(it))), "fp64_fallbacks": int(np.sum(it < 0)),
-            "backward_error_max_over_sample_in_n_eps": berr,
-            "forward_error_max_vs_fp64_oracle_over_sample": ferr, "_objects": (chol, rhs, out)}
+            **acc, "_objects": (chol, rhs, out)}
 
 
 _FP64_PEAK = {}
@@ -477,8 +470,8 @@ PROFILED_TRAFFIC = {
 def ctypes_probe(L):
     """FP64 roofline denominator: the best of a cuBLAS DGEMM (torch.matmul on
     float64, 8192^3, best of 2 -- the FP64 counterpart of the cuBLAS BF16 figure
-    in MEASURED_PEAKS.json) and the library's DFMA probe, both measured in this
-    run.  Cached per process."""
+    in MEASURED_PEAKS.json), this library's own DGEMM (nacu_dgemm, 8192^3, best
+    of 2) and its DFMA probe, all measured in this run.  Cached per process."""
     if "value" in _FP64_PEAK:
         return _FP64_PEAK["value"]
     import ctypes
@@ -502,14 +495,32 @@ def ctypes_probe(L):
         e1.record()
         torch.cuda.synchronize()
         best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3))
-    _FP64_PEAK.update(value=max(best, v.value), cublas_dgemm=best, dfma_probe=v.value)
+    # the library's own DGEMM on the same operands (column-major views of a, b)
+    c = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    sp = int(torch.cuda.current_stream().cuda_stream)
+    own = 0.0
+    for i in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = L.nacu_dgemm(n, n, n, ctypes.c_double(1.0), ctypes.c_void_p(a.data_ptr()), n,
+                          ctypes.c_void_p(b.data_ptr()), n, ctypes.c_double(0.0), ctypes.c_void_p(c.data_ptr()), n,
+                          ctypes.c_void_p(sp))
+        e1.record()
+        torch.cuda.synchronize()
+        if rc != 0:
+            raise RuntimeError("nacu_dgemm failed in the FP64 peak probe")
+        if i:
+            own = max(own, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3))
+    del a, b, c
+    _FP64_PEAK.update(value=max(best, own, v.value), cublas_dgemm=best, own_dgemm=own, dfma_probe=v.value)
     return _FP64_PEAK["value"]
 
 
 def fp64_peak_source():
-    return ("FP64: max of cuBLAS DGEMM 8192^3 (%.3f TFLOP/s) and the DFMA probe (%.3f TFLOP/s), measured in this "
-            "run; MEASURED_PEAKS.json has no FP64 figure" % (_FP64_PEAK.get("cublas_dgemm", 0) / 1e12,
-                                                             _FP64_PEAK.get("dfma_probe", 0) / 1e12))
+    return ("FP64: max of cuBLAS DGEMM 8192^3 (%.3f TFLOP/s), this library's nacu_dgemm 8192^3 (%.3f TFLOP/s) and "
+            "the DFMA probe (%.3f TFLOP/s), measured in this run; MEASURED_PEAKS.json has no FP64 figure"
+            % (_FP64_PEAK.get("cublas_dgemm", 0) / 1e12, _FP64_PEAK.get("own_dgemm", 0) / 1e12,
+               _FP64_PEAK.get("dfma_probe", 0) / 1e12))
 
 
 def cpu_baseline_ragged(data, max_seconds=20.0):
@@ -607,6 +618,20 @@ def bench_lu_ours(args, rank, world):
     ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
     flops = count * (2.0 / 3 * n ** 3 + 2.0 * n ** 2)
     peak = ctypes_probe(L)
+    # every system against the oracle (nalgebra's LU::new + solve restated):
+    # identical pivot sequences, backward error <= 10 n eps64 (residual by Dot2)
+    import oracle as O
+
+    _, piv_ref, _, _ = O.gesv_batched(a, b, n)
+    piv = ipiv.cpu().numpy().reshape(count, n)
+    x = B.cpu().numpy()
+    ns = np.full(count, n, dtype=np.int32)
+    be = O.ragged_backward_errors(ns, np.arange(count, dtype=np.int64) * n * n, a.reshape(-1),
+                                  np.arange(count, dtype=np.int64) * n, b.reshape(-1), x, 1, symmetric=False)
+    accuracy = {"systems_checked": count, "pivot_sequences_identical": int(np.sum(np.all(piv == piv_ref, axis=1))),
+                "backward_error_max_over_batch_in_n_eps": float(np.max(be) / (n * EPS64)),
+                "systems_above_10_n_eps": int(np.sum(~(be / (n * EPS64) <= 10.0))),
+                "info_nonzero": int(np.sum(info.cpu().numpy() != 0))}
     return {"metric": "solves/s (batched LU factor+solve, 4096 x 64x64 f64)", "value": count / (ms * 1e-3),
             "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -616,7 +641,7 @@ def bench_lu_ours(args, rank, world):
             "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak / 1e12,
                          "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / peak, "traffic": None,
                          "peak_source": fp64_peak_source()},
-            "gpu_launches": args.steps, "clocks": clk.summary()}
+            "accuracy": accuracy, "gpu_launches": args.steps, "clocks": clk.summary()}
 
 
 def bench_lu_inverse_ours(args, rank, world):
@@ -1081,6 +1106,23 @@ def bench_ls_ours(args, rank, world):
     peak = ctypes_probe(L)
     if np.any(info.cpu().numpy() != 0):
         raise RuntimeError("rank-deficient problems in the LS workload")
+    # every problem against the oracle (QR::new + q_tr_mul + the top-n solve):
+    # the relative difference of the solutions, and the normal-equations
+    # residual ||A^T (A x - b)|| / (||A||^2 ||x||) of the reference's LS test
+    import oracle as O
+
+    _, _, x_ref, _ = O.gels_batched(ms, n, w["a_offsets"], w["a_flat"], w["b_offsets"], w["b_flat"])
+    xg = X.cpu().numpy().reshape(count, n)
+    rel = np.max(np.abs(xg - x_ref), axis=1) / np.max(np.abs(x_ref), axis=1)
+    ne = 0.0
+    for s_ in range(0, count, 64):  # normal equations on every 64th problem
+        m_ = int(ms[s_])
+        am = w["a_flat"][w["a_offsets"][s_]:w["a_offsets"][s_] + m_ * n].reshape(n, m_).T
+        bm = w["b_flat"][w["b_offsets"][s_]:w["b_offsets"][s_] + m_]
+        ne = max(ne, float(np.abs(am.T @ (am @ xg[s_] - bm)).max() / (np.abs(am).sum(axis=0).max() ** 2 *
+                                                                      np.abs(xg[s_]).max())))
+    accuracy = {"problems_checked": count, "solution_rel_diff_vs_oracle_max": float(np.max(rel)),
+                "normal_equations_residual_max_every_64th": ne}
     return {"metric": "solves/s (batched Householder QR least squares, 8192 x m in [128,512] x 64 f64)",
             "value": count / (ms_step * 1e-3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -1090,7 +1132,7 @@ def bench_ls_ours(args, rank, world):
             "roofline": {"bound": "fp64", "achieved": flops / (ms_step * 1e-3) / 1e12, "peak": peak / 1e12,
                          "unit": "TFLOP/s", "frac": flops / (ms_step * 1e-3) / peak, "traffic": None,
                          "peak_source": fp64_peak_source()},
-            "gpu_launches": args.steps, "clocks": clk.summary()}
+            "accuracy": accuracy, "gpu_launches": args.steps, "clocks": clk.summary()}
 
 
 # ----------------------------------------------------------------------------- adjoint
@@ -1263,6 +1305,7 @@ def bench_mixed_lu_ours(args, rank, world):
 
     import torch
 
+    import oracle as O
     from nalgebra_gb300 import _lib, workloads
 
     L = _lib.load()
@@ -1282,6 +1325,7 @@ def bench_mixed_lu_ours(args, rank, world):
         flops = 2.0 / 3.0 * n ** 3 + 2.0 * n ** 2
         for cond in conds:
             A, b = workloads.conditioned_torch(n, cond, seed=int(np.log10(cond)) + n)
+            a_host = b_host = None
             it, berr, fb = ctypes.c_int(0), ctypes.c_double(0.0), ctypes.c_int(0)
 
             def mixed():
@@ -1313,8 +1357,10 @@ def bench_mixed_lu_ours(args, rank, world):
                 ms = float(np.median(times))
                 xr = x.clone()
                 xs[name] = xr
-                r = b - (A.view(n, n).t() @ xr)
-                be = float(r.abs().max() / (A.view(n, n).abs().sum(dim=0).max() * xr.abs().max() + b.abs().max()))
+                # backward error with the residual by Dot2 on the host (outside the timed events)
+                if a_host is None:
+                    a_host, b_host = A.cpu().numpy(), b.cpu().numpy()
+                be = O.dense_backward_error(a_host, n, xr.cpu().numpy(), b_host)
                 res[name] = {"ms": ms, "solves_per_s": 1e3 / ms, "gflops_fp64_equivalent": flops / (ms * 1e-3) / 1e9,
                              "backward_error": be, "backward_error_over_n_eps": be / (n * 2.220446049250313e-16),
                              "clocks": clk.summary()}
@@ -1326,7 +1372,7 @@ def bench_mixed_lu_ours(args, rank, world):
             forms[f"n{n}_cond{cond:.0e}"] = res
             if headline is None or (n == max(sizes) and cond == 1e5):
                 headline = (n, cond, res)
-            del A, b
+            del A, b, a_host, b_host
     n, cond, res = headline
     peak = ctypes_probe(L)
     fp64_rate = res["fp64"]["gflops_fp64_equivalent"] * 1e9
@@ -1342,6 +1388,54 @@ def bench_mixed_lu_ours(args, rank, world):
             "config": {"workload": "mixed_lu", "n": n, "cond": cond, "nrhs": 1, "sizes": sizes,
                        "conds": conds, "inputs": "A = U diag(s) V^T, U, V from QR of N(0,1), s log-uniform"},
             "forms": forms, "roofline": roof, "gpu_launches": None}
+
+
+# ----------------------------------------------------------------------------- every config in one line
+
+def _summary(res: dict, keep=()) -> dict:
+    out = {k: res.get(k) for k in ("metric", "value", "unit", "ms_per_step", "gflops", "dtype", "config", "roofline",
+                                   "clocks", "gpu_launches") if k in res}
+    for k in keep:
+        if k in res:
+            out[k] = res[k]
+    return out
+
+
+def other_configs(args, rank, world) -> dict:
+    """The workloads of the other configurations, each measured in this same
+    run with its own CUDA-event timing and clocks, so that one default bench
+    line carries all of them: batched LU (4096 x 64), mixed LU + refinement
+    (n = 8192 at three condition numbers), the adjoint (2048 x 128, f64 and
+    f32), GEMM 8192^3 (split and FP64) and batched QR least squares (8192
+    problems).  Steps are capped for the large single-matrix workloads."""
+    import copy
+
+    import torch
+
+    out = {}
+    plan = (
+        ("1_lu_batched", bench_lu_ours, dict(), ("accuracy",)),
+        ("3_mixed_lu_n8192", bench_mixed_lu_ours, dict(count=8192, steps=min(args.steps, 2), warmup=1), ("forms",)),
+        ("4_adjoint", bench_adjoint_ours, dict(count=0), ("forms",)),
+        ("5a_gemm", bench_gemm_ours, dict(count=0, steps=min(args.steps, 10)), ("forms",)),
+        ("5b_ls_qr", bench_ls_ours, dict(count=0), ("accuracy",)),
+    )
+    for name, fn, over, keep in plan:
+        a = copy.copy(args)
+        a.count = 0
+        a.exact = False
+        for k, v in over.items():
+            setattr(a, k, v)
+        t0 = time.perf_counter()
+        try:
+            res = fn(a, rank, world)
+            out[name] = _summary(res, keep)
+        except Exception as e:  # one workload's failure is reported, not fatal to the headline
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = round(time.perf_counter() - t0, 2)
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return out
 
 
 # ----------------------------------------------------------------------------- main
@@ -1367,6 +1461,8 @@ def main():
                     help="ragged_cholesky e2e: chunks of the host-memory pipeline (copy in / solve / copy out)")
     ap.add_argument("--profile", action="store_true", help="timed kernel only (for ncu captures)")
     ap.add_argument("--profile-mixed", action="store_true", help="with --profile: also run the mixed-precision form")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="ragged_cholesky: skip the other configurations' workloads in the line's `configs` map")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -1410,6 +1506,10 @@ def main():
     if rank == 0:
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = cpu_baseline_ragged(data)
+    del data
+    if not args.headline_only and world == 1:
+        res["configs"] = other_configs(args, rank, world)
+    if rank == 0:
         print(json.dumps(res))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -414,6 +414,16 @@ int nacu_dgetrf(int n, double* A, int64_t lda, int32_t* ipiv, int32_t* info, voi
 int nacu_dgetrs(int n, const double* LU, int64_t lda, const int32_t* ipiv, double* b, int32_t* info, void* workspace,
                 size_t workspace_bytes, nacu_stream_t stream);
 
+/* Test hook, no counterpart in nalgebra: nacu_dgetrs in which row block
+ * `skip_block` (0-based, 64 rows each) of the unit-lower solve never raises
+ * its ready flag, and every flag wait gives up after `poll_limit` polls
+ * (1 .. 2^22).  The blocks after it run out of their bounded wait, set *info
+ * to -1000 and return, so the call ends with the context usable: the failure
+ * path of the bounded waits, exercised without faulting or hanging a GPU. */
+int nacu_test_dgetrs_flag_timeout(int n, const double* LU, int64_t lda, const int32_t* ipiv, double* b,
+                                  int32_t* info, int skip_block, int poll_limit, void* workspace,
+                                  size_t workspace_bytes, nacu_stream_t stream);
+
 /* Workspace bytes of nacu_dgesv_mixed_ir (FP32 copy of A, split-GEMM slices,
  * vectors, and an FP64 copy of A for the fallback). */
 size_t nacu_gesv_mixed_workspace_bytes(int n);

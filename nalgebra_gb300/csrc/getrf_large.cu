@@ -663,7 +663,10 @@ struct TrsvArgs {
   int lower;
   int32_t* info;
   int* sync;  // [0] ticket, [1] timeout flag, [2 + b] block b solved (zeroed before the launch)
+  int poll_limit;  // polls of one flag before the wait gives up
+  int skip_flag;   // a block that never raises its flag (test hook only; -1 otherwise)
 };
+constexpr int kTrsvPollLimit = 1 << 22;  // with the 64 ns back-off: seconds, far above any block's solve
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
   int v;
@@ -730,7 +733,7 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
     if (tid == 0) {
       int polls = 0;
       while (ld_acquire(&g.sync[2 + jb]) == 0) {
-        if (++polls > (1 << 22)) {
+        if (++polls > g.poll_limit) {
           s_abort = 1;
           atomicExch(&g.sync[1], 1);
           atomicMin(g.info, kTrsvInfoTimeout);
@@ -795,7 +798,7 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
   if (tid < bs) g.x[r0 + tid] = xs[tid];
   __threadfence();
   __syncthreads();
-  if (tid == 0) st_release(&g.sync[2 + kb], 1);
+  if (tid == 0 && kb != g.skip_flag) st_release(&g.sync[2 + kb], 1);
 }
 
 // info holds a large sentinel until some pivot fails; 0 afterwards means "ok".
@@ -1056,7 +1059,8 @@ int getrf_blocked(int n, T* A, int64_t lda, int32_t* ipiv, int32_t* info, void* 
 size_t trsv_sync_bytes(int n) { return ((size_t)n / 64 + 4) * sizeof(int); }
 
 template <typename T>
-int trsv_pair(int n, const T* LU, int64_t lda, T* x, int32_t* info, int* sync, cudaStream_t s, const char* name) {
+int trsv_pair(int n, const T* LU, int64_t lda, T* x, int32_t* info, int* sync, cudaStream_t s, const char* name,
+              int poll_limit = kTrsvPollLimit, int skip_lower_flag = -1) {
   const void* tk = reinterpret_cast<const void*>(trsv_kernel<T>);
   constexpr int BS = TrsvTile<T>::BS;
   const size_t smem = (size_t)BS * (BS + 1) * sizeof(T);
@@ -1066,7 +1070,7 @@ int trsv_pair(int n, const T* LU, int64_t lda, T* x, int32_t* info, int* sync, c
   for (int lower = 1; lower >= 0; --lower) {
     e = cudaMemsetAsync(sync, 0, (size_t)(nblk + 2) * sizeof(int), s);
     if (e != cudaSuccess) return record_cuda_error(e, name);
-    TrsvArgs<T> ta{n, LU, lda, x, lower, info, sync};
+    TrsvArgs<T> ta{n, LU, lda, x, lower, info, sync, poll_limit, lower ? skip_lower_flag : -1};
     trsv_kernel<T><<<nblk, kTrsvThreads, smem, s>>>(ta);
   }
   return check_launch(name);
@@ -1076,7 +1080,7 @@ constexpr size_t kStageLimit = 160 * 1024;
 
 template <typename T>
 int getrs_one(int n, const T* LU, int64_t lda, const int32_t* ipiv, T* x, int32_t* info, int* sync, cudaStream_t s,
-              const char* name) {
+              const char* name, int poll_limit = kTrsvPollLimit, int skip_lower_flag = -1) {
   info_init_kernel<<<1, 1, 0, s>>>(info);
   const size_t stage = (size_t)n * (sizeof(T) + sizeof(int32_t));
   const int staged = stage <= kStageLimit;
@@ -1085,7 +1089,7 @@ int getrs_one(int n, const T* LU, int64_t lda, const int32_t* ipiv, T* x, int32_
     if (e != cudaSuccess) return record_cuda_error(e, name);
   }
   apply_pivots_kernel<T><<<1, 256, staged ? stage : 0, s>>>(n, ipiv, x, staged);
-  int rc = trsv_pair<T>(n, LU, lda, x, info, sync, s, name);
+  int rc = trsv_pair<T>(n, LU, lda, x, info, sync, s, name, poll_limit, skip_lower_flag);
   if (rc != NACU_SUCCESS) return rc;
   info_finalize_kernel<<<1, 1, 0, s>>>(info);
   return check_launch(name);
@@ -1374,6 +1378,24 @@ int nacu_dgetrs(int n, const double* LU, int64_t lda, const int32_t* ipiv, doubl
     return record_arg_error(-7, "dgetrs: workspace too small");
   return getrs_one<double>(n, LU, lda, ipiv, b, info, static_cast<int*>(workspace), (cudaStream_t)stream,
                            "nacu_dgetrs");
+}
+
+int nacu_test_dgetrs_flag_timeout(int n, const double* LU, int64_t lda, const int32_t* ipiv, double* b,
+                                  int32_t* info, int skip_block, int poll_limit, void* workspace,
+                                  size_t workspace_bytes, nacu_stream_t stream) {
+  using namespace nacu;
+  if (n <= 0) return record_arg_error(-1, "test_dgetrs_flag_timeout: n <= 0");
+  if (!LU || !ipiv || !b || !info) return record_arg_error(-2, "test_dgetrs_flag_timeout: null argument");
+  if (lda < n) return record_arg_error(-3, "test_dgetrs_flag_timeout: lda < n");
+  const int nblk = (n + TrsvTile<double>::BS - 1) / TrsvTile<double>::BS;
+  if (skip_block < 0 || skip_block >= nblk)
+    return record_arg_error(-7, "test_dgetrs_flag_timeout: skip_block outside the row blocks");
+  if (poll_limit < 1 || poll_limit > kTrsvPollLimit)
+    return record_arg_error(-8, "test_dgetrs_flag_timeout: poll_limit outside [1, 2^22]");
+  if (!workspace || workspace_bytes < nacu::trsv_sync_bytes(n))
+    return record_arg_error(-10, "test_dgetrs_flag_timeout: workspace too small");
+  return getrs_one<double>(n, LU, lda, ipiv, b, info, static_cast<int*>(workspace), (cudaStream_t)stream,
+                           "nacu_test_dgetrs_flag_timeout", poll_limit, skip_block);
 }
 
 }  // extern "C"

@@ -72,6 +72,9 @@ def lib():
             "orc_dgemm_dot2": (None, [_i64, _i64, _i64, C.c_double, _dp, _i64, _dp, _i64, C.c_double, _dp, _i64, C.c_int]),
             "orc_dbackward_error": (C.c_double, [_i64, _dp, _i64, _dp, _i64, _dp, _i64, _i64]),
             "orc_dlu_reconstruction": (C.c_double, [_i64, _dp, _i64, _dp, _i64, _i32p]),
+            "orc_dposv_ragged_backward_errors": (None, [_i64, _i32p, _i64p, _dp, _i64p, _dp, _dp, _i64, C.c_int,
+                                                        _dp, C.c_int]),
+            "orc_dgesv_backward_error": (C.c_double, [_i64, _dp, _i64, _dp, _dp, C.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -410,3 +413,30 @@ def lu_reconstruction(a, lu_, ipiv) -> float:
     n = a.shape[0]
     return lib().orc_dlu_reconstruction(n, _p(a), max(n, 1), _p(lu_), max(n, 1),
                                         _p(np.ascontiguousarray(ipiv, dtype=np.int32), _i32p))
+
+
+def ragged_backward_errors(ns, aoff, a_flat, boff, b_flat, x_flat, nrhs, symmetric=True, nthreads=0) -> np.ndarray:
+    """Per-system normwise backward error of a ragged batch of solves, max
+    over the right-hand sides, residuals by Dot2 (all host threads).  A is the
+    symmetric matrix of its lower triangle when ``symmetric`` (the SPD
+    solves), else the full stored matrix."""
+    ns = np.ascontiguousarray(ns, dtype=np.int32)
+    aoff = np.ascontiguousarray(aoff, dtype=np.int64)
+    boff = np.ascontiguousarray(boff, dtype=np.int64)
+    a_flat = np.ascontiguousarray(a_flat, dtype=np.float64)
+    b_flat = np.ascontiguousarray(b_flat, dtype=np.float64)
+    x_flat = np.ascontiguousarray(x_flat, dtype=np.float64)
+    out = np.zeros(ns.size, dtype=np.float64)
+    lib().orc_dposv_ragged_backward_errors(ns.size, _p(ns, _i32p), _p(aoff, _i64p), _p(a_flat), _p(boff, _i64p),
+                                           _p(b_flat), _p(x_flat), int(nrhs), int(bool(symmetric)), _p(out),
+                                           nthreads)
+    return out
+
+
+def dense_backward_error(a_colmajor_flat, n, x, b, nthreads=0) -> float:
+    """Normwise backward error of one dense n x n system (A column-major,
+    one right-hand side), residual by Dot2 over all host threads."""
+    a = np.ascontiguousarray(a_colmajor_flat, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    return lib().orc_dgesv_backward_error(int(n), _p(a), int(n), _p(x), _p(b), nthreads)

@@ -254,4 +254,140 @@ double orc_dlu_reconstruction(int64_t n, const double* a, int64_t lda, const dou
   return std::sqrt(num) / (std::sqrt(den) * (double)n * 2.220446049250313e-16);
 }
 
+// ---- accuracy metrics over whole batches (checkers, not restatements) -----
+
+namespace {
+// r = b - A x with every row's sum carried as a Dot2 pair (s, e), A given
+// by columns: column j adds -A(i, j) x_j to every row i.  `sym` takes A as
+// the symmetric matrix of its lower triangle (the only part the Cholesky
+// solvers read, cholesky.rs:221-272).  Returns max_i |r_i| and fills
+// rowabs[i] = sum_j |A(i, j)| when rowabs is given.
+double residual_inf_dd(int64_t n, const double* a, int64_t lda, bool sym, const double* x, const double* b,
+                       double* s, double* e, double* rowabs) {
+  for (int64_t i = 0; i < n; ++i) {
+    s[i] = b[i];
+    e[i] = 0.0;
+    if (rowabs) rowabs[i] = 0.0;
+  }
+  auto acc = [&](int64_t i, double aij, double xj) {
+    double pr, pe, ss, se;
+    two_prod(-aij, xj, &pr, &pe);
+    two_sum(s[i], pr, &ss, &se);
+    s[i] = ss;
+    e[i] += pe + se;
+  };
+  for (int64_t j = 0; j < n; ++j) {
+    const double* col = a + j * lda;
+    const double xj = x[j];
+    if (sym) {
+      // lower column j: rows i >= j get A(i, j) x_j; row j gets A(i, j) x_i
+      // for i > j (the mirrored upper entries A(j, i)).
+      acc(j, col[j], xj);
+      if (rowabs) rowabs[j] += std::fabs(col[j]);
+      for (int64_t i = j + 1; i < n; ++i) {
+        acc(i, col[i], xj);
+        acc(j, col[i], x[i]);
+        if (rowabs) {
+          rowabs[i] += std::fabs(col[i]);
+          rowabs[j] += std::fabs(col[i]);
+        }
+      }
+    } else {
+      for (int64_t i = 0; i < n; ++i) {
+        acc(i, col[i], xj);
+        if (rowabs) rowabs[i] += std::fabs(col[i]);
+      }
+    }
+  }
+  double rmax = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double r = std::fabs(s[i] + e[i]);
+    if (!(r <= rmax)) rmax = r;  // a NaN residual propagates
+  }
+  return rmax;
+}
+
+double normwise_berr(double rmax, double anorm, const double* x, const double* b, int64_t n) {
+  double xmax = 0.0, bmax = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    xmax = std::fmax(xmax, std::fabs(x[i]));
+    bmax = std::fmax(bmax, std::fabs(b[i]));
+  }
+  const double den = anorm * xmax + bmax;
+  if (rmax != rmax) return NAN;
+  return den > 0.0 ? rmax / den : (rmax > 0.0 ? INFINITY : 0.0);
+}
+}  // namespace
+
+// Per-system normwise backward error of a ragged batch of solves (max over
+// the system's right-hand sides), A taken from its lower triangle when `sym`
+// (the SPD solves) or as stored otherwise (the LU solves):
+// berr[s] = max_c ||b_c - A x_c||_inf / (||A||_inf ||x_c||_inf + ||b_c||_inf),
+// residuals by Dot2.  Systems run in parallel over the host threads.
+void orc_dposv_ragged_backward_errors(int64_t count, const int32_t* ns, const int64_t* aoff, const double* a,
+                                      const int64_t* boff, const double* b, const double* x, int64_t nrhs,
+                                      int sym, double* berr, int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel
+  {
+    std::vector<double> s, e, rowabs;
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t q = 0; q < count; ++q) {
+      const int64_t n = ns[q];
+      s.resize(n);
+      e.resize(n);
+      rowabs.resize(n);
+      const double* aq = a + aoff[q];
+      double worst = 0.0;
+      for (int64_t c = 0; c < nrhs; ++c) {
+        const double* bc = b + boff[q] + c * n;
+        const double* xc = x + boff[q] + c * n;
+        const double rmax = residual_inf_dd(n, aq, n, sym != 0, xc, bc, s.data(), e.data(), c ? nullptr : rowabs.data());
+        double anorm = 0.0;
+        for (int64_t i = 0; i < n; ++i) anorm = std::fmax(anorm, rowabs[i]);
+        const double be = normwise_berr(rmax, anorm, xc, bc, n);
+        if (!(be <= worst)) worst = be;
+      }
+      berr[q] = worst;
+    }
+  }
+}
+
+// Normwise backward error of one large dense system with one right-hand side,
+// the residual by Dot2, rows split over the host threads (each thread walks
+// every column over its own row block, so A is read by contiguous segments).
+double orc_dgesv_backward_error(int64_t n, const double* a, int64_t lda, const double* x, const double* b,
+                                int nthreads) {
+  set_threads(nthreads);
+  std::vector<double> s(n), e(n), rowabs(n, 0.0);
+  for (int64_t i = 0; i < n; ++i) {
+    s[i] = b[i];
+    e[i] = 0.0;
+  }
+  const int64_t blk = 256;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t i0 = 0; i0 < n; i0 += blk) {
+    const int64_t i1 = i0 + blk < n ? i0 + blk : n;
+    for (int64_t j = 0; j < n; ++j) {
+      const double* col = a + j * lda;
+      const double xj = x[j];
+      for (int64_t i = i0; i < i1; ++i) {
+        double pr, pe, ss, se;
+        two_prod(-col[i], xj, &pr, &pe);
+        two_sum(s[i], pr, &ss, &se);
+        s[i] = ss;
+        e[i] += pe + se;
+        rowabs[i] += std::fabs(col[i]);
+      }
+    }
+  }
+  double rmax = 0.0, anorm = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double r = std::fabs(s[i] + e[i]);
+    if (!(r <= rmax)) rmax = r;
+    anorm = std::fmax(anorm, rowabs[i]);
+  }
+  return normwise_berr(rmax, anorm, x, b, n);
+}
+
 }  // extern "C"

@@ -213,3 +213,21 @@ def test_mirror_host_solve(cuda):
         xs = x[w["b_offsets"][s]:w["b_offsets"][s] + 2 * n].reshape(2, n).T
         bs = w["b_flat"][w["b_offsets"][s]:w["b_offsets"][s] + 2 * n].reshape(2, n).T
         assert O.backward_error(a, xs, bs) <= n * EPS64
+
+
+def test_2000_systems_without_verify_every_system_meets_n_eps(cuda):
+    """2000 systems of the ragged SPD workload (n ~ U[8, 256], A = B B^T + n I,
+    4 right-hand sides) through nacu_dposv_ragged_mixed WITHOUT
+    NACU_FLAG_VERIFY, where the kernel may stop on its predicted convergence
+    instead of a last residual: the backward error of EVERY system, with the
+    residual by Dot2 on the host, is <= n eps64, and the solutions agree with
+    the oracle's FP64 Cholesky::solve (cholesky.rs:122-143)."""
+    w = W.ragged_spd(2000, 8, 256, nrhs=4, seed=0)
+    ns = w["ns"]
+    A, B, X, info, iters, aoff, boff = _mixed(cuda, ns, w["a_flat"], w["b_flat"], 4, 0)
+    assert np.all(info == 0) and np.all(iters > 0)
+    be = O.ragged_backward_errors(ns, aoff, w["a_flat"], boff, w["b_flat"], X, 4)
+    units = be / (ns * EPS64)
+    assert np.all(units <= 1.0), (float(units.max()), int(np.sum(units > 1.0)))
+    _, xo, _, _ = O.posv_ragged(ns, w["a_offsets"], w["a_flat"], w["b_offsets"], w["b_flat"], 4)
+    assert np.allclose(X, xo, rtol=1e-12, atol=1e-14)

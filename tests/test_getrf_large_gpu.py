@@ -92,3 +92,38 @@ def test_grid_form_panels_large_n(cuda):
     r = b - a @ x
     berr = np.abs(r).max() / (np.abs(a).sum(axis=1).max() * np.abs(x).max() + np.abs(b).max())
     assert berr <= 10 * n * EPS64
+
+
+def test_flag_wait_runs_out_and_reports(cuda):
+    """The triangular solve's bounded flag wait (one CTA per 64-row block,
+    each waiting on the ready flags of the blocks before it): with block 3's
+    flag never raised and a short poll limit, the later blocks give up, info
+    is -1000, the call returns, and the same factors then solve correctly on
+    the same context -- the failure path, without faulting or hanging the GPU."""
+    torch = cuda
+    n = 1000  # 16 row blocks, all resident at once
+    rng = np.random.default_rng(17)
+    a = rng.standard_normal((n, n))
+    b = rng.standard_normal(n)
+    lu, ipiv, info, _, _ = _getrf(cuda, a)
+    assert info == 0
+    L = _lib.load()
+    LU = torch.from_numpy(np.asfortranarray(lu).ravel(order="F")).cuda()
+    P = torch.from_numpy(ipiv.astype(np.int32)).cuda()
+    ws = torch.zeros(L.nacu_getrf_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    X = torch.from_numpy(b.copy()).cuda()
+    inf = torch.full((1,), -7, dtype=torch.int32, device="cuda")
+    _lib.call("nacu_test_dgetrs_flag_timeout", n, LU.data_ptr(), n, P.data_ptr(), X.data_ptr(), inf.data_ptr(), 3,
+              4096, ws.data_ptr(), ws.numel(), s)
+    torch.cuda.synchronize()
+    assert int(inf.item()) == -1000
+    with pytest.raises(_lib.NacuError):  # a skip_block outside the row blocks is an argument error
+        _lib.call("nacu_test_dgetrs_flag_timeout", n, LU.data_ptr(), n, P.data_ptr(), X.data_ptr(), inf.data_ptr(),
+                  16, 4096, ws.data_ptr(), ws.numel(), s)
+    X.copy_(torch.from_numpy(b))
+    _lib.call("nacu_dgetrs", n, LU.data_ptr(), n, P.data_ptr(), X.data_ptr(), inf.data_ptr(), ws.data_ptr(),
+              ws.numel(), s)
+    torch.cuda.synchronize()
+    assert int(inf.item()) == 0
+    assert O.backward_error(a, X.cpu().numpy(), b) <= 10 * n * EPS64

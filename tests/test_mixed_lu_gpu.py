@@ -113,3 +113,49 @@ def test_mirror_large_lu_and_refined_solve(cuda):
     c = DeviceMatrix.from_numpy(np.zeros((n, 1)))
     gemm(c, 1.0, DeviceMatrix.from_numpy(a), xr, 0.0)
     assert np.allclose(c.to_numpy().ravel(), b, rtol=0, atol=1e-10 * np.abs(b).max())
+
+
+@pytest.fixture(scope="module")
+def config3_systems(cuda):
+    """The mixed-LU workload at n = 4096: A = U diag(s) V^T with U, V from the
+    QR of N(0,1) matrices and s log-uniform, cond 1e2 / 1e5 / 1e8, one RHS."""
+    out = {}
+    for cond in (1e2, 1e5, 1e8):
+        A, b = workloads.conditioned_torch(4096, cond, seed=int(np.log10(cond)) + 4096)
+        a = A.cpu().numpy().reshape(4096, 4096).T  # the device buffer is column-major
+        out[cond] = (np.asfortranarray(a), b.cpu().numpy())
+        del A, b
+    return out
+
+
+@pytest.mark.parametrize("cond", [1e2, 1e5, 1e8])
+def test_config3_size_backward_error_and_fallback(cuda, config3_systems, cond):
+    """n = 4096 at the three configured condition numbers: the backward error
+    (residual by Dot2 on the host) is <= n eps64 for every condition number,
+    FP32 refinement converges at 1e2 and 1e5 (u32 * cond < 1), and exactly the
+    1e8 system takes the FP64 fallback (u32 * cond > 1)."""
+    a, b = config3_systems[cond]
+    n = a.shape[0]
+    x, iters, berr, fb = _solve(cuda, a, b)
+    assert fb == (1 if cond == 1e8 else 0)
+    assert np.all(np.isfinite(x))
+    host_berr = O.dense_backward_error(a.ravel(order="F"), n, x, b)
+    assert host_berr <= n * EPS64
+    assert berr <= n * EPS64
+
+
+def test_config3_size_fp64_pivots_match_lapack(cuda, config3_systems):
+    """The plain FP64 form at n = 4096 (nacu_dgetrf + nacu_dgetrs) on the
+    cond-1e5 system: the same pivot sequence as LAPACK's partial pivoting
+    (largest |x|, first on ties: nalgebra's icamax rule), ||PA - LU|| <=
+    10 n eps and backward error <= 10 n eps64."""
+    sla = pytest.importorskip("scipy.linalg")
+    from tests.test_getrf_large_gpu import _getrf
+
+    a, b = config3_systems[1e5]
+    n = a.shape[0]
+    lu, ipiv, info, x, info2 = _getrf(cuda, a, b)
+    assert info == 0 and info2 == 0
+    _, piv_ref = sla.lu_factor(a, check_finite=False)
+    assert np.array_equal(ipiv, piv_ref)
+    assert O.dense_backward_error(a.ravel(order="F"), n, x, b) <= 10 * n * EPS64

@@ -643,3 +643,36 @@ def test_triangular_solves_match_pure_python_restatement_bitwise(n):
             assert np.array_equal(np.asarray(got).ravel(), np.array(ref)), (upper, trans)
     got = O.triangular_solve(t, b, diag=2.5)
     assert np.array_equal(np.asarray(got).ravel(), np.array(_pure_python_trsv(t, b, False, False, diag=2.5)))
+
+
+def test_batch_backward_error_helpers_match_per_system_metric():
+    """The batch checkers the bench and the GPU tests use (Dot2 residuals,
+    per system; one large dense system) agree with the per-system
+    backward_error on the symmetric matrix of the lower triangle, and with
+    numpy's extended-precision residual."""
+    from nalgebra_gb300 import workloads as W
+
+    w = W.ragged_spd(40, 1, 40, nrhs=3, seed=9)
+    ns, aoff, boff = w["ns"], w["a_offsets"], w["b_offsets"]
+    a_flat = w["a_flat"].copy()
+    for s in range(ns.size):  # garbage in the strict upper part: only the lower triangle counts
+        n = int(ns[s])
+        m = a_flat[aoff[s]:aoff[s] + n * n].reshape(n, n)
+        m[np.tril_indices(n, -1)] = 1e3
+    _, x, _, _ = O.posv_ragged(ns, aoff, w["a_flat"], boff, w["b_flat"], 3)
+    x = x + 1e-9  # a visible error
+    be = O.ragged_backward_errors(ns, aoff, a_flat, boff, w["b_flat"], x, 3)
+    for s in range(ns.size):
+        n = int(ns[s])
+        a = w["a_flat"][aoff[s]:aoff[s] + n * n].reshape(n, n).T
+        a = np.tril(a) + np.tril(a, -1).T
+        xs = x[boff[s]:boff[s] + 3 * n].reshape(3, n).T
+        bs = w["b_flat"][boff[s]:boff[s] + 3 * n].reshape(3, n).T
+        assert be[s] == pytest.approx(O.backward_error(a, xs, bs), rel=1e-12)
+    rng = np.random.default_rng(4)
+    n = 300
+    a = rng.standard_normal((n, n))
+    xx = rng.standard_normal(n)
+    bb = a @ xx
+    ref = O.backward_error(a, xx, bb)
+    assert O.dense_backward_error(a.ravel(order="F"), n, xx, bb) == pytest.approx(ref, rel=1e-12)
