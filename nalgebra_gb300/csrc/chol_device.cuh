@@ -152,10 +152,8 @@ __device__ void chol_factor_cta(int n, T* __restrict__ a, int ldp, T* __restrict
     if (*s_info != 0) return;
     // Phase 4: write the finished panel back (lower part; the strict upper
     // triangle of the diagonal block was never modified).
-    for (int e = tid; e < rows * jb; e += nthr) {
-      const int c = e / rows, r = e - c * rows;
-      if (r >= c) a[(size_t)(J0 + c) * n + J0 + r] = P[(size_t)c * ldp + r];
-    }
+    for (int c = warp; c < jb; c += nthr >> 5)
+      for (int r = c + lane; r < rows; r += 32) a[(size_t)(J0 + c) * n + J0 + r] = P[(size_t)c * ldp + r];
     __syncthreads();
   }
 }

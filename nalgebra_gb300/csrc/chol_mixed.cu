@@ -154,22 +154,22 @@ __device__ __noinline__ void solve32_scaled(int n, const float* L32, const doubl
     s_up[tid] = __longlong_as_double((1023 + e_dn) << 52);
   }
   __syncthreads();
-  for (int e = tid; e < n * nr; e += kCholThreads) {
-    const int c = e / n, r = e - c * n;
-    X32[(size_t)c * ldx + r] = (float)(src[(size_t)c * ldsrc + r] * s_down[c]);
-  }
+  for (int c = 0; c < nr; ++c)
+    for (int r = tid; r < n; r += kCholThreads) X32[(size_t)c * ldx + r] = (float)(src[(size_t)c * ldsrc + r] * s_down[c]);
   __syncthreads();
   chol_forward_cta<false, float>(n, L32, X32, ldx, nr, rdiag32);
   chol_backward_fast_cta<float>(n, L32, X32, ldx, nr, rdiag32);
   unsigned long long dn[kRhsChunk] = {0, 0, 0, 0};
-  for (int e = tid; e < n * nr; e += kCholThreads) {
-    const int c = e / n, r = e - c * n;
-    const double d = (double)X32[(size_t)c * ldx + r] * s_up[c];
-    const unsigned long long ab = abs_bits(d);
-    dn[c] = ab > dn[c] ? ab : dn[c];
-    if (accumulate) dst[(size_t)c * ldx + r] += d;
-    else dst[(size_t)c * ldx + r] = d;
-  }
+#pragma unroll
+  for (int c = 0; c < kRhsChunk; ++c)
+    if (c < nr)
+      for (int r = tid; r < n; r += kCholThreads) {
+        const double d = (double)X32[(size_t)c * ldx + r] * s_up[c];
+        const unsigned long long ab = abs_bits(d);
+        dn[c] = ab > dn[c] ? ab : dn[c];
+        if (accumulate) dst[(size_t)c * ldx + r] += d;
+        else dst[(size_t)c * ldx + r] = d;
+      }
   if (dnorm_out) block_max4_to(dn, red, dnorm_out);
 }
 
@@ -208,21 +208,25 @@ __device__ __noinline__ void chol_factor32_cta(int n, float* __restrict__ a, int
       for (int kb = 0; kb < J0; kb += kKB) {
         const int kw = min(kKB, J0 - kb);
         __syncthreads();
-        {  // stage L[J0.., kb..kb+kw) (batched loads, then the shared stores)
-          const int tot = rows * kw;
-          for (int e0 = tid; e0 < tot; e0 += 4 * nthr) {
-            float v[4];
+        {  // stage L[J0.., kb..kb+kw): a warp per column, eight coalesced
+           // loads in flight per lane, then the shared stores.  No index
+           // division per element: the staged elements number the panel's
+           // FMAs / 16, and an integer division costs ~20 instructions.
+          for (int c = warp; c < kw; c += nthr >> 5) {
+            const float* src = a + (size_t)(kb + c) * n + J0;
+            float* dst = Lb + (size_t)c * ldl;
+            for (int r0 = 0; r0 < rows; r0 += 8 * 32) {
+              float v[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const int e = e0 + u * nthr;
-              const int c = e / rows, r = e - c * rows;
-              v[u] = (e < tot) ? a[(size_t)(kb + c) * n + J0 + r] : 0.f;
-            }
+              for (int u = 0; u < 8; ++u) {
+                const int r = r0 + u * 32 + lane;
+                v[u] = (r < rows) ? src[r] : 0.f;
+              }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const int e = e0 + u * nthr;
-              const int c = e / rows, r = e - c * rows;
-              if (e < tot) Lb[(size_t)c * ldl + r] = v[u];
+              for (int u = 0; u < 8; ++u) {
+                const int r = r0 + u * 32 + lane;
+                if (r < rows) dst[r] = v[u];
+              }
             }
           }
         }
@@ -322,10 +326,8 @@ __device__ __noinline__ void chol_factor32_cta(int n, float* __restrict__ a, int
     }
     __syncthreads();
     if (*s_info != 0) return;
-    for (int e = tid; e < rows * jb; e += nthr) {
-      const int c = e / rows, r = e - c * rows;
-      if (r >= c) a[(size_t)(J0 + c) * n + J0 + r] = P[(size_t)c * ldp + r];
-    }
+    for (int c = warp; c < jb; c += nthr >> 5)
+      for (int r = c + lane; r < rows; r += 32) a[(size_t)(J0 + c) * n + J0 + r] = P[(size_t)c * ldp + r];
     __syncthreads();
   }
 }
@@ -423,11 +425,13 @@ __device__ void mixed_one(const MixedArgs& g, int s, unsigned char* smem, int* s
   }
   {
     unsigned long long bv[kRhsChunk] = {0, 0, 0, 0};
-    for (int e = tid; e < n * g.nrhs; e += kCholThreads) {
-      const int c = e / n;
-      const unsigned long long ab = abs_bits(b[e]);
-      if (c < kRhsChunk) bv[c] = ab > bv[c] ? ab : bv[c];
-    }
+#pragma unroll
+    for (int c = 0; c < kRhsChunk; ++c)
+      if (c < g.nrhs)
+        for (int r = tid; r < n; r += kCholThreads) {
+          const unsigned long long ab = abs_bits(b[(size_t)c * n + r]);
+          bv[c] = ab > bv[c] ? ab : bv[c];
+        }
     block_max4_to(bv, red, nrm + kBn);
   }
   double anorm = 0.0;
@@ -456,13 +460,15 @@ __device__ void mixed_one(const MixedArgs& g, int s, unsigned char* smem, int* s
       }
       {
         unsigned long long rn[kRhsChunk] = {0, 0, 0, 0}, xn[kRhsChunk] = {0, 0, 0, 0};
-        for (int e = tid; e < n * nr; e += kCholThreads) {
-          const int c = e / n, r = e - c * n;
-          const unsigned long long ra = abs_bits(Rd[(size_t)c * ldp + r]);
-          const unsigned long long xa = abs_bits(Xd[(size_t)c * ldp + r]);
-          rn[c] = ra > rn[c] ? ra : rn[c];
-          xn[c] = xa > xn[c] ? xa : xn[c];
-        }
+#pragma unroll
+        for (int c = 0; c < kRhsChunk; ++c)
+          if (c < nr)
+            for (int r = tid; r < n; r += kCholThreads) {
+              const unsigned long long ra = abs_bits(Rd[(size_t)c * ldp + r]);
+              const unsigned long long xa = abs_bits(Xd[(size_t)c * ldp + r]);
+              rn[c] = ra > rn[c] ? ra : rn[c];
+              xn[c] = xa > xn[c] ? xa : xn[c];
+            }
         block_max4_to(rn, red, nrm + kRn);
         block_max4_to(xn, red, nrm + kXn);
       }
@@ -513,10 +519,8 @@ __device__ void mixed_one(const MixedArgs& g, int s, unsigned char* smem, int* s
     return;
   }
   if (status == 0)
-    for (int e = tid; e < n * nr; e += kCholThreads) {
-      const int c = e / n, r = e - c * n;
-      x[e] = Xd[(size_t)c * ldp + r];
-    }
+    for (int c = 0; c < nr; ++c)
+      for (int r = tid; r < n; r += kCholThreads) x[(size_t)c * n + r] = Xd[(size_t)c * ldp + r];
   if (tid == 0) {
     if (g.info) g.info[s] = status;
     if (g.iters) g.iters[s] = used;
