@@ -1292,6 +1292,87 @@ def bench_gemm_ours(args, rank, world):
             "gpu_launches": args.steps * 5}
 
 
+# ----------------------------------------------------------------------------- batched Mul
+
+def bench_mul_batched_ours(args, rank, world):
+    """Many `&a * &b` products of the reference's mat100_mul_mat100 shape
+    (benches/core/matrix.rs:211-224): 4096 products of 100 x 100 f64 matrices
+    (entries N(0,1)) in one nacu_dgemm_batched launch, the FMA form and the
+    EXACT form (nalgebra's gemv order).  Inputs (3 x 328 MB) exceed L2."""
+    import torch
+
+    from nalgebra_gb300 import _lib
+
+    L = _lib.load()
+    count = args.count or 4096
+    m = n = k = 100
+    g = torch.Generator(device="cuda")
+    g.manual_seed(100 + rank)
+    A = torch.randn((count, k, m), dtype=torch.float64, device="cuda", generator=g)  # column-major images
+    B = torch.randn((count, n, k), dtype=torch.float64, device="cuda", generator=g)
+    C = torch.empty((count, n, m), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    flops = 2.0 * m * n * k * count
+    peak = ctypes_probe(L)
+    res = {}
+    for name, flags in (("fma", 0), ("exact", 1)):
+        def launch():
+            _lib.call("nacu_dgemm_batched", m, n, k, 1.0, A.data_ptr(), m, m * k, B.data_ptr(), k, k * n, 0.0,
+                      C.data_ptr(), m, m * n, count, flags, sp)
+
+        for _ in range(args.warmup):
+            launch()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            for i in range(args.steps):
+                ev[i][0].record(stream)
+                launch()
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()
+        ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+        res[name] = {"ms": ms, "products_per_s": count / (ms * 1e-3), "gflops": flops / (ms * 1e-3) / 1e9,
+                     "frac_of_fp64_peak": flops / (ms * 1e-3) / peak, "clocks": clk.summary()}
+    # accuracy on a sample: EXACT against the oracle's gemv order (bit for bit),
+    # the FMA form against the compensated oracle
+    import oracle as O
+
+    sample = np.arange(0, count, max(1, count // 16))
+    a_s = np.transpose(A[sample].cpu().numpy(), (0, 2, 1))
+    b_s = np.transpose(B[sample].cpu().numpy(), (0, 2, 1))
+    exact_c = np.transpose(C[sample].cpu().numpy(), (0, 2, 1))  # the last launch was the EXACT form
+    identical = bool(np.array_equal(exact_c, O.gemm_gemv_order(1.0, a_s, b_s)))
+    _lib.call("nacu_dgemm_batched", m, n, k, 1.0, A.data_ptr(), m, m * k, B.data_ptr(), k, k * n, 0.0, C.data_ptr(), m,
+              m * n, count, 0, sp)
+    fma_c = np.transpose(C[sample].cpu().numpy(), (0, 2, 1))
+    err = max(float(np.max(np.abs(fma_c[i] - O.gemm_dot2(1.0, a_s[i], b_s[i])) / (np.abs(a_s[i]) @ np.abs(b_s[i]))))
+              for i in range(len(sample)))
+    # CPU: nalgebra's gemv-order product restated (the oracle), all host threads, a bounded sample
+    threads = O.max_threads()
+    ks = count
+    a_h = np.transpose(A[:ks].cpu().numpy(), (0, 2, 1))
+    b_h = np.transpose(B[:ks].cpu().numpy(), (0, 2, 1))
+    t0 = time.perf_counter()
+    O.gemm_gemv_order(1.0, a_h, b_h, nthreads=threads)
+    dt = time.perf_counter() - t0
+    fr = res["fma"]
+    return {"metric": "products/s (batched Mul, 4096 x (100x100 * 100x100) f64)", "value": fr["products_per_s"],
+            "unit": "products/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": fr["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mul_batched", "count": count, "m": m, "n": n, "k": k,
+                       "shape": "benches/core/matrix.rs mat100_mul_mat100", "l2": "inputs 983 MB, larger than L2"},
+            "gflops": fr["gflops"], "forms": res,
+            "roofline": {"bound": "fp64", "achieved": fr["gflops"] / 1e3, "peak": peak / 1e12, "unit": "TFLOP/s",
+                         "frac": fr["frac_of_fp64_peak"], "traffic": None, "peak_source": fp64_peak_source(),
+                         "note": "2 m n k flops per product"},
+            "accuracy": {"exact_bit_identical_to_gemv_order_sample": identical, "sample": int(len(sample)),
+                         "fma_max_err_rel_to_absAabsB": err},
+            "cpu_baseline": {"value": ks / dt, "unit": "products/s", "cores": threads, "kind": "port",
+                             "sample": f"{ks} products, nalgebra's gemv-order product (the oracle), {dt:.2f} s"},
+            "gpu_launches": 2 * args.steps, "clocks": fr["clocks"]}
+
+
 # ----------------------------------------------------------------------------- mixed LU + refinement
 
 def bench_mixed_lu_ours(args, rank, world):
@@ -1419,6 +1500,7 @@ def other_configs(args, rank, world) -> dict:
         ("4_adjoint", bench_adjoint_ours, dict(count=0), ("forms",)),
         ("5a_gemm", bench_gemm_ours, dict(count=0, steps=min(args.steps, 10)), ("forms",)),
         ("5b_ls_qr", bench_ls_ours, dict(count=0), ("accuracy",)),
+        ("f2_mul_batched_100", bench_mul_batched_ours, dict(count=0), ("forms", "accuracy", "cpu_baseline")),
     )
     for name, fn, over, keep in plan:
         a = copy.copy(args)
@@ -1448,7 +1530,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
                                                                   "mixed_lu", "lu_inverse", "trsv_batched", "chol_update",
-                                                                        "full_piv_lu", "col_piv_qr"])
+                                                                        "full_piv_lu", "col_piv_qr", "mul_batched"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--single-launch", action="store_true",
                     help="ragged_cholesky: one launch over a host-sorted order with the default tile "
@@ -1487,13 +1569,14 @@ def main():
         torch.distributed.barrier()
 
     if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse", "trsv_batched",
-                         "chol_update", "full_piv_lu", "col_piv_qr"):
+                         "chol_update", "full_piv_lu", "col_piv_qr", "mul_batched"):
         res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
                "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours,
                "lu_inverse": bench_lu_inverse_ours, "trsv_batched": bench_trsv_ours,
                "chol_update": bench_chol_update_ours,
                "full_piv_lu": bench_full_piv_lu_ours,
-               "col_piv_qr": bench_col_piv_qr_ours}[args.workload](args, rank, world)
+               "col_piv_qr": bench_col_piv_qr_ours, "mul_batched": bench_mul_batched_ours}[args.workload](args, rank,
+                                                                                                        world)
         if rank == 0:
             print(json.dumps(res))
         return

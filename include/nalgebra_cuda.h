@@ -451,6 +451,20 @@ int nacu_dgesv_mixed_ir(int n, const double* A, int64_t lda, const double* b, do
 int nacu_dgemm(int m, int n, int k, double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
                double beta, double* C, int64_t ldc, nacu_stream_t stream);
 
+/* Many independent products in one launch: C_s = alpha * A_s * B_s + beta *
+ * C_s for s < batch, each m x k by k x n, column-major with leading dimensions
+ * lda / ldb / ldc, product s at A + s*strideA, B + s*strideB, C + s*strideC.
+ * The batched form of `&a * &b` (src/base/ops.rs:566-570: gemm_uninit with
+ * alpha = 1, beta = 0) and of `Matrix::gemm` (src/base/blas.rs:729-746).
+ * beta == 0: C is never read.  NACU_FLAG_EXACT: nalgebra's gemv order of
+ * gemm_uninit (src/base/blas_uninit.rs:127-176, 320-332; the order nalgebra
+ * uses when a dimension is <= 5 or the sizes are static), bit for bit;
+ * default: one FMA per step, alpha and beta applied at the end.  Any m, n, k
+ * (tiles of up to 64 x 64 per CTA). */
+int nacu_dgemm_batched(int m, int n, int k, double alpha, const double* A, int64_t lda, int64_t strideA,
+                       const double* B, int64_t ldb, int64_t strideB, double beta, double* C, int64_t ldc,
+                       int64_t strideC, int batch, int flags, nacu_stream_t stream);
+
 /* Workspace bytes of nacu_dgemm_split_bf16 (BF16 slices of A and B, padded to
  * the 128 x 256 x 64 tiles, and the row / column exponents). */
 size_t nacu_gemm_split_workspace_bytes(int m, int n, int k);

@@ -35,6 +35,7 @@ from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 
 __all__ = [
     "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch", "solve_refined", "gemm",
+    "gemm_batched",
     "PosvLogdet", "cholesky_solve_refined_host",
     "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE", "FullPivLU", "ColPivQR",
 ]
@@ -535,6 +536,24 @@ def gemm(c: DeviceMatrix, alpha: float, a: DeviceMatrix, b: DeviceMatrix, beta: 
     else:
         _lib.call("nacu_dgemm", m, n, k, float(alpha), a.data.data_ptr(), max(m, 1), b.data.data_ptr(), max(k, 1),
                   float(beta), c.data.data_ptr(), max(m, 1), _stream_ptr())
+    return c
+
+
+def gemm_batched(c, alpha: float, a, b, beta: float, flags: int = 0):
+    """Matrix::gemm over a batch (src/base/blas.rs:729-746): c[s] = alpha a[s]
+    b[s] + beta c[s], in place, for CUDA float64 tensors of shapes (batch, k,
+    m), (batch, n, k) and (batch, n, m) -- each product's column-major image,
+    i.e. the transposed row-major view.  ``a @ b`` for many matrices
+    (src/base/ops.rs:566-570) is alpha = 1, beta = 0.  FLAG_EXACT: nalgebra's
+    gemv summation order, bit for bit."""
+    _torch()
+    batch, k, m = a.shape
+    batch2, n, k2 = b.shape
+    assert batch == batch2 and k == k2 and tuple(c.shape) == (batch, n, m), "gemm_batched dimension mismatch"
+    for t in (a, b, c):
+        assert t.is_contiguous() and t.dtype == _torch().float64 and t.is_cuda, "contiguous CUDA float64 tensors"
+    _lib.call("nacu_dgemm_batched", m, n, k, float(alpha), a.data_ptr(), max(m, 1), m * k, b.data_ptr(), max(k, 1),
+              k * n, float(beta), c.data_ptr(), max(m, 1), m * n, batch, int(flags), _stream_ptr())
     return c
 
 

@@ -76,6 +76,7 @@ SIGNATURES = {
     "nacu_dgesv_mixed_ir": (_i, [_i, _vp, _i64, _vp, _vp, _d, _i, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                  C.POINTER(C.c_int), _vp, _sz, _vp]),
     "nacu_dgemm": (_i, [_i, _i, _i, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64, _vp]),
+    "nacu_dgemm_batched": (_i, [_i, _i, _i, _d, _vp, _i64, _i64, _vp, _i64, _i64, _d, _vp, _i64, _i64, _i, _i, _vp]),
     "nacu_gemm_split_workspace_bytes": (_sz, [_i, _i, _i]),
     "nacu_dgemm_split_bf16": (_i, [_i, _i, _i, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64, _i, _vp, _sz, _vp]),
     "nacu_split_gemm_error": (_i, [C.POINTER(C.c_int)]),

@@ -70,6 +70,8 @@ def lib():
             "orc_dposv_ragged": (None, [_i64, _i32p, _i64p, _dp, _i64p, _dp, _i64, _i32p, _dp, C.c_int]),
             "orc_dgels_batched": (None, [_i64, _i32p, _i64, _i64p, _dp, _i64p, _dp, _dp, _dp, _i32p, C.c_int]),
             "orc_dgemm_dot2": (None, [_i64, _i64, _i64, C.c_double, _dp, _i64, _dp, _i64, C.c_double, _dp, _i64, C.c_int]),
+            "orc_dgemm_gemv_order_batched": (None, [_i64, _i64, _i64, C.c_double, _dp, _i64, _i64, _dp, _i64, _i64,
+                                                    C.c_double, _dp, _i64, _i64, _i64, C.c_int]),
             "orc_dbackward_error": (C.c_double, [_i64, _dp, _i64, _dp, _i64, _dp, _i64, _i64]),
             "orc_dlu_reconstruction": (C.c_double, [_i64, _dp, _i64, _dp, _i64, _i32p]),
             "orc_dposv_ragged_backward_errors": (None, [_i64, _i32p, _i64p, _dp, _i64p, _dp, _dp, _i64, C.c_int,
@@ -395,6 +397,28 @@ def gemm_dot2(alpha, a, b, beta=0.0, c=None, nthreads=0):
     out = np.zeros((m, n), dtype=np.float64, order="F") if c is None else np.array(c, dtype=np.float64, order="F", copy=True)
     lib().orc_dgemm_dot2(m, n, k, alpha, _p(a), max(m, 1), _p(b), max(k, 1), beta, _p(out), max(m, 1), nthreads)
     return out
+
+
+def gemm_gemv_order(alpha, a, b, beta=0.0, c=None, nthreads=0):
+    """alpha*A*B + beta*C in nalgebra's gemv order (gemm_uninit's path for a
+    dimension <= 5 or static sizes, blas_uninit.rs:187-333).  a: (m, k), b:
+    (k, n), or batches (batch, m, k) / (batch, k, n); returns the product(s)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    single = a.ndim == 2
+    if single:
+        a, b = a[None], b[None]
+        c = None if c is None else np.asarray(c, dtype=np.float64)[None]
+    batch, m, k = a.shape
+    n = b.shape[2]
+    af = np.ascontiguousarray(np.transpose(a, (0, 2, 1)))  # column-major per product
+    bf = np.ascontiguousarray(np.transpose(b, (0, 2, 1)))
+    cf = (np.zeros((batch, n, m)) if c is None
+          else np.array(np.transpose(np.asarray(c, dtype=np.float64), (0, 2, 1)), order="C", copy=True))
+    lib().orc_dgemm_gemv_order_batched(m, n, k, alpha, _p(af), max(m, 1), m * k, _p(bf), max(k, 1), k * n, beta,
+                                       _p(cf), max(m, 1), m * n, batch, nthreads)
+    out = np.transpose(cf, (0, 2, 1))
+    return out[0] if single else out
 
 
 def backward_error(a, x, b) -> float:

@@ -157,6 +157,17 @@ void orc_dgels_batched(int64_t count, const int32_t* ms, int64_t n, const int64_
 
 // ---- accurate FP64 metrics ---------------------------------------------------
 
+// nalgebra's gemm in its gemv order (the small / static-size path of
+// gemm_uninit), batched over `batch` products at the given strides.
+void orc_dgemm_gemv_order_batched(int64_t m, int64_t n, int64_t k, double alpha, const double* a, int64_t lda,
+                                  int64_t sa, const double* b, int64_t ldb, int64_t sb, double beta, double* c,
+                                  int64_t ldc, int64_t sc, int64_t batch, int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+  for (int64_t s = 0; s < batch; ++s)
+    orc::gemm_gemv_order<double>(m, n, k, alpha, a + s * sa, lda, b + s * sb, ldb, beta, c + s * sc, ldc);
+}
+
 // C = alpha * A * B + beta * C with every dot product accumulated by Dot2
 // (compensated), the accurate reference for the GEMM kernels.  beta == 0 means
 // C is never read (blas.rs:729-746 contract).

@@ -95,6 +95,36 @@ inline void axpy(std::size_t n, T a, const T* x, T beta, T* y) {
   for (std::size_t i = 0; i < n; ++i) y[i] = a * x[i] * T(1) + beta * y[i];
 }
 
+// gemm_uninit's non-matrixmultiply path (src/base/blas_uninit.rs:187-333, the
+// loop at :320-332), used by nalgebra when some dimension is <= 5 or the sizes
+// are static: for each output column j, gemv_uninit (:127-176) -- with k == 0,
+// y = 0 (beta == 0) or y *= beta; otherwise the first column of A through
+// axcpy with beta (array_axc when beta == 0: y = alpha * a * x, else
+// array_axcpy: y = alpha * a * x + beta * y, :32-78), the others with beta = 1.
+// C = alpha * A * B + beta * C, column-major; C is not read when beta == 0.
+template <class T>
+inline void gemm_gemv_order(std::size_t m, std::size_t n, std::size_t k, T alpha, const T* a, std::size_t lda,
+                            const T* b, std::size_t ldb, T beta, T* c, std::size_t ldc) {
+  for (std::size_t j = 0; j < n; ++j) {
+    T* y = c + j * ldc;
+    const T* x = b + j * ldb;
+    if (k == 0) {
+      for (std::size_t i = 0; i < m; ++i) y[i] = (beta == T(0)) ? T(0) : y[i] * beta;
+      continue;
+    }
+    for (std::size_t l = 0; l < k; ++l) {
+      const T* col = a + l * lda;
+      const T val = x[l];
+      const T bb = (l == 0) ? beta : T(1);
+      if (bb == T(0)) {
+        for (std::size_t i = 0; i < m; ++i) y[i] = alpha * col[i] * val;
+      } else {
+        for (std::size_t i = 0; i < m; ++i) y[i] = alpha * col[i] * val + bb * y[i];
+      }
+    }
+  }
+}
+
 // Matrix::icamax for a real column (src/base/min_max.rs:221-240): the first
 // index of the largest |x|, strict `>` so ties keep the lower index; a NaN never
 // wins unless it sits at index 0.

@@ -676,3 +676,38 @@ def test_batch_backward_error_helpers_match_per_system_metric():
     bb = a @ xx
     ref = O.backward_error(a, xx, bb)
     assert O.dense_backward_error(a.ravel(order="F"), n, xx, bb) == pytest.approx(ref, rel=1e-12)
+
+
+def test_gemm_gemv_order_restatement_bit_for_bit():
+    """The oracle's gemm in nalgebra's gemv order (blas_uninit.rs:32-78,
+    127-176, 320-332) against a pure-Python transcription of the same loops,
+    with beta zero and non-zero and k = 0; and the reference's gemm example
+    (blas.rs:713-727) to relative accuracy."""
+    rng = np.random.default_rng(12)
+
+    def loops(alpha, a, b, beta, c):
+        m, k = a.shape
+        n = b.shape[1]
+        y = c.copy()
+        for j in range(n):
+            if k == 0:
+                for i in range(m):
+                    y[i, j] = 0.0 if beta == 0.0 else y[i, j] * beta
+                continue
+            for l in range(k):
+                bb = beta if l == 0 else 1.0
+                for i in range(m):
+                    t = alpha * a[i, l] * b[l, j]
+                    y[i, j] = t if bb == 0.0 else t + bb * y[i, j]
+        return y
+
+    for (m, n, k) in [(3, 4, 5), (1, 1, 1), (6, 2, 0), (5, 7, 3)]:
+        for alpha, beta in [(1.0, 0.0), (1.3, 0.7), (-0.5, 1.0)]:
+            a = rng.standard_normal((m, k))
+            b = rng.standard_normal((k, n))
+            c = rng.standard_normal((m, n))
+            assert np.array_equal(O.gemm_gemv_order(alpha, a, b, beta, c), loops(alpha, a, b, beta, c))
+    mat1 = np.eye(2, 4)
+    mat2 = np.array([[1.0, 2.0, 3.0], [4.0, 5.0, 6.0]])
+    mat3 = np.array([[0.1, 0.2, 0.3, 0.4], [0.5, 0.6, 0.7, 0.8], [0.9, 1.0, 1.1, 1.2]])
+    assert np.allclose(O.gemm_gemv_order(10.0, mat2, mat3, 5.0, mat1), mat2 @ mat3 * 10.0 + mat1 * 5.0, rtol=1e-12)
