@@ -1446,7 +1446,9 @@ def bench_mixed_lu_ours(args, rank, world):
                              "backward_error": be, "backward_error_over_n_eps": be / (n * 2.220446049250313e-16),
                              "clocks": clk.summary()}
                 if name == "mixed_ir":
-                    res[name].update({"refinement_steps": it.value, "fp64_fallback": bool(fb.value)})
+                    res[name].update({"refinement_steps": it.value, "fp64_fallback": fb.value == 1,
+                                      "path": {0: "classical refinement", 1: "FP64 refactorization",
+                                               2: "GMRES-IR (FP32 LU preconditioner)"}.get(fb.value)})
             res["speedup_mixed_over_fp64"] = res["fp64"]["ms"] / res["mixed_ir"]["ms"]
             res["mixed_ir"]["forward_error_vs_fp64_form"] = float((xs["mixed_ir"] - xs["fp64"]).abs().max() /
                                                                   xs["fp64"].abs().max())

@@ -432,8 +432,14 @@ size_t nacu_gesv_mixed_workspace_bytes(int n);
  * FP32 LU with partial pivoting (BF16-split tensor-core trailing updates),
  * then FP64 iterative refinement r = b - A x, x += (LU)^-1 r until the normwise
  * backward error ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol_units * n *
- * eps64 (tol_units <= 0: 1), at most max_iter steps (<= 0: 30); when FP32 cannot
- * factor A or the refinement stagnates, A is refactored in FP64 (fallback).
+ * eps64 (tol_units <= 0: 1), at most max_iter steps (<= 0: 30).  When the
+ * classical refinement stagnates (u32 * cond(A) near 1), GMRES-IR takes over
+ * (Carson & Higham 2018): each correction solves M^-1 A d = M^-1 r by
+ * restarted GMRES with FP64 vectors, M = the FP32 LU factors (applied in
+ * FP64) as the preconditioner.  When FP32 cannot factor A, when classical
+ * refinement diverges outright (u32 * cond(A) well above 1), or when GMRES-IR
+ * makes no progress, A is refactored in FP64.  *fallback_out: 0 classical refinement, 2 GMRES-IR,
+ * 1 FP64 refactorization; *iters_out: FP64 residuals formed.
  * Synchronous: *iters_out, *berr_out, *fallback_out are host values.  No
  * reference counterpart (nalgebra has no mixed precision); it replaces
  * `m.lu().solve(&b)` (src/linalg/lu.rs:93-122, 221-260) when an FP64-accurate

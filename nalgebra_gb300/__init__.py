@@ -462,9 +462,10 @@ class ColPivQR:
 def solve_refined(a: DeviceMatrix, b: DeviceMatrix, tol_units: float = 1.0, max_iter: int = 0):
     """The precision form for one large system (no nalgebra counterpart): FP32
     LU with BF16-split tensor-core trailing updates, FP64 iterative refinement
-    to backward error <= tol_units * n * eps64, FP64 fallback.  ``a`` and ``b``
-    are left unchanged.  Returns (x, info) with info = dict(iters, berr,
-    fallback)."""
+    to backward error <= tol_units * n * eps64 (GMRES-IR preconditioned by the
+    FP32 factors where classical refinement stalls), FP64 fallback.  ``a`` and
+    ``b`` are left unchanged.  Returns (x, info) with info = dict(iters, berr,
+    fallback, gmres)."""
     import ctypes as C
 
     torch = _torch()
@@ -476,7 +477,7 @@ def solve_refined(a: DeviceMatrix, b: DeviceMatrix, tol_units: float = 1.0, max_
     _lib.call("nacu_dgesv_mixed_ir", n, a.data.data_ptr(), n, b.data.data_ptr(), x.data.data_ptr(),
               float(tol_units), int(max_iter), C.byref(it), C.byref(berr), C.byref(fb), ws.data_ptr(), ws.numel(),
               _stream_ptr())
-    return x, {"iters": it.value, "berr": berr.value, "fallback": bool(fb.value)}
+    return x, {"iters": it.value, "berr": berr.value, "fallback": fb.value == 1, "gmres": fb.value == 2}
 
 
 def cholesky_solve_refined_host(ns, a_offsets, a, b_offsets, b, nrhs: int, chunks: int = 8, tol_units: float = 1.0,
