@@ -73,3 +73,28 @@ def test_product_never_imports_the_oracle():
                 text = open(os.path.join(root, f)).read()
                 assert not re.search(r"^\s*(import|from)\s+oracle\b", text, re.M), f
                 assert "liboracle" not in text, f
+
+
+def test_rust_crate_binds_every_entry_point_with_its_arity():
+    """nalgebra-cuda/src/ffi.rs (the crate is source here: no Rust toolchain on
+    these machines) declares every entry point of include/nalgebra_cuda.h with
+    the header's number of parameters."""
+    import os
+    import re
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    hdr = open(os.path.join(root, "include", "nalgebra_cuda.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    decl = {}
+    for m in re.finditer(r"\b(nacu_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", hdr):
+        args = m.group(2).strip()
+        decl[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    rs = open(os.path.join(root, "nalgebra-cuda", "src", "ffi.rs")).read()
+    rs = re.sub(r"//[^\n]*", "", rs)
+    bound = {}
+    for m in re.finditer(r"pub fn (nacu_[a-z0-9_]+)\s*\(([^)]*)\)", rs):
+        args = m.group(2).strip().rstrip(",")
+        bound[m.group(1)] = 0 if not args else args.count(",") + 1
+    assert set(decl) == set(bound), (set(decl) ^ set(bound))
+    wrong = {k: (decl[k], bound[k]) for k in decl if decl[k] != bound[k]}
+    assert not wrong, wrong
