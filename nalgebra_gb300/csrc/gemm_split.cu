@@ -18,17 +18,19 @@
 // reported against a compensated FP64 oracle); the work runs at tensor-core
 // speed instead of the ~1 TFLOP/s FP64 pipe.
 //
-// Kernel: one 128 x 256 output tile per CTA, 128 threads.  Warp 0 / lane 0
-// issues TMA loads (cp.async.bulk.tensor.2d, 64-byte swizzle) of every slice
-// tile of a 32-deep k-block -- s A tiles (128 x 32 BF16) and s B tiles
-// (256 x 32 BF16) -- into one stage of a 3-stage shared-memory ring, so each
-// slice tile crosses L2 once; warp 1 / lane 0 issues the k-block's slice
-// products as tcgen05.mma 128 x 256 x 16 from that stage into a 256-column
-// FP32 TMEM accumulator and releases the stage with tcgen05.commit; after the
-// last k-block all four warps read the
-// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = rows) and
-// write C.  Every mbarrier wait is bounded: on time-out the kernel records an
-// error flag and finishes without further waiting.
+// Kernel: persistent, one CTA per SM looping over 128 x 256 output tiles,
+// 192 threads.  Warp 0 / lane 0 issues TMA loads (cp.async.bulk.tensor.2d,
+// 64-byte swizzle) of every slice tile of a 32-deep k-block -- s A tiles
+// (128 x 32 BF16) and s B tiles (256 x 32 BF16) -- into one stage of a
+// 3-stage shared-memory ring, so each slice tile crosses L2 once; the ring
+// runs on across tiles.  Warp 1 / lane 0 issues the k-block's slice products
+// as tcgen05.mma 128 x 256 x 16 from that stage into one of two 256-column
+// FP32 TMEM accumulators (tiles alternate) and releases the stage with
+// tcgen05.commit.  Warps 2-5 are the epilogue: warp w reads TMEM lanes
+// 32 (w mod 4) .. + 31 (rows) of a finished accumulator with tcgen05.ld,
+// writes C, and hands the accumulator back -- while the MMAs of the next tile
+// already run in the other one.  Every mbarrier wait is bounded: on time-out
+// the kernel records an error flag and finishes without further waiting.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -43,11 +45,11 @@ constexpr int kTM = 128, kTN = 256, kTK = 64;  // output tile; K padding of the 
 // slice products of that k-block are issued from the one stage.
 constexpr int kKB = 32;
 constexpr int kStages = 3;
-constexpr int kSplitThreads = 128;
+constexpr int kSplitThreads = 192;  // producer, MMA issuer, four epilogue warps
 constexpr uint32_t kSliceA = kTM * kKB * 2;  // 8 KB
 constexpr uint32_t kSliceB = kTN * kKB * 2;  // 16 KB
 constexpr uint32_t kStageBytes = 3 * (kSliceA + kSliceB);  // 72 KB (three slices)
-constexpr uint32_t kTmemCols = 256;
+constexpr uint32_t kTmemCols = 512;  // two 256-column accumulators
 constexpr long long kWaitLimit = 1ll << 26;
 
 __device__ int g_split_error;
@@ -104,6 +106,9 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t 
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
       "l"(da), "l"(db), "r"(idesc), "r"(accum));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -240,11 +245,12 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte aligned stage ring (every slice tile starts on a 512-byte swizzle pattern)
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], acc_bar;
+  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], acc_full[2], acc_empty[2];
   __shared__ uint32_t tmem_base_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * kTN;
-  const int iters = (g.npairs > 0) ? g.kp / kKB : 0;  // k-blocks
+  const int kblocks = (g.npairs > 0) ? g.kp / kKB : 0;  // k-blocks per tile
+  const int tiles_m = g.mp / kTM;
+  const int ntiles = tiles_m * (g.np / kTN);
   const uint32_t stage_tx = (uint32_t)g.slices * (kSliceA + kSliceB);
 
   if (threadIdx.x == 0) {
@@ -252,10 +258,13 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&acc_bar, 1);
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(&acc_full[a], 1);
+      mbar_init(&acc_empty[a], 4);  // one arrival per epilogue warp
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {  // TMEM accumulator: 128 lanes x 256 FP32 columns
+  if (warp == 0) {  // TMEM: 128 lanes x 512 FP32 columns = two accumulators
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
                  "r"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -264,92 +273,120 @@ __global__ void __launch_bounds__(kSplitThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base_sh;
 
-  if (warp >= 2 && g.beta != 0.0) {
-    // warps 2-3 are idle until the epilogue: bring the C tile the epilogue
-    // reads (beta != 0) into L2 while the products run (one 128-byte line per
-    // prefetch, valid elements only)
-    constexpr int kLineElems = 128 / (int)sizeof(TO);
-    const int lines_per_col = kTM / kLineElems;
-    for (int q = threadIdx.x - 64; q < kTN * lines_per_col; q += 64) {
-      const int col = n0 + q / lines_per_col;
-      const int row = m0 + (q % lines_per_col) * kLineElems;
-      if (col < g.n && row < g.m) {
-        const TO* cp = static_cast<const TO*>(g.C) + (size_t)col * g.ldc + row;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(cp));
-      }
-    }
-  }
   if (warp == 0 && lane == 0) {
-    // producer: TMA loads of every slice tile of A and B for k-block `it`
-    for (int it = 0; it < iters; ++it) {
-      const int s = it % kStages;
-      const uint32_t ph = (uint32_t)(it / kStages) & 1u;
-      if (!mbar_wait(&empty_bar[s], ph ^ 1u)) break;
-      unsigned char* sa = smem + (size_t)s * kStageBytes;
-      unsigned char* sb = sa + 3 * kSliceA;
-      mbar_expect_tx(&full_bar[s], stage_tx);
-      for (int p = 0; p < g.slices; ++p) tma_load_2d(sa + p * kSliceA, &mapA, it * kKB, p * g.mp + m0, &full_bar[s]);
-      for (int q = 0; q < g.slices; ++q) tma_load_2d(sb + q * kSliceB, &mapB, it * kKB, q * g.np + n0, &full_bar[s]);
+    // producer: TMA loads of every slice tile of A and B, k-block after
+    // k-block, tile after tile (the ring's position runs on across tiles)
+    int gk = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const int m0 = (t % tiles_m) * kTM, n0 = (t / tiles_m) * kTN;
+      for (int it = 0; it < kblocks; ++it, ++gk) {
+        const int s = gk % kStages;
+        const uint32_t ph = (uint32_t)(gk / kStages) & 1u;
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u)) {
+          ok = false;
+          break;
+        }
+        unsigned char* sa = smem + (size_t)s * kStageBytes;
+        unsigned char* sb = sa + 3 * kSliceA;
+        mbar_expect_tx(&full_bar[s], stage_tx);
+        for (int p = 0; p < g.slices; ++p) tma_load_2d(sa + p * kSliceA, &mapA, it * kKB, p * g.mp + m0, &full_bar[s]);
+        for (int q = 0; q < g.slices; ++q) tma_load_2d(sb + q * kSliceB, &mapB, it * kKB, q * g.np + n0, &full_bar[s]);
+      }
     }
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer
+    // MMA issuer: tile j into accumulator j & 1, once the epilogue has emptied it
     constexpr uint32_t idesc = idesc_bf16_f32(kTM, kTN);
+    int gk = 0;
     bool ok = true;
-    for (int it = 0; it < iters && ok; ++it) {
-      const int s = it % kStages;
-      const uint32_t ph = (uint32_t)(it / kStages) & 1u;
-      ok = mbar_wait(&full_bar[s], ph);
-      if (!ok) break;
+    for (int t = blockIdx.x, j = 0; t < ntiles && ok; t += gridDim.x, ++j) {
+      const int slot = j & 1;
+      const uint32_t use = (uint32_t)(j >> 1) & 1u;
+      if (!mbar_wait(&acc_empty[slot], use ^ 1u)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t sa = smem_u32(smem + (size_t)s * kStageBytes);
-      const uint32_t sb = sa + 3 * kSliceA;
-      for (int pr = 0; pr < g.npairs; ++pr) {
-        const uint32_t ta = sa + (uint32_t)g.pa[pr] * kSliceA, tb = sb + (uint32_t)g.pb[pr] * kSliceB;
+      const uint32_t acc = tmem + (uint32_t)slot * kTN;
+      for (int it = 0; it < kblocks; ++it, ++gk) {
+        const int s = gk % kStages;
+        const uint32_t ph = (uint32_t)(gk / kStages) & 1u;
+        if (!mbar_wait(&full_bar[s], ph)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t sa = smem_u32(smem + (size_t)s * kStageBytes);
+        const uint32_t sb = sa + 3 * kSliceA;
+        for (int pr = 0; pr < g.npairs; ++pr) {
+          const uint32_t ta = sa + (uint32_t)g.pa[pr] * kSliceA, tb = sb + (uint32_t)g.pb[pr] * kSliceB;
 #pragma unroll
-        for (int kk = 0; kk < kKB / 16; ++kk)  // K = 16 per instruction: +32 bytes in the swizzled row
-          mma_bf16(tmem, smem_desc_sw64(ta + kk * 32), smem_desc_sw64(tb + kk * 32), idesc,
-                   (it > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+          for (int kk = 0; kk < kKB / 16; ++kk)  // K = 16 per instruction: +32 bytes in the swizzled row
+            mma_bf16(acc, smem_desc_sw64(ta + kk * 32), smem_desc_sw64(tb + kk * 32), idesc,
+                     (it > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+        }
+        mma_commit(&empty_bar[s]);  // stage free once these MMAs have read it
       }
-      mma_commit(&empty_bar[s]);  // stage free once these MMAs have read it
+      if (ok) mma_commit(&acc_full[slot]);  // accumulator complete
     }
-    mma_commit(&acc_bar);  // accumulator complete
-  }
-  __syncwarp();
-  // epilogue: all four warps; warp w reads TMEM lanes 32w..32w+31 (rows)
-  const bool acc_ok = mbar_wait(&acc_bar, 0);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const int row = m0 + warp * 32 + lane;
-  const double srow = (row < g.m) ? pow2(scale_exp(g.rexp[row])) : 0.0;
-  const int erow = (row < g.m) ? scale_exp(g.rexp[row]) : 0;
-  const float falpha = (float)g.alpha, fbeta = (float)g.beta;
-  const bool plain = (g.alpha == 1.0 && g.beta == 0.0);  // C = A B: no FP64 arithmetic in the epilogue
-  for (int c0 = 0; c0 < kTN; c0 += 16) {
-    uint32_t v[16];
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    if (!acc_ok || row >= g.m) continue;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const int col = n0 + c0 + j;
-      if (col < g.n) {
-        TO* cp = static_cast<TO*>(g.C) + (size_t)col * g.ldc + row;
-        if constexpr (sizeof(TO) == 8) {
-          if (plain) {
-            *cp = f32_scaled_to_f64(__uint_as_float(v[j]), erow + scale_exp(g.cexp[col]));
-          } else {
-            const double val = (double)__uint_as_float(v[j]) * srow * pow2(scale_exp(g.cexp[col]));
-            *cp = (g.beta == 0.0) ? g.alpha * val : fma(g.alpha, val, g.beta * *cp);
+  } else if (warp >= 2) {
+    // epilogue: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the tile's rows)
+    const int q = warp & 3;
+    const float falpha = (float)g.alpha, fbeta = (float)g.beta;
+    const bool plain = (g.alpha == 1.0 && g.beta == 0.0);  // C = A B: no FP64 arithmetic in the epilogue
+    for (int t = blockIdx.x, j = 0; t < ntiles; t += gridDim.x, ++j) {
+      const int slot = j & 1;
+      const uint32_t use = (uint32_t)(j >> 1) & 1u;
+      const int m0 = (t % tiles_m) * kTM, n0 = (t / tiles_m) * kTN;
+      if (g.beta != 0.0) {
+        // bring the C tile this epilogue reads into L2 while the tile's
+        // products run (one 128-byte line per prefetch, valid elements only)
+        constexpr int kLineElems = 128 / (int)sizeof(TO);
+        constexpr int lines_per_col = kTM / kLineElems;
+        for (int e = threadIdx.x - 64; e < kTN * lines_per_col; e += 128) {
+          const int col = n0 + e / lines_per_col;
+          const int r = m0 + (e % lines_per_col) * kLineElems;
+          if (col < g.n && r < g.m) {
+            const TO* cp = static_cast<const TO*>(g.C) + (size_t)col * g.ldc + r;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(cp));
           }
-        } else {  // FP32 output: integer exponent arithmetic and FP32 only
-          const float val = ldexpf(__uint_as_float(v[j]), erow + scale_exp(g.cexp[col]));
-          *cp = (fbeta == 0.f) ? falpha * val : fmaf(falpha, val, fbeta * *cp);
         }
       }
+      if (!mbar_wait(&acc_full[slot], use)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int row = m0 + q * 32 + lane;
+      const double srow = (row < g.m) ? pow2(scale_exp(g.rexp[row])) : 0.0;
+      const int erow = (row < g.m) ? scale_exp(g.rexp[row]) : 0;
+      for (int c0 = 0; c0 < kTN; c0 += 16) {
+        uint32_t v[16];
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)slot * kTN + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row >= g.m) continue;
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {
+          const int col = n0 + c0 + jj;
+          if (col < g.n) {
+            TO* cp = static_cast<TO*>(g.C) + (size_t)col * g.ldc + row;
+            if constexpr (sizeof(TO) == 8) {
+              if (plain) {
+                *cp = f32_scaled_to_f64(__uint_as_float(v[jj]), erow + scale_exp(g.cexp[col]));
+              } else {
+                const double val = (double)__uint_as_float(v[jj]) * srow * pow2(scale_exp(g.cexp[col]));
+                *cp = (g.beta == 0.0) ? g.alpha * val : fma(g.alpha, val, g.beta * *cp);
+              }
+            } else {  // FP32 output: integer exponent arithmetic and FP32 only
+              const float val = ldexpf(__uint_as_float(v[jj]), erow + scale_exp(g.cexp[col]));
+              *cp = (fbeta == 0.f) ? falpha * val : fmaf(falpha, val, fbeta * *cp);
+            }
+          }
+        }
+      }
+      // the accumulator's columns are read: hand it back to the MMA issuer
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[slot]);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -493,7 +530,12 @@ int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, 
   const size_t smem = (size_t)kStages * kStageBytes + 1024;
   e = ensure_dynamic_smem(split_gemm_kernel<TO>, smem);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgemm_split_bf16");
-  dim3 grid(L.mp / kTM, L.np / kTN);
+  const int ntiles = (L.mp / kTM) * (L.np / kTN);
+  // FP64 output (the public GEMM): persistent, one CTA per SM looping over the
+  // tiles.  FP32 output (the large LU's trailing updates): one CTA per tile, so
+  // that the look-ahead's concurrent update on the other stream still finds
+  // SMs (persistent CTAs would hold every SM until the bulk update ends).
+  const int grid = (sizeof(TO) == 8 && ntiles > sm_count()) ? sm_count() : ntiles;
   if (g.npairs == 0) {  // k == 0: C = beta * C
     if constexpr (sizeof(TO) == 8)
       return nacu_dgemm(m, n, 0, alpha, nullptr, m > 1 ? m : 1, nullptr, 1, beta, C, ldc, stream);
