@@ -162,22 +162,6 @@ __global__ void row_exp_kernel(int m, int k, const TI* __restrict__ A, int64_t l
   }
   if (e != INT_MIN) atomicMax(&rexp[i], e);
 }
-// Per-column max exponent of B (column-major k x n): one warp per column.
-template <typename TI>
-__global__ void col_exp_kernel(int k, int n, const TI* __restrict__ B, int64_t ldb, int* __restrict__ cexp) {
-  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (j >= n) return;
-  int e = INT_MIN;
-  for (int r = lane; r < k; r += 32) {
-    const double v = (double)B[(size_t)j * ldb + r];
-    if (v != 0.0) e = max(e, exp_of(v));
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, off));
-  if (lane == 0) cexp[j] = (e == INT_MIN) ? 0 : e;
-}
-
 // Split one scaled value into `slices` BF16 parts (FP32 arithmetic: the
 // scaled value is first rounded to FP32, whose 24 bits three slices cover).
 __device__ __forceinline__ void split3(double v, int slices, __nv_bfloat16* out) {
@@ -190,7 +174,8 @@ __device__ __forceinline__ void split3(double v, int slices, __nv_bfloat16* out)
 }
 
 // A (m x k column-major) -> slices [s][mp][kp] (row-major: K contiguous),
-// zero padded; 32 x 32 tiles transposed through shared memory.
+// 32 x 32 tiles transposed through shared memory; the grid covers the padded
+// mp x kp extent and writes its zeros too, so the buffer needs no memset.
 template <typename TI>
 __global__ void split_a_kernel(int m, int k, const TI* __restrict__ A, int64_t lda, const int* __restrict__ rexp,
                                int mp, int kp, int slices, __nv_bfloat16* __restrict__ out) {
@@ -211,14 +196,35 @@ __global__ void split_a_kernel(int m, int k, const TI* __restrict__ A, int64_t l
     for (int s = 0; s < 3; ++s) out[((size_t)s * mp + i) * kp + c] = h[s];
   }
 }
-// B (k x n column-major: column j contiguous over K) -> slices [s][np][kp].
+// B (k x n column-major: column j contiguous over K) -> slices [s][np][kp],
+// one CTA per (padded) column: the column's max exponent (cexp[j], 0 for an
+// all-zero or padding column) first, then the split, reading the column a
+// second time from L2.
 template <typename TI>
-__global__ void split_b_kernel(int k, int n, const TI* __restrict__ B, int64_t ldb, const int* __restrict__ cexp,
-                               int np, int kp, int slices, __nv_bfloat16* __restrict__ out) {
-  const int j = blockIdx.y;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < kp; c += gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(256) split_b_kernel(int k, int n, const TI* __restrict__ B, int64_t ldb,
+                                                      int* __restrict__ cexp, int np, int kp, int slices,
+                                                      __nv_bfloat16* __restrict__ out) {
+  __shared__ int s_e[8];
+  const int j = blockIdx.x;
+  const TI* col = B + (size_t)j * ldb;
+  int e = INT_MIN;
+  if (j < n)
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+      const double v = (double)col[c];
+      if (v != 0.0) e = max(e, exp_of(v));
+    }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, off));
+  if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = e;
+  __syncthreads();
+  int ce = INT_MIN;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) ce = max(ce, s_e[w]);
+  ce = (ce == INT_MIN) ? 0 : ce;
+  if (threadIdx.x == 0 && j < np) cexp[j] = ce;
+  const double sc = pow2(-scale_exp(ce));
+  for (int c = threadIdx.x; c < kp; c += blockDim.x) {
     double v = 0.0;
-    if (j < n && c < k) v = (double)B[(size_t)j * ldb + c] * pow2(-scale_exp(cexp[j]));
+    if (j < n && c < k) v = (double)col[c] * sc;
     __nv_bfloat16 h[3];
     split3(v, slices, h);
     for (int s = 0; s < 3; ++s) out[((size_t)s * np + j) * kp + c] = h[s];
@@ -483,17 +489,16 @@ int split_gemm_run(int m, int n, int k, double alpha, const TI* A, int64_t lda, 
   __nv_bfloat16* bs = reinterpret_cast<__nv_bfloat16*>(ws + L.b_off);
   int* rexp = reinterpret_cast<int*>(ws + L.rexp_off);
   int* cexp = reinterpret_cast<int*>(ws + L.cexp_off);
-  // zero the padded slice buffers, INT_MIN the row exponents (0x80 bytes give
-  // 0x80808080 < any real exponent)
-  cudaError_t e = cudaMemsetAsync(ws, 0, L.rexp_off, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(rexp, 0x80, (size_t)L.mp * 4, s);
+  // INT_MIN the row exponents (0x80 bytes give 0x80808080 < any real
+  // exponent); the split kernels write every element of the padded slice
+  // buffers, zeros included
+  cudaError_t e = cudaMemsetAsync(rexp, 0x80, (size_t)L.mp * 4, s);
   if (e != cudaSuccess) return record_cuda_error(e, "nacu_dgemm_split_bf16");
   if (k > 0) {
     row_exp_kernel<TI><<<dim3((m + 255) / 256, (k + kRowExpChunk - 1) / kRowExpChunk), 256, 0, s>>>(m, k, A, lda,
                                                                                                  rexp);
-    col_exp_kernel<TI><<<(n + 7) / 8, 256, 0, s>>>(k, n, B, ldb, cexp);
-    split_a_kernel<TI><<<dim3((k + 31) / 32, (m + 31) / 32), 256, 0, s>>>(m, k, A, lda, rexp, L.mp, L.kp, slices, as);
-    split_b_kernel<TI><<<dim3((L.kp + 255) / 256, n), 256, 0, s>>>(k, n, B, ldb, cexp, L.np, L.kp, slices, bs);
+    split_a_kernel<TI><<<dim3(L.kp / 32, L.mp / 32), 256, 0, s>>>(m, k, A, lda, rexp, L.mp, L.kp, slices, as);
+    split_b_kernel<TI><<<L.np, 256, 0, s>>>(k, n, B, ldb, cexp, L.np, L.kp, slices, bs);
     int rc = check_launch("nacu_dgemm_split_bf16: split");
     if (rc != NACU_SUCCESS) return rc;
   } else {
