@@ -85,7 +85,7 @@ __device__ void group_rank_one(int m, double* L, int64_t ld, double* x, double* 
           a1 = dvd<EXACT>(-xj, diag);
           a2 = mul<EXACT>(dvd<EXACT>(mul<EXACT>(new_diag, sigma), gamma), xj);
           b2 = dvd<EXACT>(new_diag, diag);
-          upd = (gamma != 0.0);
+          upd = !is_zero_bits(gamma);
         } else {
           const double r = rd[j], r2 = r * r;
           const double sx = sigma * xj * xj;
@@ -96,7 +96,7 @@ __device__ void group_rank_one(int m, double* L, int64_t ld, double* x, double* 
           a1 = -xj * r;
           a2 = new_diag * sigma * xj * r2 * ib1;
           b2 = new_diag * r;
-          upd = (beta1 != 0.0);
+          upd = !is_zero_bits(beta1);
           beta = beta1;
           ib = ib1;
         }
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kFacPerCta * G) insert_kernel(int n, const dou
     double coeff = 0.0;
     if (ok) {
       const double d = lc[i];  // every lane of the group reads it: the group agrees
-      if (d == 0.0) {
+      if (is_zero_bits(d)) {
         ok = false;  // nalgebra's assertion
       } else if (gl == 0) {
         coeff = dvd<EXACT>(row[i], d);

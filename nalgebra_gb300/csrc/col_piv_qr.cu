@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
           __syncwarp();
           if (lane == 0) x[0] = cq_add<EXACT>(x[0], signed_norm);
           __syncwarp();
-          const bool nz = (factor != 0.0);
+          const bool nz = !is_zero_bits(factor);
           double rnorm = signed_norm;
           if (nz) {
             const double sf = __dsqrt_rn(factor);

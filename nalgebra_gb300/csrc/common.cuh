@@ -89,6 +89,17 @@ __device__ __forceinline__ unsigned long long abs_bits_f64(double x) {
   return ((unsigned long long)(hi & 0x7fffffffu) << 32) | lo;
 }
 
+// x == 0 (either sign) from the bit image, on the integer pipe: an FP64
+// compare issues on the FP64 pipe, which on this part takes a warp-wide
+// instruction every 64 cycles per sub-partition, so a test every thread makes
+// once per elimination step costs as much as a sixth of the step's FMAs.
+__device__ __forceinline__ bool is_zero_bits(double x) { return (abs_bits_f64(x) == 0ull); }
+__device__ __forceinline__ bool is_zero_bits(float x) {
+  unsigned u;
+  asm("mov.b32 %0, %1;" : "=r"(u) : "f"(x));
+  return (u & 0x7fffffffu) == 0u;
+}
+
 // The bit image is taken through an opaque mov: a plain mask of the
 // reinterpreted bits is recognised as fabs and then costs an FP64 add (an
 // FP64 pipe slot) per key, where the key is taken for every updated element.

@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(kFpThreads, 5) fullpiv_kernel(int n, int nrhs,
         const int msz = n - i;
         int idx;
         const double diag = fp_pick(s_key, s_idx, s_val, lane, idx);
-        if (diag == 0.0) {  // full_piv_lu.rs:73-76: the rest of the matrix is zero
+        if (is_zero_bits(diag)) {  // full_piv_lu.rs:73-76: the rest of the matrix is zero
           steps = i;
           break;
         }

@@ -49,8 +49,9 @@ __device__ __forceinline__ void lu_find_pivot(int n, int c, const T* colc, int* 
   __syncwarp();
   if (lane == 0) {
     const T d = colc[idx];
-    s_piv[c] = (d == T(0)) ? c : idx;
-    s_rcp[0] = (d == T(0)) ? T(0) : T(1) / d;  // one division per step, not per thread
+    const bool zero = is_zero_bits(d);
+    s_piv[c] = zero ? c : idx;
+    s_rcp[0] = zero ? T(0) : T(1) / d;  // one division per step, not per thread
     s_rcp[n + 1] = d;
     s_rcp[n + 2] = colc[c];
   }
@@ -77,7 +78,7 @@ __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_inf
       const T diag = s_rcp[n + 1];
       const T inv_diag = s_rcp[0];
       const T old_ii = s_rcp[n + 2];
-      const bool skip = (diag == T(0));  // lu.rs:107-110: all-zero column, no elimination
+      const bool skip = is_zero_bits(diag);  // lu.rs:107-110: all-zero column, no elimination
       if (!skip) {
         if (piv != i) {
           for (int c = tid; c < ncols; c += nthr) {
@@ -168,7 +169,7 @@ __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_inf
   if (tid == 0) {
     int inf = 0;
     for (int i = 0; i < n; ++i)
-      if (sa[(size_t)i * ld + i] == T(0)) {
+      if (is_zero_bits(sa[(size_t)i * ld + i])) {
         inf = i + 1;
         break;
       }

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(kTrsvBWarps * 32) trsv_batched_kernel(TrsvBArg
       const int i = g.upper ? n - 1 - k : k;
       const double* col = t + (size_t)i * n;
       const double d = col[i];
-      if (d == 0.0) {
+      if (is_zero_bits(d)) {
         fail = i + 1;
         break;
       }
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kTrsvBWarps * 32) trsv_batched_kernel(TrsvBArg
       const double dt = g.upper ? warp_dot<EXACT>(i, col, xs, lane)
                                 : warp_dot<EXACT>(n - i - 1, col + i + 1, xs + i + 1, lane);
       const double d = col[i];
-      if (d == 0.0) {
+      if (is_zero_bits(d)) {
         fail = i + 1;
         break;
       }
