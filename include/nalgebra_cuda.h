@@ -141,6 +141,25 @@ int nacu_dcolpivqr_solve_batched(int n, int nrhs, const double* QR, int64_t stri
                                  const int32_t* jpiv, double* B, int64_t strideB, int32_t* info, int batch, int flags,
                                  nacu_stream_t stream);
 
+/* ---- square QR (batched, n <= 128) ----------------------------------------- */
+
+/* QR::new (src/linalg/qr.rs:55-76) on A + s*strideA (n x n, in place: the
+ * Householder axes at and below the diagonal, R above it) and diag[s*n+i]
+ * (the signed diagonal; R's is |diag|); with nrhs > 0 (<= 16) QR::solve_mut
+ * (:204-256: q_tr_mul, then the upper solve dividing by |diag_i|) on B +
+ * s*strideB (n x nrhs; written even when the solve fails, as nalgebra's b
+ * is).  info[s] = 0 when every diag entry is non-zero (is_invertible,
+ * :281-292; B solved), else 1 + the first zero one.  NACU_FLAG_EXACT: factors
+ * and solutions bit-identical to nalgebra. */
+int nacu_dqr_batched(int n, int nrhs, double* A, int64_t strideA, double* diag, double* B, int64_t strideB,
+                     int32_t* info, int batch, int flags, nacu_stream_t stream);
+
+/* QR::solve_mut from factors written by nacu_dqr_batched (read only);
+ * `qr.try_inverse()` (:262-279) with B = the identity, 16 columns per call.
+ * info as above. */
+int nacu_dqr_solve_batched(int n, int nrhs, const double* QR, int64_t strideA, const double* diag, double* B,
+                           int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
+
 /* Inverse from getrf factors: `lu.try_inverse()` (src/linalg/lu.rs:266-297:
  * out = I, then solve_mut(out)), and with nacu_dgetrf_batched before it
  * `m.try_inverse()` for n > 4 (src/linalg/inverse.rs:135-137).  Ainv + s*strideInv
@@ -164,6 +183,25 @@ int nacu_dgetri_batched(int n, const double* LU, int64_t strideA, const int32_t*
 int nacu_dtrsv_batched(int n, int nrhs, int upper, int trans, int has_diag, double diag, const double* T,
                        int64_t strideT, double* B, int64_t strideB, int32_t* info, int batch, int flags,
                        nacu_stream_t stream);
+
+/* Bytes of device scratch nacu_dtrsv needs for an n x n triangle (the
+ * per-block completion flags). */
+size_t nacu_trsv_workspace_bytes(int n);
+
+/* Triangular solve of one matrix of any order (the batched kernel above stops
+ * at n = 128): B (n x nrhs, leading dimension ldb) <- T^-1 B (trans = 0) or
+ * T^-T B (trans = 1), T (lda) lower (upper = 0) or upper (upper = 1), only
+ * that triangle read; has_diag = 1 (lower, trans = 0 only):
+ * solve_lower_triangular_with_diag_mut, `diag` assumed for the diagonal (0:
+ * info = 1 and B untouched, solve.rs:115-117).  The same nalgebra functions
+ * as nacu_dtrsv_batched (src/linalg/solve.rs:55-442).  *info (device) = the
+ * 1-based index of the zero diagonal that stops nalgebra's solve in its
+ * order (forward: the first, backward: the last; B then holds garbage), 0,
+ * or -1000 when an internal wait between thread blocks ran out (does not
+ * happen in normal operation).  FMA arithmetic: NACU_FLAG_EXACT returns -14. */
+int nacu_dtrsv(int n, int nrhs, int upper, int trans, int has_diag, double diag, const double* T, int64_t lda,
+               double* B, int64_t ldb, int32_t* info, void* workspace, size_t workspace_bytes, int flags,
+               nacu_stream_t stream);
 
 /* Fused factor + solve in one launch: `m.lu()` then `.solve(&b)`
  * (src/linalg/decomposition.rs:48-54, src/linalg/lu.rs:221-236). */

@@ -26,6 +26,11 @@ extern "C" {
     pub fn nacu_dtrsv_batched(n: c_int, nrhs: c_int, upper: c_int, trans: c_int, has_diag: c_int,
                               diag: f64, t: *const f64, stride_t: i64, b: *mut f64, stride_b: i64,
                               info: *mut i32, batch: c_int, flags: c_int, s: Stream) -> c_int;
+    // the same solves for one matrix of any order
+    pub fn nacu_trsv_workspace_bytes(n: c_int) -> usize;
+    pub fn nacu_dtrsv(n: c_int, nrhs: c_int, upper: c_int, trans: c_int, has_diag: c_int, diag: f64,
+                      t: *const f64, lda: i64, b: *mut f64, ldb: i64, info: *mut i32, ws: *mut c_void,
+                      ws_bytes: usize, flags: c_int, s: Stream) -> c_int;
     // LU::try_inverse (lu.rs:266-297) from getrf factors
     pub fn nacu_dgetri_batched(n: c_int, lu: *const f64, stride_a: i64, ipiv: *const i32,
                                a_inv: *mut f64, stride_inv: i64, info: *mut i32, batch: c_int,
@@ -55,6 +60,12 @@ extern "C" {
     pub fn nacu_dcolpivqr_solve_batched(n: c_int, nrhs: c_int, qr: *const f64, stride_a: i64,
                                         diag: *const f64, jpiv: *const i32, b: *mut f64, stride_b: i64,
                                         info: *mut i32, batch: c_int, flags: c_int, s: Stream) -> c_int;
+    // QR::new and solve_mut for square matrices (qr.rs:55-76, 204-256)
+    pub fn nacu_dqr_batched(n: c_int, nrhs: c_int, a: *mut f64, stride_a: i64, diag: *mut f64, b: *mut f64,
+                            stride_b: i64, info: *mut i32, batch: c_int, flags: c_int, s: Stream) -> c_int;
+    pub fn nacu_dqr_solve_batched(n: c_int, nrhs: c_int, qr: *const f64, stride_a: i64, diag: *const f64,
+                                  b: *mut f64, stride_b: i64, info: *mut i32, batch: c_int, flags: c_int,
+                                  s: Stream) -> c_int;
     pub fn nacu_getrf_workspace_bytes(n: c_int) -> usize;
     pub fn nacu_dgetrf(n: c_int, a: *mut f64, lda: i64, ipiv: *mut i32, info: *mut i32,
                        ws: *mut c_void, ws_bytes: usize, s: Stream) -> c_int;

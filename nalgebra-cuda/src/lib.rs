@@ -135,6 +135,60 @@ impl DeviceMatrix {
         DeviceMatrix { data: self.data.clone_device(), nrows: self.nrows, ncols: self.ncols }
     }
 
+    fn trsv(&self, b: &mut DeviceMatrix, upper: bool, trans: bool, diag: Option<f64>) -> bool {
+        let n = self.nrows;
+        assert!(self.is_square() && b.nrows == n, "triangular solve dimension mismatch");
+        let mut info = DeviceBuffer::<i32>::zeroed(1);
+        let (hd, d) = (diag.is_some() as c_int, diag.unwrap_or(0.0));
+        if n <= 128 {
+            check(unsafe {
+                ffi::nacu_dtrsv_batched(n as c_int, b.ncols as c_int, upper as c_int, trans as c_int, hd, d,
+                                        self.data.as_ptr(), (n * n) as i64, b.data.as_mut_ptr(),
+                                        (n * b.ncols) as i64, info.as_mut_ptr(), 1, 0, std::ptr::null_mut())
+            });
+        } else {
+            let bytes = unsafe { ffi::nacu_trsv_workspace_bytes(n as c_int) };
+            let mut ws = DeviceBuffer::<u8>::zeroed(bytes);
+            check(unsafe {
+                ffi::nacu_dtrsv(n as c_int, b.ncols as c_int, upper as c_int, trans as c_int, hd, d,
+                                self.data.as_ptr(), n as i64, b.data.as_mut_ptr(), n as i64, info.as_mut_ptr(),
+                                ws.as_mut_ptr() as *mut c_void, bytes, 0, std::ptr::null_mut())
+            });
+        }
+        info.to_vec()[0] == 0
+    }
+
+    /// `Matrix::solve_lower_triangular_mut` (src/linalg/solve.rs:55-101).
+    pub fn solve_lower_triangular_mut(&self, b: &mut DeviceMatrix) -> bool {
+        self.trsv(b, false, false, None)
+    }
+    /// `Matrix::solve_upper_triangular_mut` (solve.rs:137-181).
+    pub fn solve_upper_triangular_mut(&self, b: &mut DeviceMatrix) -> bool {
+        self.trsv(b, true, false, None)
+    }
+    /// `Matrix::tr_solve_lower_triangular_mut` (solve.rs:233-256); `ad_` is the same for f64.
+    pub fn tr_solve_lower_triangular_mut(&self, b: &mut DeviceMatrix) -> bool {
+        self.trsv(b, false, true, None)
+    }
+    /// `Matrix::tr_solve_upper_triangular_mut` (solve.rs:258-283).
+    pub fn tr_solve_upper_triangular_mut(&self, b: &mut DeviceMatrix) -> bool {
+        self.trsv(b, true, true, None)
+    }
+    /// `Matrix::solve_lower_triangular_with_diag_mut` (solve.rs:106-134).
+    pub fn solve_lower_triangular_with_diag_mut(&self, b: &mut DeviceMatrix, diag: f64) -> bool {
+        self.trsv(b, false, false, Some(diag))
+    }
+    /// `Matrix::solve_lower_triangular` (solve.rs:15-34): a new matrix, or None.
+    pub fn solve_lower_triangular(&self, b: &DeviceMatrix) -> Option<DeviceMatrix> {
+        let mut res = b.clone_owned();
+        if self.solve_lower_triangular_mut(&mut res) { Some(res) } else { None }
+    }
+    /// `Matrix::solve_upper_triangular` (solve.rs:36-53).
+    pub fn solve_upper_triangular(&self, b: &DeviceMatrix) -> Option<DeviceMatrix> {
+        let mut res = b.clone_owned();
+        if self.solve_upper_triangular_mut(&mut res) { Some(res) } else { None }
+    }
+
     /// `Matrix::lu` (src/linalg/decomposition.rs:48-54): LU with partial
     /// pivoting, factors in place (the batched kernel up to n = 128, the
     /// blocked multi-SM factorization above).
@@ -178,11 +232,24 @@ impl DeviceMatrix {
         Some(DeviceCholesky { l: self, logdet: logdet.to_vec()[0] })
     }
 
-    /// `Matrix::qr` (src/linalg/decomposition.rs:57-63) for least squares:
-    /// m x n with m >= n, n <= 64 (the batched Householder kernel).
-    pub fn qr(self) -> DeviceQR {
-        assert!(self.nrows >= self.ncols && self.ncols <= 64, "nalgebra-cuda: QR of m x n, m >= n, n <= 64");
-        DeviceQR { a: self }
+    /// `Matrix::qr` (src/linalg/decomposition.rs:56-62).  Square n <= 128:
+    /// `QR::new` in place (the batched kernel), for `solve` / `try_inverse`.
+    /// Tall m x n with m > n, n <= 64: kept for `solve_least_squares`.
+    pub fn qr(mut self) -> DeviceQR {
+        let n = self.ncols;
+        if self.nrows == n {
+            assert!(n <= 128, "nalgebra-cuda: square QR of n <= 128");
+            let mut diag = DeviceBuffer::<f64>::zeroed(n.max(1));
+            let mut info = DeviceBuffer::<i32>::zeroed(1);
+            check(unsafe {
+                ffi::nacu_dqr_batched(n as c_int, 0, self.data.as_mut_ptr(), (n * n) as i64, diag.as_mut_ptr(),
+                                      std::ptr::null_mut(), 0, info.as_mut_ptr(), 1, 0, std::ptr::null_mut())
+            });
+            let invertible = info.to_vec()[0] == 0;
+            return DeviceQR { a: self, diag: Some(diag), invertible };
+        }
+        assert!(self.nrows > n && n <= 64, "nalgebra-cuda: QR of m x n, m >= n, n <= 64");
+        DeviceQR { a: self, diag: None, invertible: false }
     }
 
     /// `Matrix::gemm` (src/base/blas.rs:729-746): self = alpha a b + beta self.
@@ -348,16 +415,64 @@ impl DeviceCholesky {
     }
 }
 
-/// Householder QR of an m x n matrix (m >= n, n <= 64) for least squares:
-/// `QrDecomposition::solve` of nalgebra-lapack (src/qr/abstraction.rs:46-77).
+/// Householder QR.  Square (n <= 128): nalgebra's `QR` (src/linalg/qr.rs),
+/// factored in place.  Tall (m > n, n <= 64): the least-squares solve of
+/// nalgebra-lapack's `QrDecomposition::solve` (src/qr/abstraction.rs:46-77).
 pub struct DeviceQR {
     a: DeviceMatrix,
+    diag: Option<DeviceBuffer<f64>>,
+    invertible: bool,
 }
 
 impl DeviceQR {
-    /// argmin ||A x - b||: `Err` naming the first zero R_kk when A is rank
-    /// deficient.
-    pub fn solve(mut self, b: &DeviceMatrix) -> Result<DeviceMatrix, usize> {
+    fn solve_cols(&self, b: &mut DeviceMatrix) -> bool {
+        let n = self.a.nrows;
+        let diag = self.diag.as_ref().expect("QR solve: unable to solve a non-square system.");
+        let mut info = DeviceBuffer::<i32>::zeroed(1);
+        let mut ok = true;
+        let mut c0 = 0;
+        while c0 < b.ncols {
+            let k = (b.ncols - c0).min(16);
+            check(unsafe {
+                ffi::nacu_dqr_solve_batched(n as c_int, k as c_int, self.a.data.as_ptr(), (n * n) as i64,
+                                            diag.as_ptr(), b.data.as_mut_ptr().add(c0 * n), (n * k) as i64,
+                                            info.as_mut_ptr(), 1, 0, std::ptr::null_mut())
+            });
+            ok &= info.to_vec()[0] == 0;
+            c0 += k;
+        }
+        ok
+    }
+
+    /// `QR::solve_mut` (qr.rs:204-222): b is overwritten even when it
+    /// returns false.
+    pub fn solve_mut(&self, b: &mut DeviceMatrix) -> bool {
+        assert!(b.nrows == self.a.nrows, "QR solve matrix dimension mismatch.");
+        self.solve_cols(b)
+    }
+
+    /// `QR::solve` (qr.rs:182-198).
+    pub fn solve(&self, b: &DeviceMatrix) -> Option<DeviceMatrix> {
+        let mut res = b.clone_owned();
+        if self.solve_mut(&mut res) { Some(res) } else { None }
+    }
+
+    /// `QR::try_inverse` (qr.rs:262-279).
+    pub fn try_inverse(&self) -> Option<DeviceMatrix> {
+        let n = self.a.nrows;
+        let mut res = DeviceMatrix::from_dmatrix(&DMatrix::<f64>::identity(n, n));
+        if self.solve_cols(&mut res) { Some(res) } else { None }
+    }
+
+    /// `QR::is_invertible` (qr.rs:281-292).
+    pub fn is_invertible(&self) -> bool {
+        self.invertible
+    }
+
+    /// argmin ||A x - b|| for a tall factorization: `Err` naming the first
+    /// zero R_kk when A is rank deficient.
+    pub fn solve_least_squares(mut self, b: &DeviceMatrix) -> Result<DeviceMatrix, usize> {
+        assert!(self.diag.is_none(), "solve_least_squares: a tall (m > n) QR");
         let (m, n) = (self.a.nrows as c_int, self.a.ncols as c_int);
         assert!(b.nrows == self.a.nrows && b.ncols == 1, "QR solve: one right-hand side of m rows");
         let mut bb = b.clone_owned();

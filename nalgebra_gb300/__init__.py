@@ -37,7 +37,7 @@ __all__ = [
     "DeviceMatrix", "DeviceBatch", "LU", "LUBatch", "Cholesky", "CholeskyBatch", "QRBatch", "solve_refined", "gemm",
     "gemm_batched",
     "PosvLogdet", "cholesky_solve_refined_host",
-    "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE", "FullPivLU", "ColPivQR",
+    "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE", "FullPivLU", "ColPivQR", "QR",
 ]
 
 
@@ -96,11 +96,18 @@ class DeviceMatrix:
 
     # -- factorizations (consume self: the buffer is factored in place) --------
     def _trsv(self, b: "DeviceMatrix", upper: bool, trans: bool, diag=None, flags: int = 0) -> bool:
-        """nacu_dtrsv_batched on one matrix (n <= 128): b is overwritten."""
+        """nacu_dtrsv_batched on one matrix (n <= 128), nacu_dtrsv above: b is
+        overwritten."""
         torch = _torch()
         n = self.nrows
         assert self.is_square() and b.nrows == n, "triangular solve dimension mismatch"
         info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        if n > 128:
+            ws = torch.empty(_lib.load().nacu_trsv_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+            _lib.call("nacu_dtrsv", n, b.ncols, int(upper), int(trans), int(diag is not None),
+                      float(diag if diag is not None else 0.0), self.data.data_ptr(), n, b.data.data_ptr(), n,
+                      info.data_ptr(), ws.data_ptr(), ws.numel(), flags, _stream_ptr())
+            return int(info.item()) == 0
         _lib.call("nacu_dtrsv_batched", n, b.ncols, int(upper), int(trans), int(diag is not None),
                   float(diag if diag is not None else 0.0), self.data.data_ptr(), n * n, b.data.data_ptr(),
                   n * b.ncols, info.data_ptr(), 1, flags, _stream_ptr())
@@ -159,6 +166,14 @@ class DeviceMatrix:
         """Matrix::full_piv_lu (src/linalg/decomposition.rs:39-45): factors in
         place (n <= 128)."""
         return FullPivLU(self, flags)
+
+    def qr(self, flags: int = 0) -> "QR":
+        """Matrix::qr (src/linalg/decomposition.rs:56-62): factors in place
+        (square, n <= 128).  Tall least-squares batches go through
+        DeviceBatch.qr."""
+        if not self.is_square():
+            raise NotImplementedError("the square QR kernel takes n x n matrices; use DeviceBatch.qr for least squares")
+        return QR(self, flags)
 
     def col_piv_qr(self, flags: int = 0) -> "ColPivQR":
         """Matrix::col_piv_qr (src/linalg/decomposition.rs:65-75): factors in
@@ -366,6 +381,80 @@ class FullPivLU:
         zero = np.nonzero(np.diag(lu) == 0)[0]
         inv = n == 0 or lu[n - 1, n - 1] != 0
         obj.info = torch.tensor([0 if inv else int(zero[0]) + 1], dtype=torch.int32, device="cuda")
+        return obj
+
+
+class QR:
+    """Householder QR of one square matrix (n <= 128): the axes and R in the
+    matrix buffer, the signed diagonal on the device (src/linalg/qr.rs:34-40)."""
+
+    def __init__(self, m: DeviceMatrix, flags: int = 0):
+        torch = _torch()
+        assert m.is_square(), "the batched QR kernel takes square matrices"
+        n = m.nrows
+        self.qr, self.flags = m, flags
+        self.diag = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
+        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        _lib.call("nacu_dqr_batched", n, 0, m.data.data_ptr(), n * n, self.diag.data_ptr(), 0, 0,
+                  self.info.data_ptr(), 1, flags, _stream_ptr())
+
+    def _solve_cols(self, b: DeviceMatrix) -> bool:
+        torch = _torch()
+        n = self.qr.nrows
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        for c0 in range(0, b.ncols, 16):
+            k = min(16, b.ncols - c0)
+            _lib.call("nacu_dqr_solve_batched", n, k, self.qr.data.data_ptr(), n * n, self.diag.data_ptr(),
+                      b.data.data_ptr() + c0 * n * 8, n * k, info.data_ptr(), 1, self.flags, _stream_ptr())
+        return int(info.item()) == 0
+
+    def solve_mut(self, b: DeviceMatrix) -> bool:
+        """QR::solve_mut (src/linalg/qr.rs:204-222): b is overwritten even
+        when it returns False."""
+        assert b.nrows == self.qr.nrows, "QR solve matrix dimension mismatch."
+        return self._solve_cols(b)
+
+    def solve(self, b: DeviceMatrix):
+        """QR::solve (qr.rs:182-198): a new matrix, or None."""
+        res = b.clone_owned()
+        return res if self.solve_mut(res) else None
+
+    def try_inverse(self):
+        """QR::try_inverse (qr.rs:262-279)."""
+        torch = _torch()
+        n = self.qr.nrows
+        out = DeviceMatrix(torch.eye(n, dtype=torch.float64, device="cuda").reshape(-1).clone(), n, n)
+        return out if self._solve_cols(out) else None
+
+    def is_invertible(self) -> bool:
+        """QR::is_invertible (qr.rs:281-292)."""
+        return int(self.info.item()) == 0
+
+    def r(self) -> np.ndarray:
+        """QR::r (qr.rs:81-89): the upper triangle, |diag| on its diagonal."""
+        n = self.qr.nrows
+        r = np.triu(self.qr.to_numpy())
+        r[np.arange(n), np.arange(n)] = np.abs(self.diag.cpu().numpy()[:n])
+        return r
+
+    def to_json(self) -> str:
+        """nalgebra's serde JSON form of QR (src/linalg/qr.rs:34-40)."""
+        n = self.qr.nrows
+        return factor_format.qr_to_json(self.qr.to_numpy(), self.diag.cpu().numpy()[:n])
+
+    @classmethod
+    def from_json(cls, s: str, flags: int = 0) -> "QR":
+        """A square QR from nalgebra's serde JSON form."""
+        torch = _torch()
+        qr, diag = factor_format.qr_from_json(s)
+        if qr.shape[0] != qr.shape[1]:
+            raise ValueError("QR.from_json: the device QR takes square factors")
+        n = qr.shape[0]
+        obj = cls.__new__(cls)
+        obj.qr, obj.flags = DeviceMatrix.from_numpy(qr), flags
+        obj.diag = torch.from_numpy(np.append(diag, np.zeros(max(n, 1) - n))).cuda()
+        zero = np.nonzero(diag == 0)[0]
+        obj.info = torch.tensor([int(zero[0]) + 1 if len(zero) else 0], dtype=torch.int32, device="cuda")
         return obj
 
 

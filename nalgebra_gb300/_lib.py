@@ -46,6 +46,10 @@ SIGNATURES = {
     "nacu_dfullpivlu_solve_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dcolpivqr_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dcolpivqr_solve_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_dqr_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_trsv_workspace_bytes": (_sz, [_i]),
+    "nacu_dtrsv": (_i, [_i, _i, _i, _i, _i, _d, _vp, _i64, _vp, _i64, _vp, _vp, _sz, _i, _vp]),
+    "nacu_dqr_solve_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dtrsv_batched": (_i, [_i, _i, _i, _i, _i, _d, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dchol_rank1_update_batched": (_i, [_i, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dchol_remove_column_batched": (_i, [_i, _vp, _i64, _i, _vp, _i64, _i, _i, _vp]),

@@ -1,6 +1,10 @@
 // Batched QR with column pivoting (n <= 128): the GPU form of nalgebra's
 // ColPivQR::new (src/linalg/col_piv_qr.rs:59-92), ColPivQR::solve_mut
 // (:227-247) and, on identity right-hand sides, try_inverse (:288-303).
+// Without the pivot search (PIVOT = false) the same kernel is nalgebra's plain
+// square QR: QR::new (src/linalg/qr.rs:55-76, the same clear_column_unchecked
+// steps on the unswapped columns), QR::solve_mut (:204-256: q_tr_mul, then the
+// upper solve by |diag_i|, no permutation) and QR::try_inverse (:262-279).
 //
 // One CTA per system; the matrix and the right-hand sides live in shared
 // memory (column-major, odd leading dimension).  Per step i:
@@ -137,7 +141,8 @@ __device__ __forceinline__ double neg_bits(double x) {
 }
 
 // mode: 0 = factor, 1 = factor + solve, 2 = solve from given factors.
-template <bool EXACT>
+// PIVOT = false: no column search or swap, no pivots read or written.
+template <bool EXACT, bool PIVOT>
 __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, double* __restrict__ A, int64_t strideA,
                                                               double* __restrict__ diag, int32_t* __restrict__ jpiv,
                                                               double* __restrict__ B, int64_t strideB,
@@ -174,14 +179,14 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
     if (mode == 2)
       for (int i = tid; i < n; i += kCqThreads) {
         s_diag[i] = diag[(size_t)s * n + i];
-        s_jpiv[i] = jpiv[(size_t)s * n + i];
+        s_jpiv[i] = PIVOT ? jpiv[(size_t)s * n + i] : i;
       }
     __syncthreads();
 
     if (mode != 2) {
       uint64_t bkey = 0;
       int bidx = 0x7fffffff;
-      for (int e = tid; e < n * n; e += kCqThreads) {  // the first search, over the whole matrix
+      for (int e = PIVOT ? tid : n * n; e < n * n; e += kCqThreads) {  // the first search, over the whole matrix
         const int c = e / n, r = e - c * n;
         const uint64_t k = pivot_key(sa[(size_t)c * ld + r], e == 0);
         if (bidx == 0x7fffffff || k > bkey) {
@@ -198,10 +203,13 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
       for (int i = 0; i < n; ++i) {
         const int L = n - i;
         if (warp == 0) {
-          uint64_t key = lane < kCqWarps ? s_key[lane] : 0ull;
-          int idx = lane < kCqWarps ? s_idx[lane] : 0x7fffffff;
-          warp_argmax(key, idx);
-          const int cp = i + idx / L;
+          int cp = i;
+          if constexpr (PIVOT) {
+            uint64_t key = lane < kCqWarps ? s_key[lane] : 0ull;
+            int idx = lane < kCqWarps ? s_idx[lane] : 0x7fffffff;
+            warp_argmax(key, idx);
+            cp = i + idx / L;
+          }
           if (cp != i)  // swap_columns(i, cp)
             for (int r = lane; r < n; r += 32) {
               const double t = sa[(size_t)i * ld + r];
@@ -279,7 +287,7 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
               }
               col[rr] = val;
             }
-            if (c < n && rr > 0) {  // rows i+1.. of the matrix columns, column-major in the next submatrix
+            if (PIVOT && c < n && rr > 0) {  // rows i+1.. of the matrix columns, column-major in the next submatrix
               const int en = cq * lm + (rr - 1);  // increases with e: the first of equal keys stays
               const uint64_t kk = pivot_key(val, en == 0);
               if (bi == 0x7fffffff || kk > bk) {
@@ -339,7 +347,7 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
           for (int r = lane; r < i; r += 32) bc[r] = axpy1<EXACT>(bc[r], -coeff, uc[r]);
           __syncwarp();
         }
-        if (lane == 0)  // p.inv_permute_rows, whatever the upper solve returned
+        if (PIVOT && lane == 0)  // p.inv_permute_rows, whatever the upper solve returned
           for (int k = n - 1; k >= 0; --k) {
             const int q = s_jpiv[k];
             if (q != k) {
@@ -359,7 +367,7 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
       }
       for (int i = tid; i < n; i += kCqThreads) {
         diag[(size_t)s * n + i] = s_diag[i];
-        jpiv[(size_t)s * n + i] = s_jpiv[i];
+        if (PIVOT) jpiv[(size_t)s * n + i] = s_jpiv[i];
       }
     }
     if (solve_cols > 0) {  // nalgebra overwrites b even when the upper solve fails
@@ -376,12 +384,14 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
 
 int colpivqr_launch(int n, int nrhs, double* A, int64_t strideA, double* diag, int32_t* jpiv, double* B,
                     int64_t strideB, int32_t* info, int batch, int flags, int mode, cudaStream_t stream,
-                    const char* name) {
+                    const char* name, bool pivot = true) {
   const size_t smem = cq_layout(n, nrhs).total;
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  auto kern = (flags & NACU_FLAG_EXACT) ? colpivqr_kernel<true> : colpivqr_kernel<false>;
+  const bool exact = (flags & NACU_FLAG_EXACT) != 0;
+  auto kern = pivot ? (exact ? colpivqr_kernel<true, true> : colpivqr_kernel<false, true>)
+                    : (exact ? colpivqr_kernel<true, false> : colpivqr_kernel<false, false>);
   if (smem > 48 * 1024) {
     const cudaError_t e = ensure_dynamic_smem(kern, smem);
     if (e != cudaSuccess) return record_cuda_error(e, name);
@@ -429,6 +439,34 @@ int nacu_dcolpivqr_solve_batched(int n, int nrhs, const double* QR, int64_t stri
   // mode 2 reads the factors, diag and pivots and writes only B and info
   return colpivqr_launch(n, nrhs, const_cast<double*>(QR), strideA, const_cast<double*>(diag),
                          const_cast<int32_t*>(jpiv), B, strideB, info, batch, flags, 2, (cudaStream_t)stream, name);
+}
+
+int nacu_dqr_batched(int n, int nrhs, double* A, int64_t strideA, double* diag, double* B, int64_t strideB,
+                     int32_t* info, int batch, int flags, nacu_stream_t stream) {
+  const char* name = "nacu_dqr_batched";
+  if (n < 0 || n > kCqMaxN) return record_arg_error(-1, "QR batched: n out of range [0, 128]");
+  if (nrhs < 0 || nrhs > kCqMaxRhs) return record_arg_error(-2, "QR batched: nrhs out of range [0, 16]");
+  if (batch < 0) return record_arg_error(-9, "QR batched: negative batch");
+  if (batch == 0 || n == 0) return NACU_SUCCESS;
+  if (!A || !diag || (nrhs > 0 && !B)) return record_arg_error(-3, "QR batched: null pointer");
+  if (strideA < (int64_t)n * n) return record_arg_error(-4, "QR batched: strideA < n*n");
+  if (nrhs > 0 && strideB < (int64_t)n * nrhs) return record_arg_error(-7, "QR batched: strideB < n*nrhs");
+  return colpivqr_launch(n, nrhs, A, strideA, diag, nullptr, B, strideB, info, batch, flags, nrhs > 0 ? 1 : 0,
+                         (cudaStream_t)stream, name, false);
+}
+
+int nacu_dqr_solve_batched(int n, int nrhs, const double* QR, int64_t strideA, const double* diag, double* B,
+                           int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream) {
+  const char* name = "nacu_dqr_solve_batched";
+  if (n < 0 || n > kCqMaxN) return record_arg_error(-1, "QR solve: n out of range [0, 128]");
+  if (nrhs < 0 || nrhs > kCqMaxRhs) return record_arg_error(-2, "QR solve: nrhs out of range [0, 16]");
+  if (batch < 0) return record_arg_error(-9, "QR solve: negative batch");
+  if (batch == 0 || n == 0 || nrhs == 0) return NACU_SUCCESS;
+  if (!QR || !diag || !B) return record_arg_error(-3, "QR solve: null pointer");
+  if (strideA < (int64_t)n * n) return record_arg_error(-4, "QR solve: strideA < n*n");
+  if (strideB < (int64_t)n * nrhs) return record_arg_error(-7, "QR solve: strideB < n*nrhs");
+  return colpivqr_launch(n, nrhs, const_cast<double*>(QR), strideA, const_cast<double*>(diag), nullptr, B, strideB,
+                         info, batch, flags, 2, (cudaStream_t)stream, name, false);
 }
 
 }  // extern "C"

@@ -66,6 +66,7 @@ def lib():
             "orc_dgeqrf": (None, [_i64, _i64, _dp, _i64, _dp]),
             "orc_dqr_q_tr_mul": (None, [_i64, _i64, _dp, _i64, _dp, _dp, _i64, _i64]),
             "orc_dqr_ls_solve": (C.c_int, [_i64, _i64, _dp, _i64, _dp, _dp, _i64, _dp, _i64, _i64]),
+            "orc_dqr_solve": (C.c_int, [_i64, _dp, _i64, _dp, _dp, _i64, _i64]),
             "orc_dgesv_batched": (None, [_i64, _i64, _dp, _i32p, _dp, _i64, _i32p, C.c_int]),
             "orc_dposv_ragged": (None, [_i64, _i32p, _i64p, _dp, _i64p, _dp, _i64, _i32p, _dp, C.c_int]),
             "orc_dgels_batched": (None, [_i64, _i32p, _i64, _i64p, _dp, _i64p, _dp, _dp, _dp, _i32p, C.c_int]),
@@ -316,6 +317,18 @@ def qr_q_tr_mul(qr_, diag, b):
     lib().orc_dqr_q_tr_mul(m, n, _p(qr_), max(m, 1), _p(np.ascontiguousarray(diag, dtype=np.float64)),
                            _p(x2), max(m, 1), x2.shape[1])
     return x
+
+
+def qr_solve(qr_, diag, b):
+    """QR::solve_mut (src/linalg/qr.rs:204-256) on a copy of b.  Returns
+    (x, solved): nalgebra overwrites b even when it returns false."""
+    qr_ = _f64(qr_)
+    n = qr_.shape[0]
+    x = np.array(b, dtype=np.float64, order="F", copy=True)
+    x2 = x.reshape(n, -1, order="F")
+    ok = lib().orc_dqr_solve(n, _p(qr_), max(n, 1), _p(np.ascontiguousarray(diag, dtype=np.float64)), _p(x2),
+                             max(n, 1), x2.shape[1])
+    return x, bool(ok)
 
 
 def qr_r(qr_, diag):

@@ -76,6 +76,10 @@ void orc_dqr_q_tr_mul(int64_t m, int64_t n, const double* qr, int64_t lda, const
                       double* b, int64_t ldb, int64_t nrhs) {
   orc::qr_q_tr_mul<double>(m, n, qr, lda, diag, b, ldb, nrhs);
 }
+int orc_dqr_solve(int64_t n, const double* qr, int64_t lda, const double* diag, double* b, int64_t ldb,
+                  int64_t nrhs) {
+  return orc::qr_solve<double>(n, qr, lda, diag, b, ldb, nrhs) ? 1 : 0;
+}
 int orc_dqr_ls_solve(int64_t m, int64_t n, const double* qr, int64_t lda, const double* diag,
                      double* b, int64_t ldb, double* x, int64_t ldx, int64_t nrhs) {
   return orc::qr_ls_solve<double>(m, n, qr, lda, diag, b, ldb, x, ldx, nrhs);

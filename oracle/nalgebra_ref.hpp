@@ -618,6 +618,27 @@ inline void qr_q_tr_mul(std::size_t m, std::size_t n, const T* qr, std::size_t l
     reflect_with_sign(m - i, qr + i + i * lda, nrhs, b + i, ldb, signum(diag[i]));
 }
 
+// QR::solve_mut (qr.rs:204-256) for an n x n factor: q_tr_mul (:157-171),
+// then the upper solve of :224-256 (for each column, i descending: a zero
+// |diag_i| returns false at once, leaving that column partly and the later
+// ones not solved; else b_i / |diag_i| and the axpy with R's column above i).
+template <class T>
+inline bool qr_solve(std::size_t n, const T* qr, std::size_t lda, const T* diag, T* b, std::size_t ldb,
+                     std::size_t nrhs) {
+  qr_q_tr_mul(n, n, qr, lda, diag, b, ldb, nrhs);
+  for (std::size_t c = 0; c < nrhs; ++c) {
+    T* bc = b + c * ldb;
+    for (std::size_t ii = n; ii-- > 0;) {
+      const T d = std::fabs(diag[ii]);
+      if (d == T(0)) return false;
+      const T coeff = bc[ii] / d;
+      bc[ii] = coeff;
+      axpy(ii, -coeff, qr + ii * lda, T(1), bc);
+    }
+  }
+  return true;
+}
+
 // ColPivQR::new (src/linalg/col_piv_qr.rs:59-92): per step the column of
 // icamax_full over the trailing submatrix (its largest |a|, min_max.rs:146-167),
 // the column swap, then clear_column_unchecked as QR::new.  jpiv[i] is the
