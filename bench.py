@@ -1059,6 +1059,171 @@ def bench_col_piv_qr_ours(args, rank, world):
     return res
 
 
+def bench_trsv_large_ours(args, rank, world):
+    """Triangular solves of one large matrix (nacu_dtrsv) at the reference's
+    solve benchmark shape (benches/linalg/solve.rs: 1000x1000, one vector;
+    entries U[0, 1) as DMatrix::new_random, plus n on the diagonal so the
+    solutions stay finite) for the four variants, and solve_lower_triangular at
+    n = 8192 (a 256 MiB triangle, larger than L2).  One solve per launch; the
+    1000x1000 triangle (4 MB) stays in L2 between launches, as the reference's
+    CPU bench keeps it in cache.  HBM roofline at n = 8192: the triangle read
+    once, b read and x written."""
+    import time
+
+    import torch
+
+    import oracle as O
+    from nalgebra_gb300 import _lib
+
+    L = _lib.load()
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    rng = np.random.default_rng(rank)
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    out, cpu = {}, {}
+    for n in (1000, 8192):
+        t = rng.random((n, n)) + n * np.eye(n)
+        b = rng.random(n)
+        T = torch.from_numpy(np.asfortranarray(t).ravel(order="F")).cuda()
+        b0 = torch.from_numpy(b).cuda()
+        B = b0.clone()
+        ws = torch.empty(L.nacu_trsv_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+        variants = (("solve_lower_triangular", 0, 0), ("solve_upper_triangular", 1, 0),
+                    ("tr_solve_lower_triangular", 0, 1), ("tr_solve_upper_triangular", 1, 1))
+        if n > 1000:
+            variants = variants[:1]
+        reps = 20 if n <= 1000 else 4
+        for name, upper, trans in variants:
+            def launch():
+                _lib.call("nacu_dtrsv", n, 1, upper, trans, 0, 0.0, T.data_ptr(), n, B.data_ptr(), n,
+                          info.data_ptr(), ws.data_ptr(), ws.numel(), 0, sp)
+            for _ in range(args.warmup):
+                B.copy_(b0); launch()
+            torch.cuda.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+            with ClockSampler(torch.cuda.current_device()) as clk:
+                for i in range(args.steps):
+                    ev[i][0].record(stream)
+                    for _ in range(reps):
+                        launch()  # re-solving in place: same work, same data movement
+                    ev[i][1].record(stream)
+                torch.cuda.synchronize()
+            ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev])) / reps
+            B.copy_(b0); launch(); torch.cuda.synchronize()
+            x = B.cpu().numpy()
+            tri = np.triu(t) if upper else np.tril(t)
+            m = tri.T if trans else tri
+            rel = float(np.abs(m @ x - b).max() / np.abs(b).max())
+            key = f"{name}_{n}"
+            out[key] = {"ms": ms, "solves_per_s": 1e3 / ms, "rel_residual": rel, "info": int(info.item()),
+                        "clocks": clk.summary()}
+            if rank == 0 and not args.no_cpu_baseline and name == "solve_lower_triangular":
+                k = 5 if n <= 1000 else 1
+                t0 = time.perf_counter()
+                for _ in range(k):
+                    O.triangular_solve(tri, b)
+                cpu[key] = (time.perf_counter() - t0) / k * 1e3
+        del T
+        torch.cuda.empty_cache()
+    head = out["solve_lower_triangular_1000"]
+    big = out["solve_lower_triangular_8192"]
+    n = 8192
+    bytes_big = (n * (n + 1) / 2 + 2 * n) * 8
+    peaks = read_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6794.8)) if peaks else 6794.8
+    achieved = bytes_big / (big["ms"] * 1e-3) / 1e9
+    res = {"metric": "solves/s (solve_lower_triangular, one 1000x1000 f64 matrix, one vector)",
+           "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (U[0,1) entries, n added on the diagonal)",
+           "config": {"workload": "trsv_large", "n": [1000, 8192], "nrhs": 1,
+                      "l2": "1000x1000 L2-resident (4 MB), 8192x8192 triangle 256 MiB > L2"},
+           "forms": out,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                        "traffic": None, "workload": "solve_lower_triangular at n = 8192",
+                        "note": "the 64-row blocks form a dependency chain; n(n+1)/2 doubles + 2n per solve"},
+           "gpu_launches": args.steps * 20, "clocks": head["clocks"]}
+    if cpu:
+        res["cpu_baseline"] = {"value": 1e3 / cpu["solve_lower_triangular_1000"], "unit": "solves/s", "cores": 1,
+                               "kind": "port", "ms_at_8192": cpu.get("solve_lower_triangular_8192"),
+                               "sample": "oracle solve_lower_triangular (nalgebra's column axpy loop), one thread, "
+                                         "5 solves at n = 1000, 1 at n = 8192"}
+    return res
+
+
+def bench_qr_square_ours(args, rank, world):
+    """Batched square QR::new + QR::solve (src/linalg/qr.rs:55-76, 204-256) at
+    the reference's QR solve benchmark shape (benches/linalg/qr.rs: 100x100,
+    one vector; entries U[0, 1) as DMatrix::new_random): 4096 systems per step
+    (nacu_dqr_batched, the solve fused).  Work: 4/3 n^3 + 3 n^2 flops per
+    system; FP64 roofline."""
+    import time
+
+    import torch
+
+    import oracle as O
+    from nalgebra_gb300 import _lib
+
+    L = _lib.load()
+    count, n = 4096, 100
+    rng = np.random.default_rng(rank)
+    a = rng.random((count, n, n))
+    b = rng.random((count, n))
+    a0 = torch.from_numpy(np.ascontiguousarray(np.transpose(a, (0, 2, 1))).reshape(count, n * n)).cuda()
+    b0 = torch.from_numpy(b).cuda()
+    A, B = a0.clone(), b0.clone()
+    diag = torch.zeros(count * n, dtype=torch.float64, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    flags = 1 if args.exact else 0
+
+    def launch():
+        _lib.call("nacu_dqr_batched", n, 1, A.data_ptr(), n * n, diag.data_ptr(), B.data_ptr(), n, info.data_ptr(),
+                  count, flags, sp)
+
+    for _ in range(args.warmup):
+        A.copy_(a0); B.copy_(b0); launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            A.copy_(a0); B.copy_(b0); flush.zero_()
+            ev[i][0].record(stream)
+            launch()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+    x = B.cpu().numpy()
+    berr = 0.0
+    for s in range(0, count, 256):
+        berr = max(berr, float(np.abs(a[s] @ x[s] - b[s]).max() / (np.abs(a[s]).max() * np.abs(x[s]).max() * n)))
+    flops = count * (4.0 / 3 * n ** 3 + 3.0 * n ** 2)
+    peak = ctypes_probe(L)
+    res = {"metric": "solves/s (batched QR factor+solve, 4096 x 100x100 f64)", "value": count / (ms * 1e-3),
+           "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (U[0,1) entries, as DMatrix::new_random)",
+           "config": {"workload": "qr_square", "count": count, "n": n, "exact": bool(args.exact),
+                      "l2": "256 MB flush between steps"},
+           "gflops": flops / (ms * 1e-3) / 1e9, "backward_error_sample_in_eps": berr / np.finfo(float).eps,
+           "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak / 1e12,
+                        "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / peak, "traffic": None,
+                        "peak_source": fp64_peak_source()},
+           "gpu_launches": args.steps, "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = 200
+        t0 = time.perf_counter()
+        for s in range(sample):
+            qr, d = O.qr(a[s])
+            O.qr_solve(qr, d, b[s])
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": sample / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                               "sample": f"{sample} of the {count} systems, oracle QR::new + QR::solve, one thread"}
+    return res
+
+
 # ----------------------------------------------------------------------------- QR least squares
 
 def bench_ls_ours(args, rank, world):
@@ -1503,6 +1668,9 @@ def other_configs(args, rank, world) -> dict:
         ("5a_gemm", bench_gemm_ours, dict(count=0, steps=min(args.steps, 10)), ("forms",)),
         ("5b_ls_qr", bench_ls_ours, dict(count=0), ("accuracy",)),
         ("f2_mul_batched_100", bench_mul_batched_ours, dict(count=0), ("forms", "accuracy", "cpu_baseline")),
+        ("f2_trsv_large_1000", bench_trsv_large_ours, dict(count=0, steps=min(args.steps, 5)),
+         ("forms", "cpu_baseline")),
+        ("f_qr_square_100", bench_qr_square_ours, dict(count=0), ("cpu_baseline", "backward_error_sample_in_eps")),
     )
     for name, fn, over, keep in plan:
         a = copy.copy(args)
@@ -1532,7 +1700,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
                                                                   "mixed_lu", "lu_inverse", "trsv_batched", "chol_update",
-                                                                        "full_piv_lu", "col_piv_qr", "mul_batched"])
+                                                                        "full_piv_lu", "col_piv_qr", "mul_batched",
+                                                                        "trsv_large", "qr_square"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--single-launch", action="store_true",
                     help="ragged_cholesky: one launch over a host-sorted order with the default tile "
@@ -1571,14 +1740,15 @@ def main():
         torch.distributed.barrier()
 
     if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse", "trsv_batched",
-                         "chol_update", "full_piv_lu", "col_piv_qr", "mul_batched"):
+                         "chol_update", "full_piv_lu", "col_piv_qr", "mul_batched", "trsv_large", "qr_square"):
         res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
                "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours,
                "lu_inverse": bench_lu_inverse_ours, "trsv_batched": bench_trsv_ours,
                "chol_update": bench_chol_update_ours,
                "full_piv_lu": bench_full_piv_lu_ours,
-               "col_piv_qr": bench_col_piv_qr_ours, "mul_batched": bench_mul_batched_ours}[args.workload](args, rank,
-                                                                                                        world)
+               "col_piv_qr": bench_col_piv_qr_ours, "mul_batched": bench_mul_batched_ours,
+               "trsv_large": bench_trsv_large_ours, "qr_square": bench_qr_square_ours}[args.workload](args, rank,
+                                                                                                       world)
         if rank == 0:
             print(json.dumps(res))
         return

@@ -18,10 +18,21 @@ constexpr int kRowsPerPass = 256;  // rows of the panel update held in registers
 // correctly rounded sqrt and 1/sqrt as two operations; the FMA form derives
 // both from one reciprocal square root (one dependent FP64 chain instead of
 // two: on this part every dependent FP64 step costs tens of cycles).
+// d in (0, +inf], NaN excluded (the test !(d <= 0) && d >= 0), on the bits:
+// an FP64 compare costs a warp-wide FP64 issue slot.
+__device__ __forceinline__ bool pos_or_inf(double d) {
+  const long long b = __double_as_longlong(d);
+  return b > 0 && b <= 0x7ff0000000000000ll;
+}
+__device__ __forceinline__ bool pos_or_inf(float d) {
+  const int b = __float_as_int(d);
+  return b > 0 && b <= 0x7f800000;
+}
+
 template <bool EXACT, typename T>
 __device__ __forceinline__ bool chol_pivot(T d, int has_subst, double subst, T* denom, T* rcp) {
   T v;
-  if (!(d <= T(0)) && d >= T(0)) v = d;
+  if (pos_or_inf(d)) v = d;
   else if (has_subst && !(subst <= 0.0) && subst >= 0.0) v = (T)subst;
   else return false;
   if constexpr (EXACT) {
@@ -48,19 +59,31 @@ __device__ void chol_factor_cta(int n, T* __restrict__ a, int ldp, T* __restrict
     const int jb = min(NB, n - J0);
     const int rows = n - J0;
     // Phase 1+2: P = A[J0.., J0..J0+jb] - L[J0.., 0..J0] * L[J0..J0+jb, 0..J0]^T
-    // (lower part).  Warp w owns columns 4w..4w+3, lanes own rows lane + 32q;
-    // each element still takes its updates in order k = 0, 1, ..., J0-1.
-    for (int cg = warp * 4; cg < jb; cg += (nthr >> 5) * 4) {
-      for (int rb = 0; rb < rows; rb += kRowsPerPass) {
-        const int qmax = min(8, (rows - rb + 31) >> 5);
-        T acc[8][4];
+    // (lower part); each element still takes its updates in order k = 0, 1,
+    // ..., J0-1.  On this part a warp-wide FP64 instruction costs its full
+    // pipe time whatever lanes are masked, so the lanes are laid out to waste
+    // few: a warp instruction covers NB/4 column groups of 4 x R = 128/NB rows
+    // (rows below the panel's head, in R-row slabs spread over the warps), and
+    // the head's lower triangle (c <= r < jb) is a flat list of elements, one
+    // per thread.  With 32 rows per column group and the head as a square,
+    // 26% of the lanes of the ragged workload's updates were idle; now 10%.
+    {
+      constexpr int G = NB / 4;  // column groups per warp instruction
+      constexpr int R = 32 / G;  // rows per warp instruction
+      constexpr int QMAX = 8;    // slabs per thread and pass
+      static_assert(NB % 4 == 0 && 32 % G == 0 && G <= 32, "panel width");
+      const int nw = nthr >> 5;
+      const int g4 = (lane / R) * 4, rl = lane % R;
+      const int nslab = (rows - jb + R - 1) / R;
+      for (int sb = 0; sb < nslab; sb += QMAX * nw) {
+        T acc[QMAX][4];
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
+        for (int i = 0; i < QMAX; ++i) {
+          const int r = jb + (sb + warp + nw * i) * R + rl;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int r = rb + lane + 32 * q, c = cg + j;
-            acc[q][j] = (q < qmax && r < rows && c < jb && r >= c) ? a[(size_t)(J0 + c) * n + J0 + r] : T(0);
-          }
+          for (int j = 0; j < 4; ++j)
+            acc[i][j] = (r < rows && g4 + j < jb) ? a[(size_t)(J0 + g4 + j) * n + J0 + r] : T(0);
+        }
         const T* colk = a + J0;
 #pragma unroll 2
         for (int k = 0; k < J0; ++k, colk += n) {
@@ -68,24 +91,41 @@ __device__ void chol_factor_cta(int n, T* __restrict__ a, int ldp, T* __restrict
           // -x would cost one FP64 instruction per load).
           T lc[4];
 #pragma unroll
-          for (int j = 0; j < 4; ++j) lc[j] = (cg + j < jb) ? colk[cg + j] : T(0);
+          for (int j = 0; j < 4; ++j) lc[j] = (g4 + j < jb) ? colk[g4 + j] : T(0);
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            if (q < qmax) {
-              const int r = rb + lane + 32 * q;
+          for (int i = 0; i < QMAX; ++i) {
+            if (sb + warp + nw * i < nslab) {  // warp-uniform
+              const int r = jb + (sb + warp + nw * i) * R + rl;
               const T lr = (r < rows) ? colk[r] : T(0);
 #pragma unroll
-              for (int j = 0; j < 4; ++j) acc[q][j] = axpy1<EXACT>(acc[q][j], -lc[j], lr);
+              for (int j = 0; j < 4; ++j) acc[i][j] = axpy1<EXACT>(acc[i][j], -lc[j], lr);
             }
           }
         }
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
+        for (int i = 0; i < QMAX; ++i) {
+          const int r = jb + (sb + warp + nw * i) * R + rl;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int r = rb + lane + 32 * q, c = cg + j;
-            if (q < qmax && r < rows && c < jb && r >= c) P[(size_t)c * ldp + r] = acc[q][j];
-          }
+          for (int j = 0; j < 4; ++j)
+            if (sb + warp + nw * i < nslab && r < rows && g4 + j < jb) P[(size_t)(g4 + j) * ldp + r] = acc[i][j];
+        }
+      }
+      // the head: element e = r(r+1)/2 + c of the lower triangle
+      const int H = jb * (jb + 1) / 2;
+      for (int e0 = 0; e0 < H; e0 += nthr) {
+        const int e = e0 + tid;
+        int r = 0;
+        while ((r + 1) * (r + 2) / 2 <= e) ++r;  // at most NB steps, integer only
+        const int c = e - r * (r + 1) / 2;
+        const bool on = e < H;
+        T acc = on ? a[(size_t)(J0 + c) * n + J0 + r] : T(0);
+        const T* colk = a + J0;
+#pragma unroll 4
+        for (int k = 0; k < J0; ++k, colk += n) {
+          const T lrk = on ? colk[r] : T(0), lck = on ? colk[c] : T(0);
+          acc = axpy1<EXACT>(acc, -lck, lrk);
+        }
+        if (on) P[(size_t)c * ldp + r] = acc;
       }
     }
     __syncthreads();
@@ -174,19 +214,40 @@ __device__ void chol_forward_cta(int n, const T* __restrict__ a, T* X, int ldx, 
 #pragma unroll
       for (int c = 0; c < kRhsChunk; ++c) b[c] = (lane < ib && c < nr) ? X[(size_t)c * ldx + I0 + lane] : T(0);
       const T rd = (lane < ib) ? rdiag[I0 + lane] : T(0);
+      if constexpr (EXACT || sizeof(T) != 8) {  // EXACT, and FP32 (latency-bound: the short chain)
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        if (i < ib) {
+        for (int i = 0; i < 32; ++i) {
+          if (i < ib) {
 #pragma unroll
-          for (int c = 0; c < kRhsChunk; ++c) {
-            if (lane == i) {
-              if constexpr (EXACT) b[c] = b[c] / lrow[i];  // solve.rs:509: b_i / L_ii
-              else b[c] = b[c] * rd;
+            for (int c = 0; c < kRhsChunk; ++c) {
+              if (lane == i) {
+                if constexpr (EXACT) b[c] = b[c] / lrow[i];  // solve.rs:509: b_i / L_ii
+                else b[c] = b[c] * rd;
+              }
+              const T y = __shfl_sync(0xffffffffu, b[c], i);
+              if (lane > i) b[c] = axpy1<EXACT>(b[c], -y, lrow[i]);
             }
-            const T y = __shfl_sync(0xffffffffu, b[c], i);
-            if (lane > i) b[c] = axpy1<EXACT>(b[c], -y, lrow[i]);
           }
         }
+      } else {
+        // L's columns pre-scaled by 1/L_ii, so the chain broadcasts the
+        // unscaled b_i and each step is one FMA per right-hand side (a
+        // one-lane scale per step would cost a warp-wide FP64 slot); the
+        // rows are scaled once at the end.
+#pragma unroll
+        for (int i = 0; i < 32; ++i) lrow[i] *= (i < ib) ? rdiag[I0 + i] : T(0);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          if (i < ib) {
+#pragma unroll
+            for (int c = 0; c < kRhsChunk; ++c) {
+              const T y = __shfl_sync(0xffffffffu, b[c], i);
+              if (lane > i) b[c] = fma(-y, lrow[i], b[c]);
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < kRhsChunk; ++c) b[c] *= rd;
       }
 #pragma unroll
       for (int c = 0; c < kRhsChunk; ++c)
@@ -219,10 +280,11 @@ __device__ void chol_forward_cta(int n, const T* __restrict__ a, T* X, int ldx, 
   }
 }
 
-// Back solve L^T x = y, FMA form: blocked from the bottom, reductions over the
-// rows below each 32-row block, then a warp solve of the transposed block.
+// Back solve L^T x = y, FMA form, FP32: blocked from the bottom, reductions
+// over the rows below each 32-row block (16 sums per lane, one 32-lane
+// reduce-scatter), then a warp solve of the transposed block.
 template <typename T>
-__device__ void chol_backward_fast_cta(int n, const T* __restrict__ a, T* X, int ldx, int nr, const T* rdiag) {
+__device__ void chol_backward_fast32_cta(int n, const T* __restrict__ a, T* X, int ldx, int nr, const T* rdiag) {
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
   const int nblocks = (n + 31) / 32;
@@ -297,6 +359,108 @@ __device__ void chol_backward_fast_cta(int n, const T* __restrict__ a, T* X, int
     }
     __syncthreads();
   }
+}
+
+// The same in FP64 with fewer warp-wide FP64 instructions: blocked from the
+// bottom, reductions over the rows below each 32-row block, then a warp solve
+// of the transposed block.
+template <typename T>
+__device__ void chol_backward_fast64_cta(int n, const T* __restrict__ a, T* X, int ldx, int nr, const T* rdiag) {
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
+  const int nblocks = (n + 31) / 32;
+  for (int bI = nblocks - 1; bI >= 0; --bI) {
+    const int I0 = bI * 32;
+    const int ib = min(32, n - I0);
+    const int r0 = I0 + ib;
+    if (r0 < n) {
+      // y_i -= sum_{r >= r0} L[r][i] x_r for the block's columns i: warp w
+      // owns 4 columns at a time, lane = 8 column-lane x 4 + row-lane: lane
+      // (cc, rho) accumulates column cb + cc over rows r0 + rho + 8t for the
+      // 4 right-hand sides (8 consecutive rows per column load), then a
+      // reduce-scatter over the 8 row-lanes (4 adds per lane instead of the
+      // 31 of a 32-lane reduction of 16 sums: each is a warp-wide FP64 slot).
+      const int rho = lane & 7, cc = lane >> 3;
+      for (int cb = warp * 4; cb < ib; cb += nwarps * 4) {
+        const bool colok = cb + cc < ib;
+        const T* lcol = a + (size_t)(I0 + cb + (colok ? cc : 0)) * n;
+        T v[4] = {T(0), T(0), T(0), T(0)};
+        for (int rr = r0 + rho; rr < n; rr += 32) {  // four rows per lane and step: 4 loads in flight
+          T l4[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int r = rr + 8 * h;
+            l4[h] = (colok && r < n) ? lcol[r] : T(0);
+          }
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int r = rr + 8 * h;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              const T xr = (c < nr && r < n) ? X[(size_t)c * ldx + r] : T(0);
+              v[c] = fma(l4[h], xr, v[c]);
+            }
+          }
+        }
+        // reduce-scatter over lane bits 0..2: lane keeps right-hand side
+        // c = 2 * bit2 + bit1 (lanes differing in bit 0 hold the same sum)
+        {
+          const bool up4 = (lane & 4) != 0;
+#pragma unroll
+          for (int t = 0; t < 2; ++t) {
+            const T keep = up4 ? v[t + 2] : v[t];
+            const T give = up4 ? v[t] : v[t + 2];
+            v[t] = keep + __shfl_xor_sync(0xffffffffu, give, 4);
+          }
+          const bool up2 = (lane & 2) != 0;
+          const T keep = up2 ? v[1] : v[0];
+          const T give = up2 ? v[0] : v[1];
+          v[0] = keep + __shfl_xor_sync(0xffffffffu, give, 2);
+          v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+        }
+        const int c = ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+        if ((lane & 1) == 0 && colok && c < nr) X[(size_t)c * ldx + I0 + cb + cc] -= v[0];
+      }
+      __syncthreads();
+    }
+    if (warp == 0) {
+      // lane j holds column j of the diagonal block, pre-scaled by 1/L_ii
+      // (row i), so the chain broadcasts the unscaled y_i: one FMA per step
+      T lcol[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        lcol[i] = (lane < ib && i < ib && i >= lane) ? a[(size_t)(I0 + lane) * n + I0 + i] * rdiag[I0 + i] : T(0);
+      const T rd = (lane < ib) ? rdiag[I0 + lane] : T(0);
+      T y[kRhsChunk];
+#pragma unroll
+      for (int c = 0; c < kRhsChunk; ++c) y[c] = (lane < ib && c < nr) ? X[(size_t)c * ldx + I0 + lane] : T(0);
+#pragma unroll
+      for (int i = 31; i >= 0; --i) {
+        if (i < ib) {
+#pragma unroll
+          for (int c = 0; c < kRhsChunk; ++c) {
+            const T yi = __shfl_sync(0xffffffffu, y[c], i);
+            if (lane < i) y[c] = fma(-yi, lcol[i], y[c]);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < kRhsChunk; ++c)
+        if (lane < ib && c < nr) X[(size_t)c * ldx + I0 + lane] = y[c] * rd;
+    }
+    __syncthreads();
+  }
+}
+
+// Back solve L^T x = y, FMA form.  The FP64 variant is bound by the FP64
+// pipe and minimises its warp-wide FP64 instructions; the FP32 variant (the
+// refinement form's solves) is bound by L2 latency and keeps more loads in
+// flight per lane.
+template <typename T>
+__device__ __forceinline__ void chol_backward_fast_cta(int n, const T* __restrict__ a, T* X, int ldx, int nr,
+                                                       const T* rdiag) {
+  if constexpr (sizeof(T) == 8) chol_backward_fast64_cta<T>(n, a, X, ldx, nr, rdiag);
+  else chol_backward_fast32_cta<T>(n, a, X, ldx, nr, rdiag);
 }
 
 // Back solve L^T x = y in nalgebra's exact order (solve.rs:732-755): for i from
