@@ -24,8 +24,9 @@
 // The matrix stays in global memory (L2-resident while the CTA works on it);
 // each 8-column panel is factored in shared memory, then the trailing columns
 // and the right-hand side take the block reflector I - V T^T V^T, one warp per
-// column: one pass computes V^T a (8 partial dots per lane, butterfly
-// reduce-scatter), one pass applies a -= V (T^T V^T a).
+// four columns: one pass computes V^T a (8 partial dots per column and lane,
+// one butterfly reduce-scatter for the 32 sums), one pass applies
+// a -= V (T^T V^T a); each shared-memory axis value feeds four FMAs.
 #include "common.cuh"
 
 namespace nacu {
@@ -77,6 +78,54 @@ __device__ __forceinline__ void warp_reduce_scatter(double (&v)[N]) {
   for (int off = N; off < 32; off <<= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
 }
 
+// c <- c - V T^T V^T c for G columns by one warp (V: the panel's jb axes in
+// shared memory, ld ldp, zero above their diagonal; T: the kQrNB x kQrNB
+// upper-triangular factor in s_t).  Pass 1 forms V^T c for the G columns (8
+// partial dots per column and lane, then one reduce-scatter over all G x 8
+// sums); lane (g, k) forms (T^T w_g)_k; pass 2 applies c -= V w'.
+template <int G>
+__device__ __forceinline__ void qr_apply_reflector(double* const (&cols)[G], int rows, const double* P, int ldp,
+                                                   int jb, const double* s_t, int lane) {
+  constexpr int N = G * kQrNB;
+  double w[N];
+#pragma unroll
+  for (int e = 0; e < N; ++e) w[e] = 0.0;
+  for (int r = lane; r < rows; r += 32) {
+    double v[kQrNB];
+#pragma unroll
+    for (int c = 0; c < kQrNB; ++c) v[c] = (c < jb && r >= c) ? P[(size_t)c * ldp + r] : 0.0;
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const double x = cols[g][r];
+#pragma unroll
+      for (int c = 0; c < kQrNB; ++c) w[g * kQrNB + c] = fma(v[c], x, w[g * kQrNB + c]);
+    }
+  }
+  warp_reduce_scatter<N>(w);  // lane L holds the sum of value L mod N = (g, c)
+  const int idx = lane % N, gq = idx / kQrNB, k = idx % kQrNB;
+  double wk = 0.0;
+#pragma unroll
+  for (int j = 0; j < kQrNB; ++j) {
+    const double wj = __shfl_sync(0xffffffffu, w[0], gq * kQrNB + j);
+    if (j <= k) wk = fma(s_t[kTOff + j * kQrNB + k], wj, wk);
+  }
+  double wp[N];
+#pragma unroll
+  for (int e = 0; e < N; ++e) wp[e] = __shfl_sync(0xffffffffu, wk, e);
+  for (int r = lane; r < rows; r += 32) {
+    double v[kQrNB];
+#pragma unroll
+    for (int c = 0; c < kQrNB; ++c) v[c] = (c < jb && r >= c) ? P[(size_t)c * ldp + r] : 0.0;
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      double x = cols[g][r];
+#pragma unroll
+      for (int c = 0; c < kQrNB; ++c) x = fma(-v[c], wp[g * kQrNB + c], x);
+      cols[g][r] = x;
+    }
+  }
+}
+
 // CTA sum, valid in thread 0 only (the one thread that uses it: the other
 // threads add nothing, which saves the FP64 issue slots of 127 redundant sums).
 __device__ __forceinline__ double block_sum_to0(double v, double* red) {
@@ -90,6 +139,103 @@ __device__ __forceinline__ double block_sum_to0(double v, double* red) {
 #pragma unroll
     for (int w = 0; w < kQrThreads / 32; ++w) s += red[w];
   return s;
+}
+
+// A full panel (kQrNB columns, rows x kQrNB in P) in kQrNB Householder steps,
+// each ONE pass over the rows with ONE CTA reduction: the pass of step j
+// scales axis j, updates the later columns and accumulates, from the updated
+// values, the sums step j+1 needs (|x_{j+1}|^2 and x_{j+1} . P_c for every
+// other column c, x_{j+1} unscaled and unmodified); step j+1 then corrects
+// them for the modified diagonal entry and the axis scale by scalars.  The
+// steps are unrolled, so each pass issues only the FMAs of its live columns:
+// on this part an FP64 instruction with its lanes predicated off still costs
+// its issue slot.  Same reflections as the generic steps (householder.rs:
+// 19-53 without the sign step); the sums are formed in a different order.
+__device__ void qr_panel_full(double* P, int ldp, int rows, int J0, double* s_t, double* s_dstd, double* s_red) {
+  constexpr int NB = kQrNB;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  double* s_sum = s_red + 4;           // 4 warps x NB partial sums
+  double* s_par = s_red + 4 + 4 * NB;  // slot j: the axis scale; slots c > j: the column coefficients
+  {
+    double acc[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) acc[c] = 0.0;
+    for (int r = tid; r < rows; r += kQrThreads) {
+      const double x = P[r];
+      acc[0] = fma(x, x, acc[0]);
+#pragma unroll
+      for (int c = 1; c < NB; ++c) acc[c] = fma(x, P[(size_t)c * ldp + r], acc[c]);
+    }
+    warp_reduce_scatter<NB>(acc);
+    if (lane < NB) s_sum[warp * NB + lane] = acc[0];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    double* pj = P + (size_t)j * ldp;
+    if (tid < NB) {  // lanes 0..NB-1 of warp 0: the scalars (redundantly), then column tid's term
+      double sq = 0.0, dc = 0.0;
+#pragma unroll
+      for (int w = 0; w < kQrThreads / 32; ++w) {
+        sq += s_sum[w * NB + j];
+        dc += s_sum[w * NB + tid];
+      }
+      const double nrm = sqrt(sq);
+      const double x0 = pj[j];
+      const double mod = (x0 >= 0.0) ? x0 : -x0;
+      const double sgn = (x0 >= 0.0) ? 1.0 : -1.0;  // simba to_exp
+      const double signed_norm = sgn * nrm;
+      const double factor = (sq + mod * nrm) * 2.0;
+      const bool nz = factor != 0.0;
+      const double scale = nz ? rsqrt(factor) : 0.0, tau = nz ? 2.0 : 0.0;
+      // v . P_c with v = scale * x', x' = x but x'_j = x0 + signed_norm
+      const double dv = fma(signed_norm, P[(size_t)tid * ldp + j], dc) * scale;
+      if (tid == j) {
+        s_dstd[J0 + j] = nz ? -signed_norm : signed_norm;  // R_std[j][j]
+        s_t[kTauOff + j] = tau;
+        s_par[j] = scale;
+      } else if (tid > j) {
+        s_par[tid] = -tau * dv;
+      } else {
+        s_t[kGSumOff + tid * NB - tid * (tid + 1) / 2 + (j - tid - 1)] = dv;  // G[tid][j] = v_tid . v_j
+      }
+      __syncwarp(0xffu);
+      if (tid == j && nz) pj[j] = x0 + signed_norm;
+    }
+    __syncthreads();
+    const double scale = s_par[j];
+    double coef[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) coef[c] = (c > j) ? s_par[c] : 0.0;
+    double acc[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) acc[c] = 0.0;
+    for (int r = j + tid; r < rows; r += kQrThreads) {
+      const double v = pj[r] * scale;
+      pj[r] = v;
+      double pc[NB];
+#pragma unroll
+      for (int c = j + 1; c < NB; ++c) {
+        pc[c] = fma(coef[c], v, P[(size_t)c * ldp + r]);
+        P[(size_t)c * ldp + r] = pc[c];
+      }
+      if (j + 1 < NB && r > j) {  // step j+1's sums over rows > j
+        const double y = pc[j + 1];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+          if (c == j + 1) acc[c] = fma(y, y, acc[c]);
+          else if (c == j) acc[c] = fma(y, v, acc[c]);
+          else if (c < j) acc[c] = fma(y, P[(size_t)c * ldp + r], acc[c]);
+          else acc[c] = fma(y, pc[c], acc[c]);
+        }
+      }
+    }
+    if (j + 1 < NB) {
+      warp_reduce_scatter<NB>(acc);
+      if (lane < NB) s_sum[warp * NB + lane] = acc[0];
+    }
+    __syncthreads();
+  }
 }
 
 // One problem.  P: panel buffer (ldp x kQrNB), V^T V and T in s_t, per-column
@@ -116,7 +262,8 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
     }
     __syncthreads();
     // ---- panel: jb Householder steps in shared memory ----
-    for (int j = 0; j < jb; ++j) {
+    if (jb == kQrNB) qr_panel_full(P, ldp, rows, J0, s_t, s_dstd, s_red);
+    else for (int j = 0; j < jb; ++j) {
       double* pj = P + (size_t)j * ldp;
       double part = 0.0;
       for (int r = j + tid; r < rows; r += kQrThreads) part = fma(pj[r], pj[r], part);
@@ -203,43 +350,19 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
       __syncthreads();
     }
     // ---- trailing columns and the right-hand side: c <- c - V T^T V^T c ----
+    // four columns per warp at a time (each shared-memory axis value feeds
+    // four FMAs), the columns left over one at a time
     const int ntrail = n - J0 - jb;
     const int ncol = ntrail + (b ? 1 : 0);
-    for (int t = warp; t < ncol; t += kQrThreads / 32) {
-      double* col = (t < ntrail) ? a + (size_t)(J0 + jb + t) * m + J0 : b + J0;
-      double w[kQrNB];
-#pragma unroll
-      for (int c = 0; c < kQrNB; ++c) w[c] = 0.0;
-      for (int r = lane; r < rows; r += 32) {
-        const double x = col[r];
-#pragma unroll
-        for (int c = 0; c < kQrNB; ++c) {
-          const double v = (c < jb && r >= c) ? P[(size_t)c * ldp + r] : 0.0;
-          w[c] = fma(v, x, w[c]);
-        }
-      }
-      // butterfly reduce-scatter: lane L ends with the full sum of w[L & 7]
-      warp_reduce_scatter<kQrNB>(w);
-      // w' = T^T w: lane k (k = lane & 7) forms w'_k, then every lane gathers all
-      const int k = lane & (kQrNB - 1);
-      double wk = 0.0;
-#pragma unroll
-      for (int j = 0; j < kQrNB; ++j) {
-        const double wj = __shfl_sync(0xffffffffu, w[0], j);
-        if (j <= k) wk = fma(s_t[kTOff + j * kQrNB + k], wj, wk);
-      }
-      double wp[kQrNB];
-#pragma unroll
-      for (int j = 0; j < kQrNB; ++j) wp[j] = __shfl_sync(0xffffffffu, wk, j);
-      for (int r = lane; r < rows; r += 32) {
-        double x = col[r];
-#pragma unroll
-        for (int c = 0; c < kQrNB; ++c) {
-          const double v = (c < jb && r >= c) ? P[(size_t)c * ldp + r] : 0.0;
-          x = fma(-v, wp[c], x);
-        }
-        col[r] = x;
-      }
+    auto colptr = [&](int t) { return (t < ntrail) ? a + (size_t)(J0 + jb + t) * m + J0 : b + J0; };
+    const int nfull = ncol / 4;
+    for (int q = warp; q < nfull; q += kQrThreads / 32) {
+      double* cols[4] = {colptr(4 * q), colptr(4 * q + 1), colptr(4 * q + 2), colptr(4 * q + 3)};
+      qr_apply_reflector<4>(cols, rows, P, ldp, jb, s_t, lane);
+    }
+    for (int t = 4 * nfull + warp; t < ncol; t += kQrThreads / 32) {
+      double* cols[1] = {colptr(t)};
+      qr_apply_reflector<1>(cols, rows, P, ldp, jb, s_t, lane);
     }
     __syncthreads();
     // ---- write the factored panel back ----
