@@ -694,6 +694,9 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
   __shared__ T xs[BS];
   __shared__ T rd[BS];
   __shared__ T part[NC][BS];
+  constexpr int kW = kTrsvThreads / 32, kPer = 32 / kW;  // row update: warps, terms per warp
+  constexpr int kH = (BS - 32 + 31) / 32;                 // 32-row groups on the far side of a piece
+  __shared__ T pp[kW * kH * 32];
   __shared__ int s_ticket, s_abort;
   const int tid = threadIdx.x, tr = tid % BS, tc = tid / BS;
   const int n = g.n, lower = g.lower;
@@ -710,16 +713,24 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
   const int r0 = kb * BS, bs = min(BS, n - r0);
   const T* A = g.A;
   const int64_t lda = g.lda;
-  for (int e = tid; e < bs * bs; e += kTrsvThreads) {
-    const int k = e / bs, i = e - k * bs;
-    if (lower ? (i > k) : (i < k)) Ts[k * LD + i] = A[(size_t)(r0 + k) * lda + r0 + i];
-  }
-  if (!lower)
+  // U's columns are pre-scaled by 1 / U_kk, so the diagonal solve takes one
+  // FMA per step on the unscaled values (scaled once when the block is
+  // stored); L has a unit diagonal
+  if (!lower) {
     for (int i = tid; i < bs; i += kTrsvThreads) {
       const T d = A[(size_t)(r0 + i) * lda + r0 + i];
       if (d == T(0)) atomicMin(g.info, r0 + i + 1);
       rd[i] = T(1) / d;
     }
+    __syncthreads();
+  }
+  for (int e = tid; e < bs * bs; e += kTrsvThreads) {
+    const int k = e / bs, i = e - k * bs;
+    if (lower ? (i > k) : (i < k)) {
+      const T v = A[(size_t)(r0 + k) * lda + r0 + i];
+      Ts[k * LD + i] = lower ? v : v * rd[k];
+    }
+  }
   T acc = (tc == 0 && tr < bs) ? g.x[r0 + tr] : T(0);
   for (int q = 0; q < t; ++q) {
     const int jb = lower ? q : nblk - 1 - q;
@@ -778,25 +789,44 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
       } else {
 #pragma unroll
         for (int kk = 31; kk >= 0; --kk) {
-          if (lane == kk && kk < sw) v *= rd[sb + kk];
           const T xk = __shfl_sync(0xffffffffu, v, kk);
           if (lane < kk && kk < sw) v = axpy1<false>(v, -Ts[(sb + kk) * LD + sb + lane], xk);
         }
       }
-      if (lane < sw) xs[sb + lane] = v;
+      if (lane < sw) xs[sb + lane] = v;  // U: unscaled
     }
     __syncthreads();
+    // the block's rows on the far side of the piece (at most BS - 32) take its
+    // contribution: warp w sums its share of the piece's terms for row i0 +
+    // lane (+ 32h), then one thread per row adds the partial sums (a short
+    // chain instead of sw dependent FMAs on one warp)
     const int i0 = lower ? sb + sw : 0, i1 = lower ? bs : sb;
-    for (int i = i0 + tid; i < i1; i += kTrsvThreads) {
-      T acc = xs[i];
-#pragma unroll 8
-      for (int k = 0; k < sw; ++k) acc = axpy1<false>(acc, -Ts[(sb + k) * LD + i], xs[sb + k]);
-      xs[i] = acc;
+    if (i1 > i0) {
+#pragma unroll
+      for (int h = 0; h < kH; ++h) {
+        const int i = i0 + lane + 32 * h;
+        T acc = T(0);
+        if (i < i1)
+#pragma unroll
+          for (int u = 0; u < kPer; ++u) {
+            const int k = kPer * warp + u;
+            if (k < sw) acc = axpy1<false>(acc, -Ts[(sb + k) * LD + i], xs[sb + k]);
+          }
+        pp[(warp * kH + h) * 32 + lane] = acc;
+      }
+      __syncthreads();
+      for (int r = tid; r < i1 - i0; r += kTrsvThreads) {
+        T y = xs[i0 + r];
+#pragma unroll
+        for (int w = 0; w < kW; ++w) y += pp[(w * kH + (r >> 5)) * 32 + (r & 31)];
+        xs[i0 + r] = y;
+      }
     }
     __syncthreads();
   }
-  if (tid < bs) g.x[r0 + tid] = xs[tid];
-  __threadfence();
+  if (tid < bs) g.x[r0 + tid] = lower ? xs[tid] : xs[tid] * rd[tid];
+  // the barrier orders the block's stores before thread 0's release, which is
+  // cumulative over them: a CTA that acquires the flag sees x (no fence needed)
   __syncthreads();
   if (tid == 0 && kb != g.skip_flag) st_release(&g.sync[2 + kb], 1);
 }

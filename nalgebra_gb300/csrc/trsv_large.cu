@@ -85,14 +85,19 @@ __global__ void __launch_bounds__(kTrsvLThreads) trsv_large_kernel(TrsvLArgs g) 
   const int r0 = kb * BS, bs = min(BS, n - r0);
   const double* A = g.A;
   const int64_t lda = g.lda;
-  // the strict triangle of M's diagonal block (M(i, k) = T(k, i) when TRANS)
+  // the strict triangle of M's diagonal block (M(i, k) = T(k, i) when TRANS),
+  // column k pre-scaled by 1 / M_kk: the diagonal solve then broadcasts each
+  // unscaled value and takes one FMA per step (a one-lane scale per step held
+  // the chain for a second warp-wide FP64 instruction); the values are scaled
+  // once when the block is stored.  Done before this CTA's turn comes.
+  for (int i = tid; i < bs; i += kTrsvLThreads)
+    rd[i] = 1.0 / (g.diag_mode == 0 ? A[(size_t)(r0 + i) * lda + r0 + i] : g.dval);
+  __syncthreads();
   for (int e = tid; e < bs * bs; e += kTrsvLThreads) {
     const int hi = e / bs, lo = e - hi * bs;  // coalesced: lo runs along T's columns
     const int i = TRANS ? hi : lo, k = TRANS ? lo : hi;
-    if (fwd ? (i > k) : (i < k)) Ts[k * LD + i] = A[(size_t)(r0 + hi) * lda + r0 + lo];
+    if (fwd ? (i > k) : (i < k)) Ts[k * LD + i] = A[(size_t)(r0 + hi) * lda + r0 + lo] * rd[k];
   }
-  for (int i = tid; i < bs; i += kTrsvLThreads)
-    rd[i] = 1.0 / (g.diag_mode == 0 ? A[(size_t)(r0 + i) * lda + r0 + i] : g.dval);
 
   if constexpr (!TRANS) {
     const int tr = tid % BS, tc = tid / BS;
@@ -202,7 +207,6 @@ __global__ void __launch_bounds__(kTrsvLThreads) trsv_large_kernel(TrsvLArgs g) 
 #pragma unroll
         for (int kk = 0; kk < 32; ++kk) {
           if (kk < sw) {
-            if (lane == kk) v *= rd[sb + kk];
             const double xk = __shfl_sync(0xffffffffu, v, kk);
             if (lane > kk && lane < sw) v = fma(-Ts[(sb + kk) * LD + sb + lane], xk, v);
           }
@@ -211,27 +215,42 @@ __global__ void __launch_bounds__(kTrsvLThreads) trsv_large_kernel(TrsvLArgs g) 
 #pragma unroll
         for (int kk = 31; kk >= 0; --kk) {
           if (kk < sw) {
-            if (lane == kk) v *= rd[sb + kk];
             const double xk = __shfl_sync(0xffffffffu, v, kk);
             if (lane < kk) v = fma(-Ts[(sb + kk) * LD + sb + lane], xk, v);
           }
         }
       }
-      if (lane < sw) xs[sb + lane] = v;
+      if (lane < sw) xs[sb + lane] = v;  // unscaled
     }
     __syncthreads();
-    // the block's rows on the far side of the piece take its contribution
+    // the block's rows on the far side of the piece (at most 32) take its
+    // contribution: warp w sums terms 4w..4w+3 for row i0 + lane, then one
+    // thread per row adds the 8 partial sums (8 dependent FP64 steps on the
+    // chain instead of 32)
     const int i0 = fwd ? sb + sw : 0, i1 = fwd ? bs : sb;
-    for (int i = i0 + tid; i < i1; i += kTrsvLThreads) {
-      double acc = xs[i];
-#pragma unroll 8
-      for (int k = 0; k < sw; ++k) acc = fma(-Ts[(sb + k) * LD + i], xs[sb + k], acc);
-      xs[i] = acc;
+    if (i1 > i0) {
+      double* pp = &part[0][0];  // 8 warps x 32 rows (the tile sums are consumed)
+      double acc = 0.0;
+      if (i0 + lane < i1)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = 4 * warp + u;
+          if (k < sw) acc = fma(-Ts[(sb + k) * LD + i0 + lane], xs[sb + k], acc);
+        }
+      pp[warp * 32 + lane] = acc;
+      __syncthreads();
+      if (tid < i1 - i0) {
+        double y = xs[i0 + tid];
+#pragma unroll
+        for (int w = 0; w < kTrsvLThreads / 32; ++w) y += pp[w * 32 + tid];
+        xs[i0 + tid] = y;
+      }
     }
     __syncthreads();
   }
-  if (tid < bs) g.x[r0 + tid] = xs[tid];
-  __threadfence();
+  if (tid < bs) g.x[r0 + tid] = xs[tid] * rd[tid];
+  // the barrier orders the block's stores before thread 0's release, which is
+  // cumulative over them: a CTA that acquires the flag sees x (no fence needed)
   __syncthreads();
   if (tid == 0) trsvl_st_release(&g.sync[2 + kb], 1);
 }
