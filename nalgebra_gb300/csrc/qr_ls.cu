@@ -330,25 +330,29 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
       __syncthreads();
     }
     // ---- T (forward, columnwise): T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] V^T v_j ----
-    // G = V^T V (strict upper part) was formed by the panel steps; thread 0
-    // runs the small T recurrence in shared memory.
-    {
-      if (tid == 0) {
-        for (int j = 0; j < kQrNB; ++j)
-          for (int i = 0; i < kQrNB; ++i) s_t[kTOff + i * kQrNB + j] = 0.0;
-        for (int j = 0; j < jb; ++j) {
-          const double tj = s_t[kTauOff + j];
+    // G = V^T V (strict upper part) was formed by the panel steps; lanes
+    // 0..NB-1 of warp 0 run the small T recurrence in shared memory, lane i
+    // forming row i of each new column (a column costs j FP64 steps on the
+    // warp instead of j(j+1)/2 on one thread).
+    if (tid < kQrNB) {
+      const int i = tid;
+#pragma unroll
+      for (int j = 0; j < kQrNB; ++j) s_t[kTOff + i * kQrNB + j] = 0.0;
+      __syncwarp(0xffu);
+      for (int j = 0; j < jb; ++j) {
+        const double tj = s_t[kTauOff + j];
+        if (i < j) {
+          double acc = 0.0;
+          for (int l = i; l < j; ++l)
+            acc = fma(s_t[kTOff + i * kQrNB + l], s_t[kGSumOff + l * kQrNB - l * (l + 1) / 2 + (j - l - 1)], acc);
+          s_t[kTOff + i * kQrNB + j] = -tj * acc;
+        } else if (i == j) {
           s_t[kTOff + j * kQrNB + j] = tj;
-          for (int i = 0; i < j; ++i) {
-            double acc = 0.0;
-            for (int l = i; l < j; ++l)
-              acc = fma(s_t[kTOff + i * kQrNB + l], s_t[kGSumOff + l * kQrNB - l * (l + 1) / 2 + (j - l - 1)], acc);
-            s_t[kTOff + i * kQrNB + j] = -tj * acc;
-          }
         }
+        __syncwarp(0xffu);
       }
-      __syncthreads();
     }
+    __syncthreads();
     // ---- trailing columns and the right-hand side: c <- c - V T^T V^T c ----
     // four columns per warp at a time (each shared-memory axis value feeds
     // four FMAs), the columns left over one at a time
@@ -414,7 +418,12 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int r = lane + 32 * k;
-        if (r < i) yv[k] = fma(-xi, a[(size_t)i * m + r] * s_misc[2 + kQrMaxN + r], yv[k]);
+        if (r < i) {  // R[r][i] times the row sign d_r = +-1: a sign-bit flip, no FP64 multiply
+          const unsigned long long sm =
+              (unsigned long long)__double_as_longlong(s_misc[2 + kQrMaxN + r]) & 0x8000000000000000ull;
+          const double rri = __longlong_as_double(__double_as_longlong(a[(size_t)i * m + r]) ^ sm);
+          yv[k] = fma(-xi, rri, yv[k]);
+        }
       }
     }
 #pragma unroll
