@@ -20,10 +20,11 @@
 // "Collected matrix derivative results for forward and reverse mode AD";
 // Murray 2016, "Differentiation of the Cholesky decomposition".)
 //
-// Design: one CTA (256 threads) per matrix with the whole n x n matrix in
-// shared memory (column-major, odd leading dimension), so the factorization,
-// the in-place triangular inverse L -> L^-1 and the product
-// A^-1 = L^-T L^-1 run out of shared memory.  Trailing updates use a
+// Design: one CTA (256 threads) per matrix with the matrix's packed lower
+// triangle in shared memory (66 KB at n = 128 in FP64, so three CTAs share an
+// SM where the full square allowed one), so the factorization, the in-place
+// triangular inverse L -> L^-1 and the product A^-1 = L^-T L^-1 run out of
+// shared memory.  Trailing updates use a
 // pair-folded index over the lower triangle (column c paired with column
 // m-1-c fills an (m+1) x ceil(m/2) rectangle), so no lane idles on the
 // triangle's empty half.
@@ -57,13 +58,18 @@ __device__ __forceinline__ bool fold(int m, int k, int q, int* r, int* c) {
   return *r < m;
 }
 
+// Element (r, c), r >= c, of the lower triangle in shared memory sits at
+// S[cb[c] + r]: cb[c] = c * ld for a full column-major square, or
+// c * n - c (c + 1) / 2 for the packed triangle (column c's rows c..n-1 follow
+// column c-1's), which halves the backward kernel's shared memory.
+
 // Right-looking Cholesky of the n x n matrix in S (lower triangle).
 // Returns info (0 ok, j+1 first failing pivot) in *s_info.
 template <typename T>
-__device__ void chol_smem(int n, T* S, int ld, int* s_info, T* s_sc) {
+__device__ void chol_smem(int n, T* S, const int* cb, int* s_info, T* s_sc) {
   const int tid = threadIdx.x, nthr = blockDim.x;
   for (int j = 0; j < n; ++j) {
-    T* cj = S + (size_t)j * ld;
+    T* cj = S + cb[j];
     if (tid == 0) {
       const T d = cj[j];
       if (!(d <= T(0)) && d >= T(0)) {
@@ -88,7 +94,7 @@ __device__ void chol_smem(int n, T* S, int ld, int* s_info, T* s_sc) {
         if (fold(m, k, q, &r, &c)) {
           r += j + 1;
           c += j + 1;
-          S[(size_t)c * ld + r] = fma_t(-cj[r], cj[c], S[(size_t)c * ld + r]);
+          S[cb[c] + r] = fma_t(-cj[r], cj[c], S[cb[c] + r]);
         }
       }
     }
@@ -102,20 +108,20 @@ __device__ void chol_smem(int n, T* S, int ld, int* s_info, T* s_sc) {
 // warps share each column's dot products; fused multiply-adds; the
 // reciprocals of the diagonal (rdiag) are formed once beforehand.
 template <typename T>
-__device__ void trinv_smem(int n, T* S, int ld, T* tmp, const T* rdiag) {
+__device__ void trinv_smem(int n, T* S, const int* cb, T* tmp, const T* rdiag) {
   const int tid = threadIdx.x;
   const int ri = tid >> 1, h = tid & 1;
   for (int j = n - 1; j >= 0; --j) {
-    const T* cj = S + (size_t)j * ld;
+    const T* cj = S + cb[j];
     const T ajj = rdiag[j];
     const int i = j + 1 + ri;
     T acc = T(0);
     if (i < n)
-      for (int k = j + 1 + h; k <= i; k += 2) acc = fma_t(S[(size_t)k * ld + i], cj[k], acc);  // L^-1[i][k] L[k][j]
+      for (int k = j + 1 + h; k <= i; k += 2) acc = fma_t(S[cb[k] + i], cj[k], acc);  // L^-1[i][k] L[k][j]
     acc += __shfl_xor_sync(0xffffffffu, acc, 1);
     if (i < n && h == 0) tmp[i] = -ajj * acc;
     __syncthreads();
-    T* cw = S + (size_t)j * ld;
+    T* cw = S + cb[j];
     for (int r = j + 1 + tid; r < n; r += blockDim.x) cw[r] = tmp[r];
     if (tid == 0) cw[j] = ajj;
     __syncthreads();
@@ -127,21 +133,21 @@ __device__ void trinv_smem(int n, T* S, int ld, T* tmp, const T* rdiag) {
 // columns >= j of L^-1, so it can be overwritten once computed.  Two threads
 // per row, k split by parity.
 template <typename T>
-__device__ void inv_from_trinv_smem(int n, T* S, int ld, T* tmp) {
+__device__ void inv_from_trinv_smem(int n, T* S, const int* cb, T* tmp) {
   const int tid = threadIdx.x;
   const int ri = tid >> 1, h = tid & 1;
   for (int j = 0; j < n; ++j) {
-    const T* cj = S + (size_t)j * ld;
+    const T* cj = S + cb[j];
     const int i = j + ri;
     T acc = T(0);
     if (i < n) {
-      const T* ci = S + (size_t)i * ld;
+      const T* ci = S + cb[i];
       for (int k = i + h; k < n; k += 2) acc = fma_t(ci[k], cj[k], acc);  // Linv[k][i] Linv[k][j]
     }
     acc += __shfl_xor_sync(0xffffffffu, acc, 1);
     if (i < n && h == 0) tmp[i] = acc;
     __syncthreads();
-    T* cw = S + (size_t)j * ld;
+    T* cw = S + cb[j];
     for (int r = j + tid; r < n; r += blockDim.x) cw[r] = tmp[r];
     __syncthreads();
   }
@@ -157,36 +163,38 @@ __global__ void __launch_bounds__(kAdjThreads) adj_forward_kernel(int n, const T
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_info;
   __shared__ T s_sc[2];
-  const int ld = n | 1;
-  T* S = reinterpret_cast<T*>(smem_raw);
-  T* y = S + (size_t)ld * n;
+  __shared__ int cb[kAdjMaxN];
+  T* S = reinterpret_cast<T*>(smem_raw);  // the packed lower triangle
+  T* y = S + (size_t)n * (n + 1) / 2;
   const int tid = threadIdx.x;
+  for (int c = tid; c < n; c += blockDim.x) cb[c] = c * n - c * (c + 1) / 2;
+  __syncthreads();  // every column base is set before any thread stores through it
   for (int s = blockIdx.x; s < batch; s += gridDim.x) {
     const T* a = A + (size_t)s * strideA;
     for (int e = tid; e < n * n; e += blockDim.x) {
       const int c = e / n, r = e - c * n;
-      if (r >= c) S[(size_t)c * ld + r] = a[e];
+      if (r >= c) S[cb[c] + r] = a[e];
     }
     for (int i = tid; i < n; i += blockDim.x) y[i] = B[(size_t)s * n + i];
     if (tid == 0) s_info = 0;
     __syncthreads();
-    chol_smem<T>(n, S, ld, &s_info, s_sc);
+    chol_smem<T>(n, S, cb, &s_info, s_sc);
     const int inf = s_info;
     if (inf == 0) {
       // L y = b then L^T x = y; one warp (n <= 128: four rows per lane)
       if (tid < 32) {
         for (int i = 0; i < n; ++i) {
-          if (tid == 0) y[i] = y[i] / S[(size_t)i * ld + i];
+          if (tid == 0) y[i] = y[i] / S[cb[i] + i];
           __syncwarp();
           const T yi = y[i];
-          for (int r = i + 1 + tid; r < n; r += 32) y[r] = fma_t(-yi, S[(size_t)i * ld + r], y[r]);
+          for (int r = i + 1 + tid; r < n; r += 32) y[r] = fma_t(-yi, S[cb[i] + r], y[r]);
           __syncwarp();
         }
         for (int i = n - 1; i >= 0; --i) {
           T sacc = T(0);
-          for (int r = i + 1 + tid; r < n; r += 32) sacc = fma_t(S[(size_t)i * ld + r], y[r], sacc);
+          for (int r = i + 1 + tid; r < n; r += 32) sacc = fma_t(S[cb[i] + r], y[r], sacc);
           sacc = warp_sum(sacc);
-          if (tid == 0) y[i] = (y[i] - sacc) / S[(size_t)i * ld + i];
+          if (tid == 0) y[i] = (y[i] - sacc) / S[cb[i] + i];
           __syncwarp();
         }
       }
@@ -195,7 +203,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_forward_kernel(int n, const T
       if (tid == 0) {
         T sum = T(0);
         for (int i = 0; i < n; ++i) {
-          const T d = S[(size_t)i * ld + i];
+          const T d = S[cb[i] + i];
           sum += log(d * d);
         }
         logdet[s] = sum;
@@ -203,7 +211,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_forward_kernel(int n, const T
       if (Lout)
         for (int e = tid; e < n * n; e += blockDim.x) {
           const int c = e / n, r = e - c * n;
-          Lout[(size_t)s * strideA + e] = (r >= c) ? S[(size_t)c * ld + r] : T(0);
+          Lout[(size_t)s * strideA + e] = (r >= c) ? S[cb[c] + r] : T(0);
         }
     }
     if (tid == 0 && info) info[s] = inf;
@@ -223,19 +231,21 @@ __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_info;
   __shared__ T s_sc[2];
-  const int ld = n | 1;
-  T* S = reinterpret_cast<T*>(smem_raw);
-  T* tmp = S + (size_t)ld * n;
+  __shared__ int cb[kAdjMaxN];
+  T* S = reinterpret_cast<T*>(smem_raw);  // the packed lower triangle, n (n + 1) / 2 entries
+  T* tmp = S + (size_t)n * (n + 1) / 2;
   T* v = tmp + n;
   T* xs = v + n;
   T* ws = xs + n;
   T* rdiag = ws + n;
   const int tid = threadIdx.x;
+  for (int c = tid; c < n; c += blockDim.x) cb[c] = c * n - c * (c + 1) / 2;
+  __syncthreads();
   for (int s = blockIdx.x; s < batch; s += gridDim.x) {
     const T* a = AL + (size_t)s * strideA;
     for (int e = tid; e < n * n; e += blockDim.x) {
       const int c = e / n, r = e - c * n;
-      if (r >= c) S[(size_t)c * ld + r] = a[e];
+      if (r >= c) S[cb[c] + r] = a[e];
     }
     for (int i = tid; i < n; i += blockDim.x) {
       xs[i] = X[(size_t)s * n + i];
@@ -243,18 +253,18 @@ __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const 
     }
     if (tid == 0) s_info = 0;
     __syncthreads();
-    if (recompute) chol_smem<T>(n, S, ld, &s_info, s_sc);  // refactor instead of storing L
+    if (recompute) chol_smem<T>(n, S, cb, &s_info, s_sc);  // refactor instead of storing L
     const int inf = s_info;
     if (inf == 0) {
-      for (int i = tid; i < n; i += blockDim.x) rdiag[i] = T(1) / S[(size_t)i * ld + i];
+      for (int i = tid; i < n; i += blockDim.x) rdiag[i] = T(1) / S[cb[i] + i];
       __syncthreads();
-      trinv_smem<T>(n, S, ld, tmp, rdiag);
-      inv_from_trinv_smem<T>(n, S, ld, tmp);
+      trinv_smem<T>(n, S, cb, tmp, rdiag);
+      inv_from_trinv_smem<T>(n, S, cb, tmp);
       // v = A^-1 w from the lower triangle of the symmetric A^-1
       for (int i = tid; i < n; i += blockDim.x) {
         T acc = T(0);
-        for (int k = 0; k <= i; ++k) acc = fma_t(S[(size_t)k * ld + i], ws[k], acc);
-        for (int k = i + 1; k < n; ++k) acc = fma_t(S[(size_t)i * ld + k], ws[k], acc);
+        for (int k = 0; k <= i; ++k) acc = fma_t(S[cb[k] + i], ws[k], acc);
+        for (int k = i + 1; k < n; ++k) acc = fma_t(S[cb[i] + k], ws[k], acc);
         v[i] = acc;
       }
       __syncthreads();
@@ -265,8 +275,8 @@ __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const 
       for (int e = tid; e < n * n; e += blockDim.x) {
         const int c = e / n, r = e - c * n;
         T val = T(0);
-        if (r == c) val = fma_t(-v[r], xs[r], gl * S[(size_t)c * ld + r]);
-        else if (r > c) val = fma_t(-v[r], xs[c], fma_t(-v[c], xs[r], gl2 * S[(size_t)c * ld + r]));
+        if (r == c) val = fma_t(-v[r], xs[r], gl * S[cb[c] + r]);
+        else if (r > c) val = fma_t(-v[r], xs[c], fma_t(-v[c], xs[r], gl2 * S[cb[c] + r]));
         g[e] = val;
       }
     }
@@ -283,7 +293,7 @@ int adj_launch_forward(int n, const T* A, int64_t strideA, const T* B, T* X, T* 
   if (batch == 0) return NACU_SUCCESS;
   if (!A || !B || !X || !logdet) return record_arg_error(-2, "posv_logdet_forward: null A, B, X or logdet");
   if (strideA < (int64_t)n * n) return record_arg_error(-3, "posv_logdet_forward: strideA < n*n");
-  const size_t smem = ((size_t)(n | 1) * n + n) * sizeof(T);
+  const size_t smem = ((size_t)n * (n + 1) / 2 + n) * sizeof(T);
   cudaError_t e = ensure_dynamic_smem(adj_forward_kernel<T>, smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   adj_forward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, A, strideA, B, X, Lout, logdet, info, batch);
@@ -298,7 +308,7 @@ int adj_launch_backward(int n, const T* AL, int64_t strideA, int recompute, cons
   if (batch == 0) return NACU_SUCCESS;
   if (!AL || !X || !W || !dA || !db) return record_arg_error(-2, "posv_logdet_backward: null argument");
   if (strideA < (int64_t)n * n) return record_arg_error(-3, "posv_logdet_backward: strideA < n*n");
-  const size_t smem = ((size_t)(n | 1) * n + 5 * (size_t)n) * sizeof(T);
+  const size_t smem = ((size_t)n * (n + 1) / 2 + 5 * (size_t)n) * sizeof(T);
   cudaError_t e = ensure_dynamic_smem(adj_backward_kernel<T>, smem);
   if (e != cudaSuccess) return record_cuda_error(e, name);
   adj_backward_kernel<T><<<batch, kAdjThreads, smem, stream>>>(n, AL, strideA, recompute, X, W, G, dA, db, info,
