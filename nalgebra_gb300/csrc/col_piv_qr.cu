@@ -231,12 +231,22 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
           const bool nz = !is_zero_bits(factor);
           double rnorm = signed_norm;
           if (nz) {
-            const double sf = __dsqrt_rn(factor);
-            for (int k = lane; k < L; k += 32) x[k] = __ddiv_rn(x[k], sf);  // unscale_mut
-            __syncwarp();
-            const double n2 = __dsqrt_rn(cq_add<EXACT>(0.0, cq_dot<EXACT>(L, x, x, lane)));  // normalize_mut
-            __syncwarp();
-            for (int k = lane; k < L; k += 32) x[k] = __ddiv_rn(x[k], n2);
+            if constexpr (EXACT) {
+              const double sf = __dsqrt_rn(factor);
+              for (int k = lane; k < L; k += 32) x[k] = __ddiv_rn(x[k], sf);  // unscale_mut
+              __syncwarp();
+              const double n2 = __dsqrt_rn(cq_add<EXACT>(0.0, cq_dot<EXACT>(L, x, x, lane)));  // normalize_mut
+              __syncwarp();
+              for (int k = lane; k < L; k += 32) x[k] = __ddiv_rn(x[k], n2);
+            } else {
+              // factor = 2 (sq + |x0| nrm) is |x'|^2 for the updated axis x',
+              // so one scale by rsqrt(factor) makes it a unit vector: the
+              // second normalisation and the two divisions per element (each
+              // a chain of FP64 instructions on this warp, the step's
+              // critical path) only corrected rounding
+              const double rs = rsqrt(factor);
+              for (int k = lane; k < L; k += 32) x[k] *= rs;
+            }
             rnorm = -signed_norm;
           }
           if (lane == 0) {
