@@ -174,10 +174,11 @@ __global__ void __launch_bounds__(kTrsvLThreads) trsv_large_kernel(TrsvLArgs g) 
       for (int u = 0; u < CW; ++u) acc[u] = fma(-a[u], xv, acc[u]);
       __syncthreads();
     }
-    // reduce the 16 sums of each thread over the tile's 64 columns: within
-    // each warp a butterfly reduce-scatter leaves the sum of row k = lane & 15
-    // in lanes k and k + 16; the two warps of a row quarter meet in part[]
-    const int lane = tid & 31, half = (tid >> 5) & 1;
+    // reduce the CW sums of each thread over the tile's BS columns: within
+    // each warp a butterfly reduce-scatter leaves the sum of row k = lane % CW
+    // in the lanes congruent to k; the BS / 32 warps of a row part meet in part[]
+    constexpr int WP = BS / 32;
+    const int lane = tid & 31, half = (tid >> 5) % WP;
 #pragma unroll
     for (int h = CW / 2; h >= 1; h >>= 1) {
       const bool up = (lane & h) != 0;
@@ -188,10 +189,16 @@ __global__ void __launch_bounds__(kTrsvLThreads) trsv_large_kernel(TrsvLArgs g) 
         acc[u] = keep + __shfl_xor_sync(0xffffffffu, give, h);
       }
     }
-    acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], 16);
+#pragma unroll
+    for (int off = CW; off < 32; off <<= 1) acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], off);
     if (lane < CW) part[half][trp * CW + lane] = acc[0];
     __syncthreads();
-    if (tid < bs) xs[tid] = g.x[r0 + tid] + (part[0][tid] + part[1][tid]);
+    if (tid < bs) {
+      double y = part[0][tid];
+#pragma unroll
+      for (int h = 1; h < WP; ++h) y += part[h][tid];
+      xs[tid] = g.x[r0 + tid] + y;
+    }
   }
   __syncthreads();
   // the diagonal block, 32 rows at a time: warp 0 solves the 32 x 32 piece
