@@ -106,49 +106,100 @@ __device__ void chol_smem(int n, T* S, const int* cb, int* s_info, T* s_sc) {
 // L^-1[i][j] = -(1/L_jj) * sum_{k=j+1..i} L^-1[i][k] L[k][j]  (i > j).
 // Two threads per row i (k split by parity, combined by a shuffle), so all
 // warps share each column's dot products; fused multiply-adds; the
-// reciprocals of the diagonal (rdiag) are formed once beforehand.
+// reciprocals of the diagonal (rdiag) are formed once beforehand.  Columns go
+// two at a time (j and j-1 share each L^-1[i][k] load and one pair of
+// barriers): with s0, s1 the sums over k > j,
+//   L^-1[i][j] = -s0 / L_jj,  L^-1[i][j-1] = -(s1 + L^-1[i][j] L[j][j-1]) / L_{j-1,j-1}.
+// tmp holds 2n values.
 template <typename T>
 __device__ void trinv_smem(int n, T* S, const int* cb, T* tmp, const T* rdiag) {
   const int tid = threadIdx.x;
   const int ri = tid >> 1, h = tid & 1;
-  for (int j = n - 1; j >= 0; --j) {
+  int j = n - 1;
+  for (; j >= 1; j -= 2) {
     const T* cj = S + cb[j];
-    const T ajj = rdiag[j];
+    const T* cj1 = S + cb[j - 1];
+    const T ajj = rdiag[j], aj1 = rdiag[j - 1];
     const int i = j + 1 + ri;
-    T acc = T(0);
+    T s0 = T(0), s1 = T(0);
     if (i < n)
-      for (int k = j + 1 + h; k <= i; k += 2) acc = fma_t(S[cb[k] + i], cj[k], acc);  // L^-1[i][k] L[k][j]
-    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-    if (i < n && h == 0) tmp[i] = -ajj * acc;
+      for (int k = j + 1 + h; k <= i; k += 2) {
+        const T li = S[cb[k] + i];  // L^-1[i][k]
+        s0 = fma_t(li, cj[k], s0);
+        s1 = fma_t(li, cj1[k], s1);
+      }
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+    if (i < n && h == 0) {
+      const T x0 = -ajj * s0;
+      tmp[i] = x0;
+      tmp[n + i] = -aj1 * fma_t(x0, cj1[j], s1);
+    }
     __syncthreads();
     T* cw = S + cb[j];
-    for (int r = j + 1 + tid; r < n; r += blockDim.x) cw[r] = tmp[r];
-    if (tid == 0) cw[j] = ajj;
+    T* cw1 = S + cb[j - 1];
+    for (int r = j + 1 + tid; r < n; r += blockDim.x) {
+      cw[r] = tmp[r];
+      cw1[r] = tmp[n + r];
+    }
+    if (tid == 0) {
+      cw1[j] = -aj1 * (ajj * cw1[j]);  // L^-1[j][j-1] = -L[j][j-1] / (L_jj L_{j-1,j-1})
+      cw[j] = ajj;
+      cw1[j - 1] = aj1;
+    }
+    __syncthreads();
+  }
+  if (j == 0) {  // odd n: the first column on its own
+    const T* c0 = S + cb[0];
+    const T a00 = rdiag[0];
+    const int i = 1 + ri;
+    T acc = T(0);
+    if (i < n)
+      for (int k = 1 + h; k <= i; k += 2) acc = fma_t(S[cb[k] + i], c0[k], acc);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    if (i < n && h == 0) tmp[i] = -a00 * acc;
+    __syncthreads();
+    T* cw = S + cb[0];
+    for (int r = 1 + tid; r < n; r += blockDim.x) cw[r] = tmp[r];
+    if (tid == 0) cw[0] = a00;
     __syncthreads();
   }
 }
 
-// In place L^-1 -> A^-1 = L^-T L^-1 (lower triangle), column by column:
-// (A^-1)_ij = sum_{k >= i} Linv_ki Linv_kj  (i >= j); column j needs only
-// columns >= j of L^-1, so it can be overwritten once computed.  Two threads
-// per row, k split by parity.
+// In place L^-1 -> A^-1 = L^-T L^-1 (lower triangle):
+// (A^-1)_ij = sum_{k >= i} Linv_ki Linv_kj  (i >= j).  Given L^-1 the columns
+// are independent, and column j needs only columns >= j, so four columns are
+// formed per pair of barriers (each Linv_ki load feeds four FMAs) into tmp and
+// written back over their L^-1 columns.  Two threads per row, k split by
+// parity.  tmp holds 4n values.
 template <typename T>
 __device__ void inv_from_trinv_smem(int n, T* S, const int* cb, T* tmp) {
   const int tid = threadIdx.x;
   const int ri = tid >> 1, h = tid & 1;
-  for (int j = 0; j < n; ++j) {
-    const T* cj = S + cb[j];
+  for (int j = 0; j < n; j += 4) {
+    const int jw = min(4, n - j);
     const int i = j + ri;
-    T acc = T(0);
+    T acc[4] = {T(0), T(0), T(0), T(0)};
     if (i < n) {
       const T* ci = S + cb[i];
-      for (int k = i + h; k < n; k += 2) acc = fma_t(ci[k], cj[k], acc);  // Linv[k][i] Linv[k][j]
+      const T* cju[4] = {S + cb[j], S + cb[min(j + 1, n - 1)], S + cb[min(j + 2, n - 1)], S + cb[min(j + 3, n - 1)]};
+      for (int k = i + h; k < n; k += 2) {
+        const T lki = ci[k];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (u < jw && i >= j + u) acc[u] = fma_t(lki, cju[u][k], acc[u]);  // Linv[k][j+u], k >= i >= j+u
+      }
     }
-    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-    if (i < n && h == 0) tmp[i] = acc;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], 1);
+      if (i < n && h == 0 && u < jw && i >= j + u) tmp[u * n + i] = acc[u];
+    }
     __syncthreads();
-    T* cw = S + cb[j];
-    for (int r = j + tid; r < n; r += blockDim.x) cw[r] = tmp[r];
+    for (int u = 0; u < jw; ++u) {
+      T* cw = S + cb[j + u];
+      for (int r = j + u + tid; r < n; r += blockDim.x) cw[r] = tmp[u * n + r];
+    }
     __syncthreads();
   }
 }
@@ -247,10 +298,6 @@ __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const 
       const int c = e / n, r = e - c * n;
       if (r >= c) S[cb[c] + r] = a[e];
     }
-    for (int i = tid; i < n; i += blockDim.x) {
-      xs[i] = X[(size_t)s * n + i];
-      ws[i] = Wt[(size_t)s * n + i];
-    }
     if (tid == 0) s_info = 0;
     __syncthreads();
     if (recompute) chol_smem<T>(n, S, cb, &s_info, s_sc);  // refactor instead of storing L
@@ -258,8 +305,13 @@ __global__ void __launch_bounds__(kAdjThreads) adj_backward_kernel(int n, const 
     if (inf == 0) {
       for (int i = tid; i < n; i += blockDim.x) rdiag[i] = T(1) / S[cb[i] + i];
       __syncthreads();
-      trinv_smem<T>(n, S, cb, tmp, rdiag);
-      inv_from_trinv_smem<T>(n, S, cb, tmp);
+      trinv_smem<T>(n, S, cb, tmp, rdiag);     // tmp, v: 2n of scratch
+      inv_from_trinv_smem<T>(n, S, cb, tmp);   // tmp, v, xs, ws: 4n of scratch
+      for (int i = tid; i < n; i += blockDim.x) {
+        xs[i] = X[(size_t)s * n + i];
+        ws[i] = Wt[(size_t)s * n + i];
+      }
+      __syncthreads();
       // v = A^-1 w from the lower triangle of the symmetric A^-1
       for (int i = tid; i < n; i += blockDim.x) {
         T acc = T(0);
