@@ -91,7 +91,7 @@ __device__ void group_rank_one(int m, double* L, int64_t ld, double* x, double* 
           const double sx = sigma * xj * xj;
           const double new_diag = sqrt(fma(sx, ib, diag * diag));
           const double beta1 = fma(sx, r2, beta);
-          const double ib1 = 1.0 / beta1;
+          const double ib1 = rcp_nr(beta1);  // on the column chain: the short Newton form
           col[j] = new_diag;
           a1 = -xj * r;
           a2 = new_diag * sigma * xj * r2 * ib1;

@@ -159,6 +159,24 @@ __device__ __forceinline__ float f64_to_f32_rn(double x) {
   return (float)x;
 }
 
+// 1/d for the FMA forms: the hardware's approximate reciprocal
+// (rcp.approx.ftz.f64) refined by two Newton-Raphson steps for 1/d,
+// e = 1 - d r, r <- r + r e (quadratic convergence), four FP64 instructions
+// after the approximation where an IEEE division takes a longer dependent
+// chain.  Within a few ulps of 1/d (not always correctly rounded; the EXACT
+// forms divide).  For |d| outside [2^-1000, 2^1000], zero, infinities and NaN
+// it takes the division.
+__device__ __forceinline__ double rcp_nr(double d) {
+  const long long b = __double_as_longlong(d) & 0x7fffffffffffffffll;
+  if (b < 0x0170000000000000ll || b >= 0x7e70000000000000ll) return 1.0 / d;
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
 // A lower bound of |x| in binary32 for norm sums, from the high word alone:
 // the fraction truncated to 20 bits, magnitudes below 2^-127 counted as 0 and
 // above the binary32 range clamped just under FLT_MAX (a smaller ||A|| only

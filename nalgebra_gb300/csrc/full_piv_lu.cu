@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(kFpThreads, 5) fullpiv_kernel(int n, int nrhs,
         if (warp == 0) {
           // columns i and cp at once, from registers: the column swap, the
           // row swap of rows i and rp, and the multipliers of column i
-          const double inv_diag = 1.0 / diag;  // gauss_step's inv_diag
+          const double inv_diag = EXACT ? 1.0 / diag : rcp_nr(diag);  // gauss_step's inv_diag
           double* ci = sa + (size_t)i * ld;
           double* cq = sa + (size_t)cp * ld;
           const double a_ii = ci[i], a_rpi = ci[rp], a_icp = cq[i];

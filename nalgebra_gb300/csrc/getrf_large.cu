@@ -167,6 +167,11 @@ __device__ void panel_compose_swaps(const PanelArgs<T>& g, int nb, int tid) {
 // exchange; row c and the pivot row are swapped by their owners (nalgebra
 // swaps whole rows, lu.rs:111-116; the columns outside the panel are swapped
 // afterwards by lu_swap_kernel).
+// The panel's pivot reciprocal, on its serial per-column path: the Newton
+// form in FP64 (rcp_nr), a division in FP32.
+__device__ __forceinline__ double pivot_rcp(double d) { return rcp_nr(d); }
+__device__ __forceinline__ float pivot_rcp(float d) { return 1.0f / d; }
+
 template <typename T>
 __global__ void __launch_bounds__(kPanelThreads) lu_panel_grid_kernel(PanelArgs<T> g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -273,7 +278,7 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_grid_kernel(PanelArgs<
         s_prow[t] = win_row[t];
         if (own_p && piv != c) s_drow[t] = c_row[t];
       }
-      if (tid == 0) s_inv = T(1) / win_row[j];
+      if (tid == 0) s_inv = pivot_rcp(win_row[j]);
     }
     __syncthreads();
     if (piv != c) {
@@ -450,7 +455,7 @@ __global__ void __launch_bounds__(kPanelThreads) lu_panel_cluster_kernel(PanelAr
           g.ipiv[c] = zero ? c : bi;
           if (zero) atomicMin(g.info, c + 1);
         }
-        if (!zero) s_inv = T(1) / cpub_row<T>(cpub, nb, par, bw)[j];  // column j: complete in the copy
+        if (!zero) s_inv = pivot_rcp(cpub_row<T>(cpub, nb, par, bw)[j]);  // column j: complete in the copy
       }
     }
     __syncthreads();

@@ -34,7 +34,7 @@ constexpr int kLuThreads = 256;
 // [0] = 1/pivot, [n+1] = the pivot, [n+2] = the old diagonal a[c][c].  Each
 // lane scans the rows it updated itself (r = c + lane + 32k), so the scan
 // needs no barrier after that update.
-template <typename T>
+template <typename T, bool EXACT>
 __device__ __forceinline__ void lu_find_pivot(int n, int c, const T* colc, int* s_piv, T* s_rcp, int lane) {
   uint64_t key = 0;
   int idx = 0x7fffffff;
@@ -51,7 +51,10 @@ __device__ __forceinline__ void lu_find_pivot(int n, int c, const T* colc, int* 
     const T d = colc[idx];
     const bool zero = is_zero_bits(d);
     s_piv[c] = zero ? c : idx;
-    s_rcp[0] = zero ? T(0) : T(1) / d;  // one division per step, not per thread
+    // one reciprocal per step, not per thread; it sits on warp 0's look-ahead
+    // chain, so the FMA form of the FP64 kernel takes the short Newton form
+    if constexpr (EXACT || sizeof(T) != 8) s_rcp[0] = zero ? T(0) : T(1) / d;
+    else s_rcp[0] = zero ? T(0) : (T)rcp_nr((double)d);
     s_rcp[n + 1] = d;
     s_rcp[n + 2] = colc[c];
   }
@@ -70,7 +73,7 @@ __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_inf
     // next step (look-ahead), the other warps update columns i+2.. (the
     // right-hand sides included).  Every element still receives nalgebra's
     // operations in nalgebra's order.
-    if (warp == 0 && n > 0) lu_find_pivot<T>(n, 0, sa, s_piv, s_rcp, lane);
+    if (warp == 0 && n > 0) lu_find_pivot<T, EXACT>(n, 0, sa, s_piv, s_rcp, lane);
     __syncthreads();
     for (int i = 0; i < n; ++i) {
       T* coli = sa + (size_t)i * ld;
@@ -134,7 +137,7 @@ __device__ void lu_system(int n, int nrhs, int ld, T* sa, int* s_piv, int* s_inf
             }
           }
         }
-        if (warp == 0) lu_find_pivot<T>(n, i + 1, coln, s_piv, s_rcp, lane);
+        if (warp == 0) lu_find_pivot<T, EXACT>(n, i + 1, coln, s_piv, s_rcp, lane);
       }
       __syncthreads();
     }
