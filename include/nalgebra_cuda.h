@@ -462,6 +462,12 @@ int nacu_test_dgetrs_flag_timeout(int n, const double* LU, int64_t lda, const in
                                   int32_t* info, int skip_block, int poll_limit, void* workspace,
                                   size_t workspace_bytes, nacu_stream_t stream);
 
+/* Test hook, no counterpart in nalgebra: out[i] = the reciprocal the FMA
+ * forms use on their serial pivot paths (rcp.approx.ftz.f64 refined by two
+ * Newton-Raphson steps; division outside |d| in [2^-1000, 2^1000]) for
+ * d[0..n) in device memory, so a test can hold it to IEEE 1/d. */
+int nacu_test_rcp(int n, const double* d, double* out, nacu_stream_t stream);
+
 /* Workspace bytes of nacu_dgesv_mixed_ir (FP32 copy of A, split-GEMM slices,
  * vectors, and an FP64 copy of A for the fallback). */
 size_t nacu_gesv_mixed_workspace_bytes(int n);

@@ -157,6 +157,7 @@ extern "C" {
     pub fn nacu_ragged_get_tuning(table: *mut i32, nbuckets: c_int) -> c_int;
     pub fn nacu_probe_fp64_peak(flops: *mut f64) -> c_int;
     // test hook: the triangular solve's bounded flag wait made to run out
+    pub fn nacu_test_rcp(n: c_int, d: *const f64, out: *mut f64, s: Stream) -> c_int;
     pub fn nacu_test_dgetrs_flag_timeout(n: c_int, lu: *const f64, lda: i64, ipiv: *const i32, b: *mut f64,
                                          info: *mut i32, skip_block: c_int, poll_limit: c_int, ws: *mut c_void,
                                          ws_bytes: usize, s: Stream) -> c_int;

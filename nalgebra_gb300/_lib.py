@@ -72,6 +72,7 @@ SIGNATURES = {
     "nacu_dgetrf": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _sz, _vp]),
     "nacu_dgetrs": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _vp, _sz, _vp]),
     "nacu_test_dgetrs_flag_timeout": (_i, [_i, _vp, _i64, _vp, _vp, _vp, _i, _i, _vp, _sz, _vp]),
+    "nacu_test_rcp": (_i, [_i, _vp, _vp, _vp]),
     "nacu_ragged_tuning_layout": (_i, [_vp, _vp, _vp]),
     "nacu_ragged_set_tuning": (_i, [_vp, _i]),
     "nacu_ragged_get_tuning": (_i, [_vp, _i]),

@@ -1,4 +1,5 @@
 // Library-level entry points: version, error reporting, the FP64 roofline probe.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
@@ -43,12 +44,26 @@ __global__ void __launch_bounds__(256) fp64_probe_kernel(int iters, double s) {
   if (r == -12345.678) g_probe_sink = r;
 }
 
+__global__ void rcp_test_kernel(int n, const double* __restrict__ d, double* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = rcp_nr(d[i]);
+}
+
 }  // namespace
 }  // namespace nacu
 
 extern "C" {
 
 const char* nacu_version(void) { return "0.1.0"; }
+
+int nacu_test_rcp(int n, const double* d, double* out, nacu_stream_t stream) {
+  using namespace nacu;
+  if (n < 0) return record_arg_error(-1, "test_rcp: n < 0");
+  if (n == 0) return NACU_SUCCESS;
+  if (!d || !out) return record_arg_error(-2, "test_rcp: null pointer");
+  const int blocks = std::min((n + 255) / 256, sm_count() * 8);
+  rcp_test_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(n, d, out);
+  return check_launch("nacu_test_rcp");
+}
 
 const char* nacu_last_error(void) { return nacu::g_last_error; }
 
