@@ -219,12 +219,28 @@ __global__ void __launch_bounds__(kCqThreads) colpivqr_kernel(int n, int nrhs, d
           __syncwarp();
           // reflection_axis_mut on rows i.. of column i
           double* x = sa + (size_t)i * ld + i;
-          const double sq = cq_add<EXACT>(0.0, cq_dot<EXACT>(L, x, x, lane));
-          const double nrm = __dsqrt_rn(sq);
-          double modulus, sign;
-          cq_to_exp(x[0], modulus, sign);
-          const double signed_norm = cq_mul<EXACT>(sign, nrm);
-          const double factor = cq_mul<EXACT>(cq_add<EXACT>(sq, cq_mul<EXACT>(modulus, nrm)), 2.0);
+          double sq, nrm, signed_norm, factor;
+          if constexpr (EXACT) {
+            sq = cq_add<EXACT>(0.0, cq_dot<EXACT>(L, x, x, lane));
+            nrm = __dsqrt_rn(sq);
+            double modulus, sign;
+            cq_to_exp(x[0], modulus, sign);
+            signed_norm = cq_mul<EXACT>(sign, nrm);
+            factor = cq_mul<EXACT>(cq_add<EXACT>(sq, cq_mul<EXACT>(modulus, nrm)), 2.0);
+          } else {
+            // the same values with the sign logic on the bits (x0 >= 0 holds
+            // for +-0 and fails for NaN, as to_exp's test) and one FMA: on
+            // this warp every FP64 instruction is on the step's critical path
+            sq = cq_dot<EXACT>(L, x, x, lane);
+            nrm = __dsqrt_rn(sq);
+            const long long xb = __double_as_longlong(x[0]);
+            const long long mag = xb & 0x7fffffffffffffffll;
+            const bool ge0 = mag == 0 || (xb >= 0 && mag <= 0x7ff0000000000000ll);
+            const long long flip = ge0 ? 0ll : (long long)0x8000000000000000ull;
+            const double modulus = __longlong_as_double(xb ^ flip);
+            signed_norm = __longlong_as_double(__double_as_longlong(nrm) ^ flip);
+            factor = fma(modulus, nrm, sq) * 2.0;
+          }
           __syncwarp();
           if (lane == 0) x[0] = cq_add<EXACT>(x[0], signed_norm);
           __syncwarp();
