@@ -385,7 +385,7 @@ int nacu_sposv_logdet_backward(int n, const float* AL, int64_t strideA, int reco
 /* Bytes of device scratch nacu_dgels_batched needs (the work-queue head). */
 size_t nacu_qr_workspace_bytes(int count);
 
-/* Householder QR of `count` tall matrices with n <= 64 columns and
+/* Householder QR of `count` tall matrices with n <= 128 columns and
  * ms[s] >= n rows (ms[s] <= m_max <= 2048), A + a_offsets[s] (lda = ms[s]),
  * factored in place into nalgebra's QR layout: unit reflection axes on and
  * below the diagonal, R strictly above it, and diag[s*n + i] = the signed

@@ -234,7 +234,7 @@ impl DeviceMatrix {
 
     /// `Matrix::qr` (src/linalg/decomposition.rs:56-62).  Square n <= 128:
     /// `QR::new` in place (the batched kernel), for `solve` / `try_inverse`.
-    /// Tall m x n with m > n, n <= 64: kept for `solve_least_squares`.
+    /// Tall m x n with m > n, n <= 128: kept for `solve_least_squares`.
     pub fn qr(mut self) -> DeviceQR {
         let n = self.ncols;
         if self.nrows == n {
@@ -248,7 +248,7 @@ impl DeviceMatrix {
             let invertible = info.to_vec()[0] == 0;
             return DeviceQR { a: self, diag: Some(diag), invertible };
         }
-        assert!(self.nrows > n && n <= 64, "nalgebra-cuda: QR of m x n, m >= n, n <= 64");
+        assert!(self.nrows > n && n <= 128, "nalgebra-cuda: QR of m x n, m >= n, n <= 128");
         DeviceQR { a: self, diag: None, invertible: false }
     }
 
@@ -416,7 +416,7 @@ impl DeviceCholesky {
 }
 
 /// Householder QR.  Square (n <= 128): nalgebra's `QR` (src/linalg/qr.rs),
-/// factored in place.  Tall (m > n, n <= 64): the least-squares solve of
+/// factored in place.  Tall (m > n, n <= 128): the least-squares solve of
 /// nalgebra-lapack's `QrDecomposition::solve` (src/qr/abstraction.rs:46-77).
 pub struct DeviceQR {
     a: DeviceMatrix,

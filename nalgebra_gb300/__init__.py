@@ -978,7 +978,7 @@ class CholeskyBatch:
 
 
 class QRBatch:
-    """Batched Householder QR of tall matrices (equal column count n <= 64,
+    """Batched Householder QR of tall matrices (equal column count n <= 128,
     ragged row counts m >= n, m <= 2048), nalgebra's stored layout and sign
     convention (src/linalg/qr.rs:55-76).  Lazy: ``solve`` runs factor + Q^T b +
     least squares in one launch."""

@@ -431,6 +431,11 @@ int colpivqr_launch(int n, int nrhs, double* A, int64_t strideA, double* diag, i
 }
 
 }  // namespace
+
+// qr_ls.cu: the compact-WY Householder kernel on a uniform batch
+int qr_uniform_launch(int n, int count, double* A, int64_t strideA, double* diag, double* B, int64_t strideB,
+                      int32_t* info, cudaStream_t s, const char* name);
+
 }  // namespace nacu
 
 using namespace nacu;
@@ -477,6 +482,12 @@ int nacu_dqr_batched(int n, int nrhs, double* A, int64_t strideA, double* diag, 
   if (!A || !diag || (nrhs > 0 && !B)) return record_arg_error(-3, "QR batched: null pointer");
   if (strideA < (int64_t)n * n) return record_arg_error(-4, "QR batched: strideA < n*n");
   if (nrhs > 0 && strideB < (int64_t)n * nrhs) return record_arg_error(-7, "QR batched: strideB < n*nrhs");
+  // the FMA form with at most one right-hand side runs on the compact-WY
+  // Householder kernel of the least-squares path (same stored layout and
+  // signs); EXACT and more right-hand sides keep this kernel's steps
+  if (!(flags & NACU_FLAG_EXACT) && nrhs <= 1)
+    return qr_uniform_launch(n, batch, A, strideA, diag, nrhs == 1 ? B : nullptr, strideB, info,
+                             (cudaStream_t)stream, name);
   return colpivqr_launch(n, nrhs, A, strideA, diag, nullptr, B, strideB, info, batch, flags, nrhs > 0 ? 1 : 0,
                          (cudaStream_t)stream, name, false);
 }

@@ -34,7 +34,7 @@ namespace {
 
 constexpr int kQrThreads = 128;
 constexpr int kQrNB = 8;
-constexpr int kQrMaxN = 64;
+constexpr int kQrMaxN = 128;
 // s_t layout: T (NB x NB) | tau (NB) | scratch (128) | V^T V strict upper part (28, padded to 32)
 constexpr int kTOff = 0;
 constexpr int kTauOff = kQrNB * kQrNB;
@@ -46,16 +46,19 @@ struct QrArgs {
   int count;
   int n;
   int m_max;
-  const int32_t* ms;
-  const int64_t* aoff;
+  const int32_t* ms;    // null: every problem is m_uni x n
+  const int64_t* aoff;  // null: problem s at A + s * strideA
   double* A;
-  const int64_t* boff;  // nullable: factor only
-  double* B;
+  const int64_t* boff;  // null with B set: b of problem s at B + s * strideB
+  double* B;            // nullable: factor only
   double* X;      // n per problem, nullable
   double* diag;   // n per problem
   int32_t* info;
   const int32_t* order;
-  int32_t* counter;
+  int32_t* counter;     // null: problems taken grid-stride (no queue)
+  int m_uni;
+  int64_t strideA, strideB;
+  int x_in_b;           // the square form: the solution overwrites b (QR::solve_mut)
 };
 
 // Butterfly reduce-scatter of N (a power of two <= 32) per-lane values: lane L
@@ -245,13 +248,13 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int n = g.n;
-  const int m = g.ms[s];
+  const int m = g.ms ? g.ms[s] : g.m_uni;
   if (m < n || m > g.m_max) {
     if (tid == 0 && g.info) g.info[s] = -1;
     return;
   }
-  double* a = g.A + g.aoff[s];
-  double* b = g.boff ? g.B + g.boff[s] : nullptr;
+  double* a = g.A + (g.aoff ? g.aoff[s] : (int64_t)s * g.strideA);
+  double* b = g.B ? g.B + (g.boff ? g.boff[s] : (int64_t)s * g.strideB) : nullptr;
   double* s_coef = s_red + 4 + 4 * kQrNB;
   for (int J0 = 0; J0 < n; J0 += kQrNB) {
     const int jb = min(kQrNB, n - J0);
@@ -377,7 +380,7 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
     __syncthreads();
   }
   // ---- sign sweep (nalgebra's reflect_with_sign convention) ----
-  // s_misc[2 + i] = P_i (axis sign), s_misc[2 + 64 + i] = d_i (row sign).
+  // s_misc[2 + i] = P_i (axis sign), s_misc[2 + kQrMaxN + i] = d_i (row sign).
   if (tid == 0) {
     double pi = 1.0;
     int inf = 0;
@@ -400,23 +403,27 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
   // The least-squares solution.  With R_nal = D R_std and (Q^T b)_nal = D (Q^T b)_std
   // the signs cancel; the solve uses nalgebra's R (rows scaled by d_r, diagonal
   // |diag_i|) exactly as qr.rs:224-256 restricted to the top n rows.
-  if (b && g.X && inf == 0 && warp == 0) {
-    double* x = g.X + (size_t)s * n;
-    double yv[2];
+  if (b && (g.X || g.x_in_b) && inf == 0 && warp == 0) {
+    constexpr int KR = kQrMaxN / 32;  // rows per lane
+    double* x = g.x_in_b ? b : g.X + (size_t)s * n;
+    double yv[KR];
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < KR; ++k) {
       const int r = lane + 32 * k;
       yv[k] = (r < n) ? b[r] * s_misc[2 + kQrMaxN + r] : 0.0;
     }
     for (int i = n - 1; i >= 0; --i) {
-      const double yi = __shfl_sync(0xffffffffu, (i < 32) ? yv[0] : yv[1], i & 31);
-      const double xi = yi * s_t[kGOff + i];
-      if (lane == (i & 31)) {
-        if (i < 32) yv[0] = xi;
-        else yv[1] = xi;
-      }
+      double own = yv[0];
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
+      for (int k = 1; k < KR; ++k)
+        if ((i >> 5) == k) own = yv[k];
+      const double yi = __shfl_sync(0xffffffffu, own, i & 31);
+      const double xi = yi * s_t[kGOff + i];
+#pragma unroll
+      for (int k = 0; k < KR; ++k)
+        if (lane == (i & 31) && (i >> 5) == k) yv[k] = xi;
+#pragma unroll
+      for (int k = 0; k < KR; ++k) {
         const int r = lane + 32 * k;
         if (r < i) {  // R[r][i] times the row sign d_r = +-1: a sign-bit flip, no FP64 multiply
           const unsigned long long sm =
@@ -426,8 +433,9 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
         }
       }
     }
+    __syncwarp();
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < KR; ++k) {
       const int r = lane + 32 * k;
       if (r < n) x[r] = yv[k];
     }
@@ -442,7 +450,7 @@ __device__ void qr_one(const QrArgs& g, int s, double* P, int ldp, double* s_t, 
     const unsigned long long mask = (unsigned long long)__double_as_longlong(f) & 0x8000000000000000ull;
     *p = __longlong_as_double(__double_as_longlong(*p) ^ mask);
   }
-  if (b)
+  if (b && !(g.x_in_b && inf == 0))  // Q^T b in nalgebra's signs (the square form's solved b is x)
     for (int r = tid; r < m; r += kQrThreads) {
       const double f = s_misc[2 + kQrMaxN + min(r, n - 1)];
       const unsigned long long mask = (unsigned long long)__double_as_longlong(f) & 0x8000000000000000ull;
@@ -462,6 +470,10 @@ __global__ void __launch_bounds__(kQrThreads, 4) qr_batched_kernel(QrArgs g) {
   __shared__ int s_item;
   const int ldp = g.m_max | 1;
   double* P = reinterpret_cast<double*>(smem_raw);
+  if (!g.counter) {  // uniform batch: problems grid-stride
+    for (int s = blockIdx.x; s < g.count; s += gridDim.x) qr_one(g, s, P, ldp, s_t, s_dstd, s_red, s_misc);
+    return;
+  }
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(g.counter, 1);
     __syncthreads();
@@ -474,6 +486,28 @@ __global__ void __launch_bounds__(kQrThreads, 4) qr_batched_kernel(QrArgs g) {
 }
 
 }  // namespace
+
+// The square QR's FMA form on this kernel: count uniform n x n problems
+// (n <= kQrMaxN) at A + s * strideA, nalgebra's QR layout and signs in place,
+// diag and info out; with B (one right-hand side per problem at B + s *
+// strideB) QR::solve_mut overwrites b with x.
+int qr_uniform_launch(int n, int count, double* A, int64_t strideA, double* diag, double* B, int64_t strideB,
+                      int32_t* info, cudaStream_t s, const char* name) {
+  QrArgs g{count, n, n, nullptr, nullptr, A, nullptr, B, nullptr, diag, info, nullptr, nullptr, n, strideA, strideB,
+           1};
+  const size_t smem = (size_t)(n | 1) * kQrNB * sizeof(double);
+  cudaError_t e = ensure_dynamic_smem(qr_batched_kernel, smem);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_batched_kernel, kQrThreads, smem);
+  if (e != cudaSuccess) return record_cuda_error(e, name);
+  if (per_sm < 1) per_sm = 1;
+  int grid = sm_count() * per_sm;
+  if (grid > count) grid = count;
+  qr_batched_kernel<<<grid, kQrThreads, smem, s>>>(g);
+  return check_launch(name);
+}
+
 }  // namespace nacu
 
 extern "C" {
@@ -489,7 +523,7 @@ int nacu_dgels_batched(int count, int n, int m_max, const int32_t* ms, const int
                        nacu_stream_t stream) {
   using namespace nacu;
   if (count < 0) return record_arg_error(-1, "dgels_batched: negative count");
-  if (n < 1 || n > kQrMaxN) return record_arg_error(-2, "dgels_batched: n out of range [1, 64]");
+  if (n < 1 || n > kQrMaxN) return record_arg_error(-2, "dgels_batched: n out of range [1, 128]");
   if (m_max < n || m_max > NACU_QR_MAX_M) return record_arg_error(-3, "dgels_batched: m_max out of range [n, 2048]");
   if (count == 0) return NACU_SUCCESS;
   if (!ms || !a_offsets || !A) return record_arg_error(-4, "dgels_batched: null ms, a_offsets or A");
@@ -499,7 +533,7 @@ int nacu_dgels_batched(int count, int n, int m_max, const int32_t* ms, const int
     return record_arg_error(-14, "dgels_batched: workspace too small");
   if (flags & NACU_FLAG_EXACT) return record_arg_error(-15, "dgels_batched: NACU_FLAG_EXACT is not available for QR");
   QrArgs g{count, n, m_max, ms, a_offsets, A, b_offsets, B, X, diag, info, order,
-           reinterpret_cast<int32_t*>(workspace)};
+           reinterpret_cast<int32_t*>(workspace), 0, 0, 0, 0};
   const size_t smem = (size_t)(m_max | 1) * kQrNB * sizeof(double);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = ensure_dynamic_smem(qr_batched_kernel, smem);

@@ -67,7 +67,7 @@ def _qtb_oracle(w, qr_o, diag_o):
     return out
 
 
-@pytest.mark.parametrize("n", [1, 3, 8, 13, 64])
+@pytest.mark.parametrize("n", [1, 3, 8, 13, 64, 100, 128])
 def test_shapes(cuda, n):
     w = W.ragged_ls(40, n, 3 * n + 7, n, seed=n)
     A, B, X, diag, info = _gels(cuda, w)

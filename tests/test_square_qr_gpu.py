@@ -127,6 +127,32 @@ def test_fma_form_reconstructs_and_solves(cuda, n):
         assert berr <= 8 * np.finfo(float).eps, (n, k, berr)
 
 
+@pytest.mark.parametrize("n", [1, 7, 64, 100, 128])
+@pytest.mark.parametrize("nrhs", [0, 1])
+def test_fma_single_rhs_form(cuda, n, nrhs):
+    """The FMA form with at most one right-hand side (the compact-WY kernel of
+    the least-squares path): nalgebra's stored layout and signs to rounding,
+    info as QR::is_invertible, and b overwritten by the solution."""
+    mats = _batch(n, 6, 200 + n)
+    rng = np.random.default_rng(201 + n)
+    rhs = [rng.standard_normal((n, 1)) for _ in mats] if nrhs else None
+    A, diag, info, B = _factor(cuda, mats, n, 0, rhs)
+    for k, m in enumerate(mats):
+        qr_o, d_o = O.qr(m)
+        assert info[k] == _info_ref(d_o), (n, k)
+        if np.isnan(m).any() or info[k] != 0:
+            continue
+        scale = np.abs(m).max()
+        assert np.abs(A[k].reshape(n, n).T - qr_o).max() <= 1e-10 * max(1.0, scale), (n, k)
+        assert np.abs(diag[k] - d_o).max() <= 1e-10 * scale, (n, k)
+        if nrhs:
+            x = B[k].reshape(n)
+            berr = np.abs(m @ x - rhs[k][:, 0]).max() / (scale * np.abs(x).max() * n)
+            assert berr <= 8 * np.finfo(float).eps, (n, k, berr)
+            x_o, ok = O.qr_solve(qr_o, d_o, rhs[k])
+            assert ok and np.abs(x - x_o[:, 0]).max() <= 1e-9 * np.abs(x_o).max(), (n, k)
+
+
 def test_mirror_qr(cuda):
     from nalgebra_gb300 import QR, DeviceMatrix
 
