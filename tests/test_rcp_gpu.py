@@ -38,7 +38,7 @@ def test_within_one_ulp_of_ieee(cuda):
 def test_edge_operands_take_the_division(cuda):
     d = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-310, -1e-305, 2.0 ** -1001, 2.0 ** 1000, 1e308, 1.0, -3.0])
     got = _rcp(cuda, d)
-    with np.errstate(divide="ignore"):
+    with np.errstate(divide="ignore", over="ignore"):
         ref = 1.0 / d
     assert np.array_equal(got[~np.isnan(ref)], ref[~np.isnan(ref)])
     assert np.isnan(got[np.isnan(ref)]).all()
