@@ -711,3 +711,39 @@ def test_gemm_gemv_order_restatement_bit_for_bit():
     mat2 = np.array([[1.0, 2.0, 3.0], [4.0, 5.0, 6.0]])
     mat3 = np.array([[0.1, 0.2, 0.3, 0.4], [0.5, 0.6, 0.7, 0.8], [0.9, 1.0, 1.1, 1.2]])
     assert np.allclose(O.gemm_gemv_order(10.0, mat2, mat3, 5.0, mat1), mat2 @ mat3 * 10.0 + mat1 * 5.0, rtol=1e-12)
+
+
+@pytest.mark.parametrize("n", [1, 4, 10, 20])
+def test_qr_solve_properties(n):
+    """tests/linalg/qr.rs:55-69, 87-99: for invertible square m, QR::solve gives
+    m x = b (1e-6; here far tighter) and solve_mut on the identity gives the
+    inverse (m m^-1 = I to 1e-5)."""
+    rng = np.random.default_rng(700 + n)
+    a = rng.uniform(-100, 100, size=(n, n))
+    qr, diag = O.qr(a)
+    b = rng.standard_normal((n, 3))
+    x, ok = O.qr_solve(qr, diag, b)
+    assert ok and np.allclose(a @ x, b, atol=1e-9, rtol=0)
+    inv, ok = O.qr_solve(qr, diag, np.eye(n))
+    assert ok and np.allclose(a @ inv, np.eye(n), atol=1e-9, rtol=0)
+    assert np.allclose(inv @ a, np.eye(n), atol=1e-9, rtol=0)
+
+
+def test_qr_solve_equals_col_piv_solve_without_pivots():
+    """QR::solve_mut and ColPivQR::solve_mut run the same q_tr_mul and upper
+    solve; with an identity permutation their restatements agree bit for bit
+    (the one difference is the inverse permutation)."""
+    rng = np.random.default_rng(711)
+    a = rng.uniform(-100, 100, size=(12, 12))
+    qr, diag = O.qr(a)
+    b = rng.standard_normal((12, 2))
+    x, ok = O.qr_solve(qr, diag, b)
+    y, ok2 = O.col_piv_qr_solve(qr, diag, np.arange(12, dtype=np.int32), b)
+    assert ok and ok2 and np.array_equal(x, y)
+
+
+def test_qr_solve_zero_diagonal_returns_false():
+    """A zero |diag_i| stops the upper solve (qr.rs:238-242): false."""
+    qr, diag = O.qr(np.zeros((3, 3)))
+    _, ok = O.qr_solve(qr, diag, np.array([1.0, 2.0, 3.0]))
+    assert not ok
