@@ -207,6 +207,8 @@ def bench_ragged_ours(args, rank, world):
     batch = DeviceBatch(A, ns, ns, aoff)
     rhs = DeviceBatch(B, ns, np.full(count, nrhs), boff)
     chol = batch.cholesky()
+    info_t = torch.as_tensor(chol.info, device=dev)  # torch views of the mirror's buffers
+    logdet_t = torch.as_tensor(chol.logdet, device=dev)
     stream = torch.cuda.current_stream()
     sp = int(stream.cuda_stream)
     n_max = int(ns.max())
@@ -235,10 +237,10 @@ def bench_ragged_ours(args, rank, world):
         launch()
     stream = torch.cuda.current_stream()
     restore()
-    chol.info.fill_(-7)
+    info_t.fill_(-7)
     graph.replay()
     torch.cuda.synchronize()
-    if int((chol.info != 0).sum().item()) != 0:
+    if int((info_t != 0).sum().item()) != 0:
         raise RuntimeError("graph replay did not run the factorization")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if world > 1:
@@ -262,7 +264,7 @@ def bench_ragged_ours(args, rank, world):
                                               b0.cpu().numpy())
             out["mixed"].pop("_objects")
         return out, None
-    info = chol.info.cpu().numpy()
+    info = info_t.cpu().numpy()
     if np.any(info != 0):
         raise RuntimeError(f"{int(np.sum(info != 0))} systems failed to factor")
     # accuracy of the last step's solutions, every system of the batch
@@ -313,8 +315,8 @@ def bench_ragged_ours(args, rank, world):
             chol.factored = False
             chol.solve_mut(rhs)
             x_pin.copy_(B, non_blocking=True)
-            i_pin.copy_(chol.info, non_blocking=True)
-            l_pin.copy_(chol.logdet, non_blocking=True)
+            i_pin.copy_(info_t, non_blocking=True)
+            l_pin.copy_(logdet_t, non_blocking=True)
 
     e2e_step()
     torch.cuda.synchronize()
@@ -417,7 +419,7 @@ def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_
     graph-replayed launch per step."""
     import torch
 
-    from nalgebra_gb300 import DeviceBatch
+    from nalgebra_gb300 import DeviceBatch, Graph
 
     count = ns.size
     batch = DeviceBatch(a0, ns, ns, aoff)
@@ -427,8 +429,8 @@ def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_
     for _ in range(args.warmup):
         chol.solve_refined_into(rhs, out)
     torch.cuda.synchronize()
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph):
+    graph = Graph()  # the mirror's own capture (nacu_graph_*), replayed on the default stream
+    with graph.capture():
         chol.solve_refined_into(rhs, out)
     out.data.zero_()
     graph.replay()
@@ -440,10 +442,10 @@ def bench_ragged_mixed(args, L, ns, aoff, boff, a0, b0, nrhs, stream, a_host, b_
         ev[i][1].record(stream)
     torch.cuda.synchronize()
     ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
-    it = chol._iters.cpu().numpy()[:count]
-    if np.any(chol.info.cpu().numpy()[:count] != 0):
+    it = chol._iters.to_numpy()[:count]
+    if np.any(chol.info.to_numpy()[:count] != 0):
         raise RuntimeError("mixed form: systems reported not SPD")
-    x_host = out.data.cpu().numpy()
+    x_host = out.data.to_numpy()
     acc = batch_accuracy(ns, aoff, a_host, boff, b_host, x_host, nrhs, x_ref)
     n = ns.astype(np.float64)
     fp64_flops = float(np.sum(np.abs(it) * 2.0 * nrhs * n * n))  # FP64 residual work actually executed

@@ -70,7 +70,7 @@ typedef void* nacu_stream_t;
 #define NACU_LU_BATCHED_MAX_N 128
 #define NACU_LU_BATCHED_MAX_NRHS 16
 #define NACU_CHOL_RAGGED_MAX_N 512
-#define NACU_QR_MAX_N 64
+#define NACU_QR_MAX_N 128
 #define NACU_QR_MAX_M 2048
 
 /* ---- library ------------------------------------------------------------- */
@@ -81,6 +81,47 @@ const char* nacu_version(void);
 const char* nacu_last_error(void);
 /* Compiled device architecture, e.g. 103 for sm_103a. */
 int nacu_device_arch(void);
+
+/* ---- device memory, copies, streams, graphs -------------------------------
+ * Plumbing for hosts without a CUDA binding of their own (nalgebra's side of
+ * the FFI has none: a `DMatrix` is host memory).  Each is one CUDA runtime
+ * call under the library's error convention.  nalgebra counterpart: none; a
+ * `nalgebra-cuda` `DeviceMatrix::from(&DMatrix)` / `to_host()` is
+ * nacu_malloc + nacu_memcpy. */
+
+/* Number of visible CUDA devices (0 and NACU_ERR_CUDA when there is none). */
+int nacu_device_count(int* count);
+/* Device memory; bytes == 0 gives NULL.  nacu_free(NULL) is a no-op.
+ * nacu_free synchronizes the device (cudaFree). */
+int nacu_malloc(void** ptr, size_t bytes);
+int nacu_free(void* ptr);
+/* Page-locked host memory (lets nacu_memcpy and the *_host entry points
+ * overlap copies with kernels). */
+int nacu_host_alloc(void** ptr, size_t bytes);
+int nacu_host_free(void* ptr);
+/* Asynchronous copy on `stream`, any direction (unified addressing decides:
+ * host->device, device->host, device->device).  A copy to pageable host
+ * memory returns when it is complete. */
+int nacu_memcpy(void* dst, const void* src, size_t bytes, nacu_stream_t stream);
+/* Asynchronous byte fill on `stream`. */
+int nacu_memset(void* ptr, int value, size_t bytes, nacu_stream_t stream);
+/* A non-blocking stream; destroy(NULL) is a no-op. */
+int nacu_stream_create(nacu_stream_t* stream);
+int nacu_stream_destroy(nacu_stream_t stream);
+int nacu_stream_synchronize(nacu_stream_t stream);
+/* Work queued on `waiting` after this call starts after the work queued on
+ * `on` before it. */
+int nacu_stream_wait(nacu_stream_t waiting, nacu_stream_t on);
+int nacu_device_synchronize(void);
+/* CUDA-graph capture of the calls queued on `stream` (a created stream, not
+ * NULL) between begin and end; *graph_exec is the instantiated graph, run by
+ * nacu_graph_launch on any stream.  No call of this library allocates or
+ * synchronizes inside its compute entry points, so every one of them can be
+ * captured. */
+int nacu_graph_begin_capture(nacu_stream_t stream);
+int nacu_graph_end_capture(nacu_stream_t stream, void** graph_exec);
+int nacu_graph_launch(void* graph_exec, nacu_stream_t stream);
+int nacu_graph_destroy(void* graph_exec);
 
 /* ---- LU with partial pivoting (batched, n <= 128) ------------------------- */
 

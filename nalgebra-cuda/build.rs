@@ -50,6 +50,4 @@ fn main() {
     assert!(status.success(), "nvcc link failed");
     println!("cargo:rustc-link-search=native={}", out.display());
     println!("cargo:rustc-link-lib=dylib=nalgebra_cuda");
-    // the crate's own device-memory calls (cuda.rs) go to the CUDA runtime
-    println!("cargo:rustc-link-lib=dylib=cudart");
 }

@@ -13,6 +13,23 @@ pub const NACU_FLAG_VERIFY: c_int = 8;
 #[link(name = "nalgebra_cuda")]
 extern "C" {
     pub fn nacu_last_error() -> *const c_char;
+    // device memory, copies, streams, graphs (the crate's DeviceBuffer uses these)
+    pub fn nacu_device_count(count: *mut c_int) -> c_int;
+    pub fn nacu_malloc(ptr: *mut *mut c_void, bytes: usize) -> c_int;
+    pub fn nacu_free(ptr: *mut c_void) -> c_int;
+    pub fn nacu_host_alloc(ptr: *mut *mut c_void, bytes: usize) -> c_int;
+    pub fn nacu_host_free(ptr: *mut c_void) -> c_int;
+    pub fn nacu_memcpy(dst: *mut c_void, src: *const c_void, bytes: usize, s: Stream) -> c_int;
+    pub fn nacu_memset(ptr: *mut c_void, value: c_int, bytes: usize, s: Stream) -> c_int;
+    pub fn nacu_stream_create(s: *mut Stream) -> c_int;
+    pub fn nacu_stream_destroy(s: Stream) -> c_int;
+    pub fn nacu_stream_synchronize(s: Stream) -> c_int;
+    pub fn nacu_stream_wait(waiting: Stream, on: Stream) -> c_int;
+    pub fn nacu_device_synchronize() -> c_int;
+    pub fn nacu_graph_begin_capture(s: Stream) -> c_int;
+    pub fn nacu_graph_end_capture(s: Stream, graph_exec: *mut *mut c_void) -> c_int;
+    pub fn nacu_graph_launch(graph_exec: *mut c_void, s: Stream) -> c_int;
+    pub fn nacu_graph_destroy(graph_exec: *mut c_void) -> c_int;
     // LU, batched (n <= 128) and large
     pub fn nacu_dgetrf_batched(n: c_int, a: *mut f64, stride_a: i64, ipiv: *mut i32,
                                info: *mut i32, batch: c_int, flags: c_int, s: Stream) -> c_int;

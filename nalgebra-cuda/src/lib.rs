@@ -47,17 +47,17 @@ impl<T: Copy> DeviceBuffer<T> {
         let mut p: *mut c_void = std::ptr::null_mut();
         let bytes = len.max(1) * std::mem::size_of::<T>();
         unsafe {
-            cuda::check(cuda::cudaMalloc(&mut p, bytes), "cudaMalloc");
-            cuda::check(cuda::cudaMemset(p, 0, bytes), "cudaMemset");
+            cuda::check(cuda::nacu_malloc(&mut p, bytes), "nacu_malloc");
+            cuda::check(cuda::nacu_memset(p, 0, bytes, std::ptr::null_mut()), "nacu_memset");
         }
         DeviceBuffer { ptr: p as *mut T, len, _t: PhantomData }
     }
     pub fn from_slice(h: &[T]) -> Self {
         let b = Self::zeroed(h.len());
         unsafe {
-            cuda::check(cuda::cudaMemcpy(b.ptr as *mut c_void, h.as_ptr() as *const c_void,
-                                         h.len() * std::mem::size_of::<T>(), cuda::MEMCPY_HOST_TO_DEVICE),
-                        "cudaMemcpy");
+            cuda::check(cuda::nacu_memcpy(b.ptr as *mut c_void, h.as_ptr() as *const c_void,
+                                          h.len() * std::mem::size_of::<T>(), std::ptr::null_mut()),
+                        "nacu_memcpy");
         }
         b
     }
@@ -65,9 +65,10 @@ impl<T: Copy> DeviceBuffer<T> {
     pub fn to_vec(&self) -> Vec<T> {
         let mut v: Vec<T> = Vec::with_capacity(self.len);
         unsafe {
-            cuda::check(cuda::cudaMemcpy(v.as_mut_ptr() as *mut c_void, self.ptr as *const c_void,
-                                         self.len * std::mem::size_of::<T>(), cuda::MEMCPY_DEVICE_TO_HOST),
-                        "cudaMemcpy");
+            cuda::check(cuda::nacu_memcpy(v.as_mut_ptr() as *mut c_void, self.ptr as *const c_void,
+                                          self.len * std::mem::size_of::<T>(), std::ptr::null_mut()),
+                        "nacu_memcpy");
+            cuda::check(cuda::nacu_stream_synchronize(std::ptr::null_mut()), "nacu_stream_synchronize");
             v.set_len(self.len);
         }
         v
@@ -75,9 +76,9 @@ impl<T: Copy> DeviceBuffer<T> {
     pub fn clone_device(&self) -> Self {
         let b = Self::zeroed(self.len);
         unsafe {
-            cuda::check(cuda::cudaMemcpy(b.ptr as *mut c_void, self.ptr as *const c_void,
-                                         self.len * std::mem::size_of::<T>(), cuda::MEMCPY_DEVICE_TO_DEVICE),
-                        "cudaMemcpy");
+            cuda::check(cuda::nacu_memcpy(b.ptr as *mut c_void, self.ptr as *const c_void,
+                                          self.len * std::mem::size_of::<T>(), std::ptr::null_mut()),
+                        "nacu_memcpy");
         }
         b
     }
@@ -95,13 +96,13 @@ impl<T: Copy> DeviceBuffer<T> {
 impl<T> Drop for DeviceBuffer<T> {
     fn drop(&mut self) {
         unsafe {
-            cuda::cudaFree(self.ptr as *mut c_void);
+            cuda::nacu_free(self.ptr as *mut c_void);
         }
     }
 }
 
 fn sync() {
-    unsafe { cuda::check(cuda::cudaStreamSynchronize(std::ptr::null_mut()), "cudaStreamSynchronize") };
+    unsafe { cuda::check(cuda::nacu_stream_synchronize(std::ptr::null_mut()), "nacu_stream_synchronize") };
 }
 
 /// An nrows x ncols f64 matrix on the GPU, column-major like nalgebra's

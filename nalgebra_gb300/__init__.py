@@ -18,9 +18,13 @@ nalgebra (reference)                here
 ``chol.ln_determinant()`` :172     ``Cholesky.ln_determinant()``
 =================================  ==============================================
 
-Device memory and streams come from PyTorch (plumbing only); every numerical
-operation is a hand-written sm_103a kernel reached through the C ABI.  There
-is no CPU fallback: without a GPU or without the built library, calls raise.
+Device memory, copies, streams and CUDA graphs go through the library's own
+plumbing entry points (``_device``: nacu_malloc, nacu_memcpy, nacu_graph_*),
+so the mirror needs nothing but libnalgebra_cuda.so and numpy; device arrays
+of other libraries plug in through ``__cuda_array_interface__``.  Every
+numerical operation is a hand-written sm_103a kernel reached through the C
+ABI.  There is no CPU fallback: without a GPU or without the built library,
+calls raise.
 Factorizations are lazy where that lets one launch do factor + solve: ``lu()``
 and ``cholesky()`` on a batch record the request, and the first ``solve``
 runs the fused kernel, writing the factors as a side effect.
@@ -29,8 +33,10 @@ from __future__ import annotations
 
 import numpy as np
 
+from . import _device as _dev
 from . import _lib
 from . import factor_format
+from ._device import DeviceBuffer, Graph, Stream, current_stream, pinned_empty, set_stream, stream, synchronize
 from ._lib import FLAG_EXACT, FLAG_NO_FACTORS, FLAG_SUBSTITUTE, NacuError
 
 __all__ = [
@@ -38,37 +44,49 @@ __all__ = [
     "gemm_batched",
     "PosvLogdet", "cholesky_solve_refined_host",
     "NacuError", "FLAG_EXACT", "FLAG_NO_FACTORS", "FLAG_SUBSTITUTE", "FullPivLU", "ColPivQR", "QR",
+    "DeviceBuffer", "Graph", "Stream", "current_stream", "set_stream", "stream", "synchronize", "pinned_empty",
 ]
 
 
-def _torch():
-    import torch  # deferred: plumbing only
-
-    if not torch.cuda.is_available():
-        raise NacuError("nalgebra_gb300 needs a CUDA GPU: there is no CPU fallback")
-    return torch
+def _stream_ptr() -> int:
+    return _dev.current_stream()
 
 
-def _stream_ptr(stream=None) -> int:
-    torch = _torch()
-    s = stream if stream is not None else torch.cuda.current_stream()
-    return int(s.cuda_stream)
+def _dev_f64(x) -> DeviceBuffer:
+    """A float64 device array as it is, or a host array copied to the device."""
+    return _dev.as_device(x, np.float64)
 
 
-def _dev_f64(x, torch):
-    if isinstance(x, torch.Tensor):
-        return x.to(device="cuda", dtype=torch.float64).contiguous()
-    return torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to("cuda")
+def _i32(k: int) -> DeviceBuffer:
+    return _dev.zeros(max(int(k), 1), np.int32)
+
+
+def _f64(k: int) -> DeviceBuffer:
+    return _dev.zeros(max(int(k), 1), np.float64)
+
+
+def _bytes(k: int) -> DeviceBuffer:
+    return _dev.empty(max(int(k), 1), np.uint8)
+
+
+def _padded_i32(v, n: int) -> DeviceBuffer:
+    return _dev.from_numpy(np.append(np.asarray(v).astype(np.int32), np.zeros(max(n, 1) - n, np.int32)))
+
+
+def _padded_f64(v, n: int) -> DeviceBuffer:
+    return _dev.from_numpy(np.append(np.asarray(v, dtype=np.float64), np.zeros(max(n, 1) - n)))
 
 
 class DeviceMatrix:
     """An nrows x ncols f64 matrix resident on the GPU, column-major like
     nalgebra's DMatrix (src/base/vec_storage.rs:28-32).  ``data`` is a flat
-    CUDA tensor of nrows*ncols elements."""
+    float64 device buffer of nrows*ncols elements (a DeviceBuffer; a device
+    array of another library is wrapped without a copy, a host array is
+    copied)."""
 
     def __init__(self, data, nrows: int, ncols: int):
-        torch = _torch()
-        self.data = data if isinstance(data, torch.Tensor) else _dev_f64(data, torch)
+        _dev.require_gpu()
+        self.data = _dev_f64(data)
         if self.data.numel() != nrows * ncols:
             raise ValueError("data size does not match nrows * ncols")
         self.nrows, self.ncols = int(nrows), int(ncols)
@@ -82,7 +100,7 @@ class DeviceMatrix:
         return cls(flat, a.shape[0], a.shape[1])
 
     def to_numpy(self) -> np.ndarray:
-        return self.data.cpu().numpy().reshape(self.ncols, self.nrows).T.copy()
+        return self.data.to_numpy().reshape(self.ncols, self.nrows).T.copy()
 
     @property
     def shape(self):
@@ -98,12 +116,11 @@ class DeviceMatrix:
     def _trsv(self, b: "DeviceMatrix", upper: bool, trans: bool, diag=None, flags: int = 0) -> bool:
         """nacu_dtrsv_batched on one matrix (n <= 128), nacu_dtrsv above: b is
         overwritten."""
-        torch = _torch()
         n = self.nrows
         assert self.is_square() and b.nrows == n, "triangular solve dimension mismatch"
-        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        info = _i32(1)
         if n > 128:
-            ws = torch.empty(_lib.load().nacu_trsv_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+            ws = _bytes(_lib.load().nacu_trsv_workspace_bytes(n))
             _lib.call("nacu_dtrsv", n, b.ncols, int(upper), int(trans), int(diag is not None),
                       float(diag if diag is not None else 0.0), self.data.data_ptr(), n, b.data.data_ptr(), n,
                       info.data_ptr(), ws.data_ptr(), ws.numel(), flags, _stream_ptr())
@@ -193,15 +210,14 @@ class LU:
     kernel (batch of one); larger n: the blocked multi-SM factorization."""
 
     def __init__(self, m: DeviceMatrix, flags: int = 0):
-        torch = _torch()
         self.lu = m
         n = m.nrows
         self.flags = flags
-        self.ipiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
-        self.info = torch.zeros(2, dtype=torch.int32, device="cuda")
+        self.ipiv = _i32(n)
+        self.info = _i32(2)
         self.large = n > 128
         if self.large:
-            self._ws = torch.empty(_lib.load().nacu_getrf_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+            self._ws = _bytes(_lib.load().nacu_getrf_workspace_bytes(n))
             _lib.call("nacu_dgetrf", n, m.data.data_ptr(), n, self.ipiv.data_ptr(), self.info.data_ptr(),
                       self._ws.data_ptr(), self._ws.numel(), _stream_ptr())
         else:
@@ -212,8 +228,7 @@ class LU:
         """LU::solve_mut (src/linalg/lu.rs:242-260)."""
         n = self.lu.nrows
         assert b.nrows == n, "LU solve matrix dimension mismatch."
-        torch = _torch()
-        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        info = _i32(1)
         if self.large:
             ok = True
             for c in range(b.ncols):
@@ -233,7 +248,7 @@ class LU:
 
     def p(self):
         """The PermutationSequence as nalgebra stores it: (i, piv) swaps in order."""
-        piv = self.ipiv.cpu().numpy()[: self.lu.nrows]
+        piv = self.ipiv.to_numpy()[: self.lu.nrows]
         return [(i, int(p)) for i, p in enumerate(piv) if p != i]
 
     def determinant(self) -> float:
@@ -245,7 +260,7 @@ class LU:
         return d * (1.0 if len(self.p()) % 2 == 0 else -1.0)
 
     def is_invertible(self) -> bool:
-        return int(self.info[0].item()) == 0
+        return int(self.info.item()) == 0
 
     def try_inverse(self):
         """LU::try_inverse (src/linalg/lu.rs:266-297): the inverse as a new
@@ -253,9 +268,8 @@ class LU:
         n = self.lu.nrows
         if self.large:
             raise NotImplementedError("try_inverse: n <= 128 (the batched kernels)")
-        torch = _torch()
-        out = DeviceMatrix(torch.empty(n * n, dtype=torch.float64, device="cuda"), n, n)
-        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        out = DeviceMatrix(_dev.empty(n * n, np.float64), n, n)
+        info = _i32(1)
         _lib.call("nacu_dgetri_batched", n, self.lu.data.data_ptr(), n * n, self.ipiv.data_ptr(), out.data.data_ptr(),
                   n * n, info.data_ptr(), 1, self.flags, _stream_ptr())
         return out if int(info.item()) == 0 else None
@@ -269,21 +283,20 @@ class LU:
 
     def to_json(self) -> str:
         """nalgebra's serde JSON form of LU (src/linalg/lu.rs:14-38)."""
-        return factor_format.lu_to_json(self.lu.to_numpy(), self.ipiv.cpu().numpy()[: self.lu.nrows])
+        return factor_format.lu_to_json(self.lu.to_numpy(), self.ipiv.to_numpy()[: self.lu.nrows])
 
     @classmethod
     def from_json(cls, s: str, flags: int = 0) -> "LU":
         """An LU from nalgebra's serde JSON form, its factors on the device."""
-        torch = _torch()
         lu, ipiv = factor_format.lu_from_json(s)
         n = lu.shape[0]
         obj = cls.__new__(cls)
         obj.lu, obj.flags, obj.large = DeviceMatrix.from_numpy(lu), flags, n > 128
-        obj.ipiv = torch.from_numpy(np.append(ipiv.astype(np.int32), np.zeros(max(n, 1) - n, np.int32))).cuda()
+        obj.ipiv = _padded_i32(ipiv, n)
         zero = np.nonzero(np.diag(lu) == 0)[0]
-        obj.info = torch.tensor([int(zero[0]) + 1 if len(zero) else 0, 0], dtype=torch.int32, device="cuda")
+        obj.info = _dev.from_numpy(np.array([int(zero[0]) + 1 if len(zero) else 0, 0], np.int32))
         if obj.large:
-            obj._ws = torch.empty(_lib.load().nacu_getrf_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+            obj._ws = _bytes(_lib.load().nacu_getrf_workspace_bytes(n))
         return obj
 
 
@@ -292,20 +305,18 @@ class FullPivLU:
     the matrix buffer, row and column pivots on the device."""
 
     def __init__(self, m: DeviceMatrix, flags: int = 0):
-        torch = _torch()
         assert m.is_square(), "the batched full-pivot kernel takes square matrices"
         n = m.nrows
         self.lu, self.flags = m, flags
-        self.ipiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
-        self.jpiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
-        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.ipiv = _i32(n)
+        self.jpiv = _i32(n)
+        self.info = _i32(1)
         _lib.call("nacu_dfullpivlu_batched", n, 0, m.data.data_ptr(), n * n, self.ipiv.data_ptr(),
                   self.jpiv.data_ptr(), 0, 0, self.info.data_ptr(), 1, flags, _stream_ptr())
 
     def _solve_cols(self, b: DeviceMatrix) -> bool:
-        torch = _torch()
         n = self.lu.nrows
-        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        info = _i32(1)
         for c0 in range(0, b.ncols, 16):
             k = min(16, b.ncols - c0)
             _lib.call("nacu_dfullpivlu_solve_batched", n, k, self.lu.data.data_ptr(), n * n, self.ipiv.data_ptr(),
@@ -326,9 +337,8 @@ class FullPivLU:
     def try_inverse(self):
         """FullPivLU::try_inverse (full_piv_lu.rs:216-233): solve_mut on the
         identity, 16 columns per launch; None when not invertible."""
-        torch = _torch()
         n = self.lu.nrows
-        out = DeviceMatrix(torch.eye(n, dtype=torch.float64, device="cuda").t().contiguous().reshape(-1), n, n)
+        out = DeviceMatrix(np.eye(n).reshape(-1), n, n)
         return out if self._solve_cols(out) else None
 
     def is_invertible(self) -> bool:
@@ -336,11 +346,11 @@ class FullPivLU:
         return int(self.info.item()) == 0
 
     def p(self):
-        piv = self.ipiv.cpu().numpy()[: self.lu.nrows]
+        piv = self.ipiv.to_numpy()[: self.lu.nrows]
         return [(i, int(q)) for i, q in enumerate(piv) if q != i]
 
     def q(self):
-        piv = self.jpiv.cpu().numpy()[: self.lu.nrows]
+        piv = self.jpiv.to_numpy()[: self.lu.nrows]
         return [(i, int(q)) for i, q in enumerate(piv) if q != i]
 
     def determinant(self) -> float:
@@ -364,23 +374,22 @@ class FullPivLU:
     def to_json(self) -> str:
         """nalgebra's serde JSON form of FullPivLU (src/linalg/full_piv_lu.rs:14-39)."""
         n = self.lu.nrows
-        return factor_format.full_piv_lu_to_json(self.lu.to_numpy(), self.ipiv.cpu().numpy()[:n],
-                                                 self.jpiv.cpu().numpy()[:n])
+        return factor_format.full_piv_lu_to_json(self.lu.to_numpy(), self.ipiv.to_numpy()[:n],
+                                                 self.jpiv.to_numpy()[:n])
 
     @classmethod
     def from_json(cls, s: str, flags: int = 0) -> "FullPivLU":
         """A FullPivLU from nalgebra's serde JSON form; info is 0 when
         U[n-1][n-1] != 0, else 1 + the first zero U_ii."""
-        torch = _torch()
         lu, ipiv, jpiv = factor_format.full_piv_lu_from_json(s)
         n = lu.shape[0]
         obj = cls.__new__(cls)
         obj.lu, obj.flags = DeviceMatrix.from_numpy(lu), flags
-        obj.ipiv = torch.from_numpy(np.append(ipiv.astype(np.int32), np.zeros(max(n, 1) - n, np.int32))).cuda()
-        obj.jpiv = torch.from_numpy(np.append(jpiv.astype(np.int32), np.zeros(max(n, 1) - n, np.int32))).cuda()
+        obj.ipiv = _padded_i32(ipiv, n)
+        obj.jpiv = _padded_i32(jpiv, n)
         zero = np.nonzero(np.diag(lu) == 0)[0]
         inv = n == 0 or lu[n - 1, n - 1] != 0
-        obj.info = torch.tensor([0 if inv else int(zero[0]) + 1], dtype=torch.int32, device="cuda")
+        obj.info = _dev.from_numpy(np.array([0 if inv else int(zero[0]) + 1], np.int32))
         return obj
 
 
@@ -389,19 +398,17 @@ class QR:
     matrix buffer, the signed diagonal on the device (src/linalg/qr.rs:34-40)."""
 
     def __init__(self, m: DeviceMatrix, flags: int = 0):
-        torch = _torch()
         assert m.is_square(), "the batched QR kernel takes square matrices"
         n = m.nrows
         self.qr, self.flags = m, flags
-        self.diag = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
-        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.diag = _f64(n)
+        self.info = _i32(1)
         _lib.call("nacu_dqr_batched", n, 0, m.data.data_ptr(), n * n, self.diag.data_ptr(), 0, 0,
                   self.info.data_ptr(), 1, flags, _stream_ptr())
 
     def _solve_cols(self, b: DeviceMatrix) -> bool:
-        torch = _torch()
         n = self.qr.nrows
-        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        info = _i32(1)
         for c0 in range(0, b.ncols, 16):
             k = min(16, b.ncols - c0)
             _lib.call("nacu_dqr_solve_batched", n, k, self.qr.data.data_ptr(), n * n, self.diag.data_ptr(),
@@ -421,9 +428,8 @@ class QR:
 
     def try_inverse(self):
         """QR::try_inverse (qr.rs:262-279)."""
-        torch = _torch()
         n = self.qr.nrows
-        out = DeviceMatrix(torch.eye(n, dtype=torch.float64, device="cuda").reshape(-1).clone(), n, n)
+        out = DeviceMatrix(np.eye(n).reshape(-1), n, n)
         return out if self._solve_cols(out) else None
 
     def is_invertible(self) -> bool:
@@ -434,27 +440,26 @@ class QR:
         """QR::r (qr.rs:81-89): the upper triangle, |diag| on its diagonal."""
         n = self.qr.nrows
         r = np.triu(self.qr.to_numpy())
-        r[np.arange(n), np.arange(n)] = np.abs(self.diag.cpu().numpy()[:n])
+        r[np.arange(n), np.arange(n)] = np.abs(self.diag.to_numpy()[:n])
         return r
 
     def to_json(self) -> str:
         """nalgebra's serde JSON form of QR (src/linalg/qr.rs:34-40)."""
         n = self.qr.nrows
-        return factor_format.qr_to_json(self.qr.to_numpy(), self.diag.cpu().numpy()[:n])
+        return factor_format.qr_to_json(self.qr.to_numpy(), self.diag.to_numpy()[:n])
 
     @classmethod
     def from_json(cls, s: str, flags: int = 0) -> "QR":
         """A square QR from nalgebra's serde JSON form."""
-        torch = _torch()
         qr, diag = factor_format.qr_from_json(s)
         if qr.shape[0] != qr.shape[1]:
             raise ValueError("QR.from_json: the device QR takes square factors")
         n = qr.shape[0]
         obj = cls.__new__(cls)
         obj.qr, obj.flags = DeviceMatrix.from_numpy(qr), flags
-        obj.diag = torch.from_numpy(np.append(diag, np.zeros(max(n, 1) - n))).cuda()
+        obj.diag = _padded_f64(diag, n)
         zero = np.nonzero(diag == 0)[0]
-        obj.info = torch.tensor([int(zero[0]) + 1 if len(zero) else 0], dtype=torch.int32, device="cuda")
+        obj.info = _dev.from_numpy(np.array([int(zero[0]) + 1 if len(zero) else 0], np.int32))
         return obj
 
 
@@ -464,20 +469,18 @@ class ColPivQR:
     on the device."""
 
     def __init__(self, m: DeviceMatrix, flags: int = 0):
-        torch = _torch()
         assert m.is_square(), "the batched column-pivot kernel takes square matrices"
         n = m.nrows
         self.qr, self.flags = m, flags
-        self.diag = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
-        self.jpiv = torch.zeros(max(n, 1), dtype=torch.int32, device="cuda")
-        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.diag = _f64(n)
+        self.jpiv = _i32(n)
+        self.info = _i32(1)
         _lib.call("nacu_dcolpivqr_batched", n, 0, m.data.data_ptr(), n * n, self.diag.data_ptr(),
                   self.jpiv.data_ptr(), 0, 0, self.info.data_ptr(), 1, flags, _stream_ptr())
 
     def _solve_cols(self, b: DeviceMatrix) -> bool:
-        torch = _torch()
         n = self.qr.nrows
-        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        info = _i32(1)
         for c0 in range(0, b.ncols, 16):
             k = min(16, b.ncols - c0)
             _lib.call("nacu_dcolpivqr_solve_batched", n, k, self.qr.data.data_ptr(), n * n, self.diag.data_ptr(),
@@ -498,9 +501,8 @@ class ColPivQR:
 
     def try_inverse(self):
         """ColPivQR::try_inverse (col_piv_qr.rs:288-303)."""
-        torch = _torch()
         n = self.qr.nrows
-        out = DeviceMatrix(torch.eye(n, dtype=torch.float64, device="cuda").reshape(-1).clone(), n, n)
+        out = DeviceMatrix(np.eye(n).reshape(-1), n, n)
         return out if self._solve_cols(out) else None
 
     def is_invertible(self) -> bool:
@@ -508,14 +510,14 @@ class ColPivQR:
         return int(self.info.item()) == 0
 
     def p(self):
-        piv = self.jpiv.cpu().numpy()[: self.qr.nrows]
+        piv = self.jpiv.to_numpy()[: self.qr.nrows]
         return [(i, int(q)) for i, q in enumerate(piv) if q != i]
 
     def determinant(self) -> float:
         """ColPivQR::determinant (col_piv_qr.rs:324-338): the product of diag
         in order, times the sign of p."""
         res = 1.0
-        for d in self.diag.cpu().numpy()[: self.qr.nrows]:
+        for d in self.diag.to_numpy()[: self.qr.nrows]:
             res *= float(d)
         return res * (-1.0 if len(self.p()) % 2 else 1.0)
 
@@ -524,27 +526,26 @@ class ColPivQR:
         its diagonal."""
         n = self.qr.nrows
         r = np.triu(self.qr.to_numpy())
-        r[np.arange(n), np.arange(n)] = np.abs(self.diag.cpu().numpy()[:n])
+        r[np.arange(n), np.arange(n)] = np.abs(self.diag.to_numpy()[:n])
         return r
 
     def to_json(self) -> str:
         """nalgebra's serde JSON form of ColPivQR (src/linalg/col_piv_qr.rs:14-43)."""
         n = self.qr.nrows
-        return factor_format.col_piv_qr_to_json(self.qr.to_numpy(), self.jpiv.cpu().numpy()[:n],
-                                                self.diag.cpu().numpy()[:n])
+        return factor_format.col_piv_qr_to_json(self.qr.to_numpy(), self.jpiv.to_numpy()[:n],
+                                                self.diag.to_numpy()[:n])
 
     @classmethod
     def from_json(cls, s: str, flags: int = 0) -> "ColPivQR":
         """A ColPivQR from nalgebra's serde JSON form."""
-        torch = _torch()
         qr, jpiv, diag = factor_format.col_piv_qr_from_json(s)
         n = qr.shape[0]
         obj = cls.__new__(cls)
         obj.qr, obj.flags = DeviceMatrix.from_numpy(qr), flags
-        obj.diag = torch.from_numpy(np.append(diag, np.zeros(max(n, 1) - n))).cuda()
-        obj.jpiv = torch.from_numpy(np.append(jpiv.astype(np.int32), np.zeros(max(n, 1) - n, np.int32))).cuda()
+        obj.diag = _padded_f64(diag, n)
+        obj.jpiv = _padded_i32(jpiv, n)
         zero = np.nonzero(diag == 0)[0]
-        obj.info = torch.tensor([int(zero[0]) + 1 if len(zero) else 0], dtype=torch.int32, device="cuda")
+        obj.info = _dev.from_numpy(np.array([int(zero[0]) + 1 if len(zero) else 0], np.int32))
         return obj
 
 
@@ -557,11 +558,10 @@ def solve_refined(a: DeviceMatrix, b: DeviceMatrix, tol_units: float = 1.0, max_
     fallback, gmres)."""
     import ctypes as C
 
-    torch = _torch()
     n = a.nrows
     assert a.is_square() and b.nrows == n and b.ncols == 1, "one n x n system with one right-hand side"
-    x = DeviceMatrix(torch.empty(n, dtype=torch.float64, device="cuda"), n, 1)
-    ws = torch.empty(_lib.load().nacu_gesv_mixed_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    x = DeviceMatrix(_dev.empty(n, np.float64), n, 1)
+    ws = _bytes(_lib.load().nacu_gesv_mixed_workspace_bytes(n))
     it, berr, fb = C.c_int(0), C.c_double(0.0), C.c_int(0)
     _lib.call("nacu_dgesv_mixed_ir", n, a.data.data_ptr(), n, b.data.data_ptr(), x.data.data_ptr(),
               float(tol_units), int(max_iter), C.byref(it), C.byref(berr), C.byref(fb), ws.data_ptr(), ws.numel(),
@@ -577,49 +577,44 @@ def cholesky_solve_refined_host(ns, a_offsets, a, b_offsets, b, nrhs: int, chunk
     the packed ragged layout (matrix s at a[a_offsets[s]:], ns[s] x ns[s]
     column-major; its nrhs right-hand sides at b[b_offsets[s]:]).  The copies in
     and out are pipelined with the solves over ``chunks`` parts
-    (nacu_dposv_ragged_mixed_host); page-locked host memory (torch tensors
-    with pin_memory) gives the overlap.  Returns (x, info, iters) as host
-    arrays, x in the layout of b."""
-    torch = _torch()
-
-    def host(v, dtype):
-        if isinstance(v, torch.Tensor):
-            return v.contiguous()
-        return torch.from_numpy(np.ascontiguousarray(v, dtype=dtype))
-
-    hns, haoff, hboff = host(ns, np.int32), host(a_offsets, np.int64), host(b_offsets, np.int64)
-    ha, hb = host(a, np.float64), host(b, np.float64)
-    count = int(hns.numel())
-    pinned = bool(ha.is_pinned())
-    hx = torch.empty(hb.numel(), dtype=torch.float64, pin_memory=pinned)
-    hinfo = torch.empty(count, dtype=torch.int32, pin_memory=pinned)
-    hit = torch.empty(count, dtype=torch.int32, pin_memory=pinned)
+    (nacu_dposv_ragged_mixed_host); inputs in page-locked host memory
+    (``pinned_empty``) let the copies in overlap the solves, and the outputs
+    are page-locked.  Returns (x, info, iters) as host arrays, x in the layout
+    of b."""
+    _dev.require_gpu()
+    hns = np.ascontiguousarray(ns, dtype=np.int32)
+    haoff, hboff = np.ascontiguousarray(a_offsets, dtype=np.int64), np.ascontiguousarray(b_offsets, dtype=np.int64)
+    ha, hb = np.ascontiguousarray(a, dtype=np.float64), np.ascontiguousarray(b, dtype=np.float64)
+    count = int(hns.size)
+    hx = pinned_empty(hb.size, np.float64)
+    hinfo = pinned_empty(count, np.int32)
+    hit = pinned_empty(count, np.int32)
     n_max = int(hns.max()) if count else 0
     L = _lib.load()
-    nbytes = L.nacu_mixed_host_workspace_bytes(count, n_max, hns.data_ptr(), haoff.data_ptr(), hboff.data_ptr(),
+    nbytes = L.nacu_mixed_host_workspace_bytes(count, n_max, hns.ctypes.data, haoff.ctypes.data, hboff.ctypes.data,
                                                int(nrhs), int(chunks))
     if count and nbytes == 0:
         raise NacuError("cholesky_solve_refined_host: invalid layout (orders or offsets)")
-    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
-    _lib.call("nacu_dposv_ragged_mixed_host", count, n_max, hns.data_ptr(), haoff.data_ptr(), ha.data_ptr(),
-              int(nrhs), hboff.data_ptr(), hb.data_ptr(), hx.data_ptr(), hinfo.data_ptr(), hit.data_ptr(),
-              int(chunks), ws.data_ptr(), ws.numel(), float(tol_units), int(max_iter), 0.0, 0,
-              int(stream.cuda_stream))
-    stream.synchronize()
-    return hx.numpy(), hinfo.numpy(), hit.numpy()
+    ws = _bytes(max(nbytes, 256))
+    s = _stream_ptr()
+    _lib.call("nacu_dposv_ragged_mixed_host", count, n_max, hns.ctypes.data, haoff.ctypes.data, ha.ctypes.data,
+              int(nrhs), hboff.ctypes.data, hb.ctypes.data, hx.ctypes.data if hx.size else None,
+              hinfo.ctypes.data if count else None, hit.ctypes.data if count else None, int(chunks),
+              ws.data_ptr(), ws.numel(), float(tol_units), int(max_iter), 0.0, 0, s)
+    synchronize(s)
+    return hx, hinfo, hit
 
 
 def gemm(c: DeviceMatrix, alpha: float, a: DeviceMatrix, b: DeviceMatrix, beta: float, split_slices: int = 0):
     """Matrix::gemm (src/base/blas.rs:729-746): c = alpha a b + beta c, in
     place.  split_slices = 1..3 selects the BF16-split tensor-core form."""
-    torch = _torch()
+    _dev.require_gpu()
     m, k = a.shape
     k2, n = b.shape
     assert k == k2 and c.shape == (m, n), "gemm dimension mismatch"
     if split_slices:
         wsb = _lib.load().nacu_gemm_split_workspace_bytes(m, n, k)
-        ws = torch.empty(wsb + 1024, dtype=torch.uint8, device="cuda")
+        ws = _bytes(wsb + 1024)
         wp = (ws.data_ptr() + 1023) // 1024 * 1024
         _lib.call("nacu_dgemm_split_bf16", m, n, k, float(alpha), a.data.data_ptr(), max(m, 1), b.data.data_ptr(),
                   max(k, 1), float(beta), c.data.data_ptr(), max(m, 1), int(split_slices), wp, wsb, _stream_ptr())
@@ -631,19 +626,25 @@ def gemm(c: DeviceMatrix, alpha: float, a: DeviceMatrix, b: DeviceMatrix, beta: 
 
 def gemm_batched(c, alpha: float, a, b, beta: float, flags: int = 0):
     """Matrix::gemm over a batch (src/base/blas.rs:729-746): c[s] = alpha a[s]
-    b[s] + beta c[s], in place, for CUDA float64 tensors of shapes (batch, k,
-    m), (batch, n, k) and (batch, n, m) -- each product's column-major image,
-    i.e. the transposed row-major view.  ``a @ b`` for many matrices
-    (src/base/ops.rs:566-570) is alpha = 1, beta = 0.  FLAG_EXACT: nalgebra's
-    gemv summation order, bit for bit."""
-    _torch()
-    batch, k, m = a.shape
-    batch2, n, k2 = b.shape
-    assert batch == batch2 and k == k2 and tuple(c.shape) == (batch, n, m), "gemm_batched dimension mismatch"
-    for t in (a, b, c):
-        assert t.is_contiguous() and t.dtype == _torch().float64 and t.is_cuda, "contiguous CUDA float64 tensors"
-    _lib.call("nacu_dgemm_batched", m, n, k, float(alpha), a.data_ptr(), max(m, 1), m * k, b.data_ptr(), max(k, 1),
-              k * n, float(beta), c.data_ptr(), max(m, 1), m * n, batch, int(flags), _stream_ptr())
+    b[s] + beta c[s], in place, for C-contiguous float64 device arrays
+    (DeviceBuffer, or any array with ``__cuda_array_interface__``) of shapes
+    (batch, k, m), (batch, n, k) and (batch, n, m) -- each product's
+    column-major image, i.e. the transposed row-major view.  ``a @ b`` for many
+    matrices (src/base/ops.rs:566-570) is alpha = 1, beta = 0.  FLAG_EXACT:
+    nalgebra's gemv summation order, bit for bit."""
+    _dev.require_gpu()
+    da, db = _dev.as_device(a, np.float64), _dev.as_device(b, np.float64)
+    dc = DeviceBuffer.wrap(c)  # written in place: a device array
+    if dc.dtype != np.float64:
+        raise TypeError("gemm_batched: c must be a float64 device array")
+    for t in (da, db, dc):
+        if len(t.shape) != 3:
+            raise ValueError("gemm_batched takes (batch, rows, cols) device arrays")
+    batch, k, m = da.shape
+    batch2, n, k2 = db.shape
+    assert batch == batch2 and k == k2 and tuple(dc.shape) == (batch, n, m), "gemm_batched dimension mismatch"
+    _lib.call("nacu_dgemm_batched", m, n, k, float(alpha), da.data_ptr(), max(m, 1), m * k, db.data_ptr(),
+              max(k, 1), k * n, float(beta), dc.data_ptr(), max(m, 1), m * n, batch, int(flags), _stream_ptr())
     return c
 
 
@@ -652,23 +653,21 @@ class Cholesky:
     keeps the input values, as nalgebra's l_dirty (src/linalg/cholesky.rs:115)."""
 
     def __init__(self, m: DeviceMatrix, flags: int = 0, substitute: float | None = None):
-        torch = _torch()
         self.chol = m
         self.flags = flags | (FLAG_SUBSTITUTE if substitute is not None else 0)
         self.substitute = 0.0 if substitute is None else float(substitute)
-        self.info = torch.zeros(1, dtype=torch.int32, device="cuda")
-        self.logdet = torch.zeros(1, dtype=torch.float64, device="cuda")
+        self.info = _i32(1)
+        self.logdet = _f64(1)
         _lib.call("nacu_dposv", m.nrows, m.data.data_ptr(), 0, 0, self.info.data_ptr(), self.logdet.data_ptr(),
                   self.substitute, self.flags, _stream_ptr())
 
     def solve_mut(self, b: DeviceMatrix) -> None:
         """Cholesky::solve_mut (src/linalg/cholesky.rs:122-129)."""
-        torch = _torch()
         n = self.chol.nrows
         assert b.nrows == n
-        ns = torch.tensor([n], dtype=torch.int32, device="cuda")
-        off = torch.zeros(1, dtype=torch.int64, device="cuda")
-        ws = torch.zeros(_lib.load().nacu_ragged_workspace_bytes(1), dtype=torch.uint8, device="cuda")
+        ns = _dev.from_numpy(np.array([n], np.int32))
+        off = _dev.zeros(1, np.int64)
+        ws = _dev.zeros(_lib.load().nacu_ragged_workspace_bytes(1), np.uint8)
         _lib.call("nacu_dpotrs_ragged", 1, n, ns.data_ptr(), off.data_ptr(), self.chol.data.data_ptr(), b.ncols,
                   off.data_ptr(), b.data.data_ptr(), 0, ws.data_ptr(), ws.numel(), self.flags, _stream_ptr())
 
@@ -702,10 +701,9 @@ class Cholesky:
     def rank_one_update(self, x: DeviceMatrix, sigma: float) -> None:
         """Cholesky::rank_one_update (src/linalg/cholesky.rs:277-285): the factor
         becomes that of L L^T + sigma x x^T, in place (n <= 128); x is read only."""
-        torch = _torch()
         n = self.chol.nrows
         assert x.nrows == n and x.ncols == 1
-        s = torch.full((1,), float(sigma), dtype=torch.float64, device="cuda")
+        s = _dev.from_numpy(np.array([float(sigma)]))
         _lib.call("nacu_dchol_rank1_update_batched", n, self.chol.data.data_ptr(), n * n, x.data.data_ptr(), n,
                   s.data_ptr(), 1, self.flags & FLAG_EXACT, _stream_ptr())
         self.logdet = None
@@ -713,10 +711,9 @@ class Cholesky:
     def remove_column(self, j: int) -> "Cholesky":
         """Cholesky::remove_column (src/linalg/cholesky.rs:365-399): the factor
         of the matrix without row and column j (n <= 128)."""
-        torch = _torch()
         n = self.chol.nrows
         assert 0 <= j < n
-        out = DeviceMatrix(torch.zeros((n - 1) * (n - 1), dtype=torch.float64, device="cuda"), n - 1, n - 1)
+        out = DeviceMatrix(_dev.zeros((n - 1) * (n - 1), np.float64), n - 1, n - 1)
         _lib.call("nacu_dchol_remove_column_batched", n, self.chol.data.data_ptr(), n * n, j, out.data.data_ptr(),
                   max((n - 1) * (n - 1), 0), 1, self.flags & FLAG_EXACT, _stream_ptr())
         return Cholesky._from_factor(out, self.flags & FLAG_EXACT)
@@ -725,11 +722,10 @@ class Cholesky:
         """Cholesky::insert_column (src/linalg/cholesky.rs:287-357): the factor of
         the matrix with col (n+1 values) inserted as row and column j (n <= 127).
         Raises ValueError where nalgebra's assertion on the lower solve fails."""
-        torch = _torch()
         n = self.chol.nrows
         assert 0 <= j <= n and col.nrows == n + 1 and col.ncols == 1
-        out = DeviceMatrix(torch.zeros((n + 1) * (n + 1), dtype=torch.float64, device="cuda"), n + 1, n + 1)
-        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        out = DeviceMatrix(_dev.zeros((n + 1) * (n + 1), np.float64), n + 1, n + 1)
+        info = _i32(1)
         _lib.call("nacu_dchol_insert_column_batched", n, self.chol.data.data_ptr(), n * n, j, col.data.data_ptr(),
                   n + 1, out.data.data_ptr(), (n + 1) * (n + 1), info.data_ptr(), 1, self.flags & FLAG_EXACT,
                   _stream_ptr())
@@ -757,16 +753,15 @@ class DeviceBatch:
     ``ns`` are the row counts, ``ms`` the column counts (== ns for square)."""
 
     def __init__(self, data, nrows, ncols=None, offsets=None):
-        torch = _torch()
         self.nrows = np.asarray(nrows, dtype=np.int64)
         self.ncols = self.nrows.copy() if ncols is None else np.asarray(ncols, dtype=np.int64)
         sizes = self.nrows * self.ncols
         if offsets is None:
             offsets = np.concatenate([[0], np.cumsum(sizes)[:-1]]) if sizes.size else np.zeros(0, np.int64)
         self.offsets = np.asarray(offsets, dtype=np.int64)
-        self.data = data if isinstance(data, torch.Tensor) else _dev_f64(data, torch)
-        self._d_rows = torch.from_numpy(self.nrows.astype(np.int32)).to("cuda")
-        self._d_off = torch.from_numpy(self.offsets).to("cuda")
+        self.data = _dev_f64(data)
+        self._d_rows = _dev.from_numpy(self.nrows.astype(np.int32))
+        self._d_off = _dev.from_numpy(self.offsets)
 
     @classmethod
     def from_numpy(cls, mats) -> "DeviceBatch":
@@ -779,7 +774,7 @@ class DeviceBatch:
         return int(self.nrows.size)
 
     def to_numpy(self):
-        host = self.data.cpu().numpy()
+        host = self.data.to_numpy().reshape(-1)
         return [host[o:o + r * c].reshape(c, r).T.copy()
                 for o, r, c in zip(self.offsets, self.nrows, self.ncols)]
 
@@ -804,14 +799,13 @@ class LUBatch:
     ``solve`` runs the fused factor + solve kernel."""
 
     def __init__(self, batch: DeviceBatch, flags: int = 0):
-        torch = _torch()
         if not batch.is_uniform() or batch.nrows[0] != batch.ncols[0]:
             raise ValueError("LUBatch needs equal-order square matrices")
         self.batch = batch
         self.n = int(batch.nrows[0])
         self.flags = flags
-        self.ipiv = torch.zeros(len(batch) * self.n, dtype=torch.int32, device="cuda")
-        self.info = torch.zeros(len(batch), dtype=torch.int32, device="cuda")
+        self.ipiv = _i32(len(batch) * self.n)
+        self.info = _dev.zeros(len(batch), np.int32)
         self.factored = False
 
     def factor(self) -> "LUBatch":
@@ -847,11 +841,10 @@ class LUBatch:
         """LU::try_inverse (src/linalg/lu.rs:266-297) of every matrix: returns
         (inverses as a DeviceBatch, device info: 0 = invertible, k = U_kk == 0,
         nalgebra's None)."""
-        torch = _torch()
         self.factor()
         n, cnt = self.n, len(self.batch)
-        data = torch.empty(cnt * n * n, dtype=torch.float64, device="cuda")
-        info = torch.zeros(cnt, dtype=torch.int32, device="cuda")
+        data = _dev.empty(max(cnt * n * n, 1), np.float64)
+        info = _dev.zeros(cnt, np.int32)
         _lib.call("nacu_dgetri_batched", n, self.batch.data.data_ptr(), n * n, self.ipiv.data_ptr(), data.data_ptr(),
                   n * n, info.data_ptr(), cnt, self.flags, _stream_ptr())
         nn = np.full(cnt, n, dtype=np.int32)
@@ -859,7 +852,7 @@ class LUBatch:
 
     def pivots(self) -> np.ndarray:
         self.factor()
-        return self.ipiv.cpu().numpy().reshape(len(self.batch), self.n)
+        return self.ipiv.to_numpy().reshape(len(self.batch), self.n)
 
 
 class CholeskyBatch:
@@ -869,7 +862,6 @@ class CholeskyBatch:
     log-determinant in one pass over the batch."""
 
     def __init__(self, batch: DeviceBatch, flags: int = 0, substitute: float | None = None):
-        torch = _torch()
         if np.any(batch.nrows != batch.ncols):
             raise ValueError("Cholesky needs square matrices")
         self.batch = batch
@@ -877,11 +869,11 @@ class CholeskyBatch:
         self.substitute = 0.0 if substitute is None else float(substitute)
         count = len(batch)
         self.n_max = int(batch.nrows.max()) if count else 0
-        self.info = torch.zeros(count, dtype=torch.int32, device="cuda")
-        self.logdet = torch.zeros(count, dtype=torch.float64, device="cuda")
+        self.info = _dev.zeros(count, np.int32)
+        self.logdet = _dev.zeros(count, np.float64)
         order = np.argsort(-batch.nrows, kind="stable").astype(np.int32)  # largest first
-        self._order = torch.from_numpy(order).to("cuda")
-        self._ws = torch.zeros(_lib.load().nacu_ragged_workspace_bytes(count), dtype=torch.uint8, device="cuda")
+        self._order = _dev.from_numpy(order)
+        self._ws = _dev.zeros(_lib.load().nacu_ragged_workspace_bytes(count), np.uint8)
         self.factored = False
 
     def factor(self) -> "CholeskyBatch":
@@ -918,28 +910,22 @@ class CholeskyBatch:
         self.solve_mut(res)
         return res
 
-    def capture(self, rhs: DeviceBatch):
+    def capture(self, rhs: DeviceBatch) -> Graph:
         """Capture the fused factor + solve + log-det of this batch into a CUDA
-        graph (torch.cuda.CUDAGraph); ``graph.replay()`` re-runs it on the
-        same device buffers (refill them between replays: the factorization is
-        in place).  The calls it captures neither synchronize nor allocate."""
-        torch = _torch()
-        g = torch.cuda.CUDAGraph()
-        stream = torch.cuda.Stream()
-        stream.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(stream):
-            self.factored = False
-            self.solve_mut(rhs)  # warm-up launch outside the graph (first-use set-up)
-        torch.cuda.current_stream().wait_stream(stream)
-        torch.cuda.synchronize()
-        with torch.cuda.graph(g):
+        graph (``Graph``); ``graph.replay()`` re-runs it on the same device
+        buffers (refill them between replays: the factorization is in place).
+        The calls it captures neither synchronize nor allocate."""
+        self.factored = False
+        self.solve_mut(rhs)  # warm-up launch outside the graph (first-use set-up)
+        g = Graph()
+        with g.capture():
             self.factored = False
             self.solve_mut(rhs)
         return g
 
     def ln_determinant(self) -> np.ndarray:
         self.factor()
-        return self.logdet.cpu().numpy()
+        return self.logdet.to_numpy()
 
     def solve_refined_into(self, rhs: DeviceBatch, out: DeviceBatch, tol_units: float = 1.0, max_iter: int = 0,
                            verify: bool = False):
@@ -948,14 +934,12 @@ class CholeskyBatch:
         fallback per matrix.  The batch's matrices and ``rhs`` are left
         unchanged; solutions go to ``out`` (same layout as ``rhs``).  Returns the
         device per-matrix residual counts (negative: FP64 fallback used)."""
-        torch = _torch()
         b = self.batch
         nrhs = int(rhs.ncols[0]) if len(rhs) else 0
         if not hasattr(self, "_mws"):
             total = int(b.data.numel())
-            self._mws = torch.empty(_lib.load().nacu_mixed_workspace_bytes(len(b), total), dtype=torch.uint8,
-                                    device="cuda")
-            self._iters = torch.zeros(max(len(b), 1), dtype=torch.int32, device="cuda")
+            self._mws = _bytes(_lib.load().nacu_mixed_workspace_bytes(len(b), total))
+            self._iters = _i32(len(b))
         flags = self.flags & FLAG_SUBSTITUTE
         if verify:
             flags |= _lib.FLAG_VERIFY
@@ -974,7 +958,7 @@ class CholeskyBatch:
     def is_ok(self) -> np.ndarray:
         """Per matrix: True where nalgebra's ``cholesky()`` returns Some."""
         self.factor()
-        return self.info.cpu().numpy() == 0
+        return self.info.to_numpy() == 0
 
 
 class QRBatch:
@@ -984,7 +968,6 @@ class QRBatch:
     least squares in one launch."""
 
     def __init__(self, batch: DeviceBatch):
-        torch = _torch()
         if len(batch) and not np.all(batch.ncols == batch.ncols[0]):
             raise ValueError("QRBatch needs the same column count in every matrix")
         self.batch = batch
@@ -993,11 +976,11 @@ class QRBatch:
             raise ValueError("least squares needs m >= n (nalgebra-lapack Error::Underdetermined)")
         count = len(batch)
         self.m_max = int(batch.nrows.max()) if count else 0
-        self.diag = torch.zeros(max(count * self.n, 1), dtype=torch.float64, device="cuda")
-        self.info = torch.zeros(max(count, 1), dtype=torch.int32, device="cuda")
+        self.diag = _f64(count * self.n)
+        self.info = _i32(count)
         order = np.argsort(-batch.nrows, kind="stable").astype(np.int32)
-        self._order = torch.from_numpy(order).to("cuda")
-        self._ws = torch.zeros(_lib.load().nacu_qr_workspace_bytes(count), dtype=torch.uint8, device="cuda")
+        self._order = _dev.from_numpy(order)
+        self._ws = _dev.zeros(_lib.load().nacu_qr_workspace_bytes(count), np.uint8)
         self.factored = False
 
     def _launch(self, rhs: "DeviceBatch | None", x):
@@ -1022,7 +1005,7 @@ class QRBatch:
             raise NotImplementedError("solve after a separate factor(): call solve on a fresh QRBatch")
         if len(rhs) != len(self.batch) or np.any(rhs.nrows != self.batch.nrows) or np.any(rhs.ncols != 1):
             raise ValueError("one m x 1 right-hand side per matrix")
-        x = _torch().zeros(max(len(self.batch) * self.n, 1), dtype=_torch().float64, device="cuda")
+        x = _f64(len(self.batch) * self.n)
         self._launch(rhs, x)
         return x
 
@@ -1030,14 +1013,14 @@ class QRBatch:
         """nalgebra-lapack QR::solve (nalgebra-lapack/src/qr/abstraction.rs:48-77):
         the (count, n) least-squares solutions (host), rank-deficient rows NaN."""
         res = rhs.clone_owned()
-        x = self.solve_mut(res).cpu().numpy()[: len(self.batch) * self.n].reshape(len(self.batch), self.n)
-        bad = self.info.cpu().numpy()[: len(self.batch)] != 0
+        x = self.solve_mut(res).to_numpy()[: len(self.batch) * self.n].reshape(len(self.batch), self.n)
+        bad = self.info.to_numpy()[: len(self.batch)] != 0
         x[bad] = np.nan
         return x
 
     def diag_host(self) -> np.ndarray:
         self.factor()
-        return self.diag.cpu().numpy()[: len(self.batch) * self.n].reshape(len(self.batch), self.n)
+        return self.diag.to_numpy()[: len(self.batch) * self.n].reshape(len(self.batch), self.n)
 
 
 class PosvLogdet:
@@ -1055,25 +1038,26 @@ class PosvLogdet:
     store form keeps the Cholesky factor from the forward pass; the recompute
     form keeps nothing and refactors A in the backward pass (n^2 values per
     matrix saved for n^3/3 extra flops).  A is (batch, n*n) column-major rows,
-    b (batch, n); device tensors."""
+    b (batch, n): host arrays (copied) or device arrays of the form's dtype
+    (used in place); the results are DeviceBuffers."""
 
     def __init__(self, n: int, batch: int, dtype="float64", recompute: bool = False):
-        torch = _torch()
+        _dev.require_gpu()
         self.n, self.batch = int(n), int(batch)
-        self.tdt = torch.float64 if str(dtype).endswith("64") else torch.float32
-        self.pre = "d" if self.tdt == torch.float64 else "s"
+        self.tdt = np.dtype(np.float64 if str(dtype).endswith("64") else np.float32)
+        self.pre = "d" if self.tdt == np.float64 else "s"
         self.recompute = bool(recompute)
-        self.L = None if self.recompute else torch.zeros((self.batch, self.n * self.n), dtype=self.tdt,
-                                                          device="cuda")
-        self.info = torch.zeros(self.batch, dtype=torch.int32, device="cuda")
+        self.L = None if self.recompute else _dev.zeros((self.batch, self.n * self.n), self.tdt)
+        self.info = _dev.zeros(max(self.batch, 1), np.int32)
         self._A = self._x = None
 
     def forward(self, A, b):
-        torch = _torch()
-        A = A.to(device="cuda", dtype=self.tdt).contiguous()
-        b = b.to(device="cuda", dtype=self.tdt).contiguous()
-        x = torch.empty((self.batch, self.n), dtype=self.tdt, device="cuda")
-        logdet = torch.empty(self.batch, dtype=self.tdt, device="cuda")
+        A = _dev.as_device(A, self.tdt)
+        b = _dev.as_device(b, self.tdt)
+        if A.numel() != self.batch * self.n * self.n or b.numel() != self.batch * self.n:
+            raise ValueError("PosvLogdet.forward: A is (batch, n*n) and b (batch, n)")
+        x = _dev.empty((self.batch, self.n), self.tdt)
+        logdet = _dev.empty(self.batch, self.tdt)
         _lib.call(f"nacu_{self.pre}posv_logdet_forward", self.n, A.data_ptr(), self.n * self.n, b.data_ptr(),
                   x.data_ptr(), None if self.L is None else self.L.data_ptr(), logdet.data_ptr(),
                   self.info.data_ptr(), self.batch, _stream_ptr())
@@ -1082,13 +1066,14 @@ class PosvLogdet:
 
     def backward(self, x_bar, logdet_bar=None):
         """Returns (A_bar, b_bar); logdet_bar None means 1 for every system."""
-        torch = _torch()
         if self._x is None:
             raise RuntimeError("backward before forward")
-        w = x_bar.to(device="cuda", dtype=self.tdt).contiguous()
-        g = None if logdet_bar is None else logdet_bar.to(device="cuda", dtype=self.tdt).contiguous()
-        dA = torch.empty((self.batch, self.n * self.n), dtype=self.tdt, device="cuda")
-        db = torch.empty((self.batch, self.n), dtype=self.tdt, device="cuda")
+        w = _dev.as_device(x_bar, self.tdt)
+        g = None if logdet_bar is None else _dev.as_device(logdet_bar, self.tdt)
+        if w.numel() != self.batch * self.n or (g is not None and g.numel() != self.batch):
+            raise ValueError("PosvLogdet.backward: x_bar is (batch, n) and logdet_bar (batch,)")
+        dA = _dev.empty((self.batch, self.n * self.n), self.tdt)
+        db = _dev.empty((self.batch, self.n), self.tdt)
         src = self._A if self.recompute else self.L
         _lib.call(f"nacu_{self.pre}posv_logdet_backward", self.n, src.data_ptr(), self.n * self.n,
                   1 if self.recompute else 0, self._x.data_ptr(), w.data_ptr(), None if g is None else g.data_ptr(),
@@ -1096,4 +1081,4 @@ class PosvLogdet:
         return dA, db
 
     def is_ok(self) -> np.ndarray:
-        return self.info.cpu().numpy() == 0
+        return self.info.to_numpy() == 0

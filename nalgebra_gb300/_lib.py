@@ -33,6 +33,22 @@ SIGNATURES = {
     "nacu_version": (C.c_char_p, []),
     "nacu_last_error": (C.c_char_p, []),
     "nacu_device_arch": (_i, []),
+    "nacu_device_count": (_i, [C.POINTER(C.c_int)]),
+    "nacu_malloc": (_i, [C.POINTER(C.c_void_p), _sz]),
+    "nacu_free": (_i, [_vp]),
+    "nacu_host_alloc": (_i, [C.POINTER(C.c_void_p), _sz]),
+    "nacu_host_free": (_i, [_vp]),
+    "nacu_memcpy": (_i, [_vp, _vp, _sz, _vp]),
+    "nacu_memset": (_i, [_vp, _i, _sz, _vp]),
+    "nacu_stream_create": (_i, [C.POINTER(C.c_void_p)]),
+    "nacu_stream_destroy": (_i, [_vp]),
+    "nacu_stream_synchronize": (_i, [_vp]),
+    "nacu_stream_wait": (_i, [_vp, _vp]),
+    "nacu_device_synchronize": (_i, []),
+    "nacu_graph_begin_capture": (_i, [_vp]),
+    "nacu_graph_end_capture": (_i, [_vp, C.POINTER(C.c_void_p)]),
+    "nacu_graph_launch": (_i, [_vp, _vp]),
+    "nacu_graph_destroy": (_i, [_vp]),
     "nacu_dgetrf_batched": (_i, [_i, _vp, _i64, _vp, _vp, _i, _i, _vp]),
     "nacu_dgetrs_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dgesv_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _i64, _vp, _i, _i, _vp]),

@@ -144,8 +144,8 @@ def test_mirror_reverse_mode_with_logdet_cotangent(cuda, recompute):
     x, logdet = op.forward(torch.from_numpy(a), torch.from_numpy(b))
     dA, db = op.backward(torch.from_numpy(w), torch.from_numpy(g))
     assert op.is_ok().all()
-    dA = dA.cpu().numpy().reshape(count, n, n).transpose(0, 2, 1)
-    db = db.cpu().numpy()
+    dA = dA.to_numpy().reshape(count, n, n).transpose(0, 2, 1)
+    db = db.to_numpy()
     for s in range(count):
         A = a[s].reshape(n, n).T
         l, _ = O.cholesky(A)

@@ -177,4 +177,4 @@ def test_cuda_graph_replay_matches_direct_launch(cuda):
         got = b.to_numpy()
         for x, y in zip(got, ref):
             assert np.array_equal(x, y)
-        assert np.all(chol.info.cpu().numpy() == 0)
+        assert np.all(chol.info.to_numpy() == 0)

@@ -96,8 +96,7 @@ def test_max_iter_one_forces_fallback_but_stays_correct(cuda):
 def test_mirror_solve_refined_and_graph_capture(cuda):
     """CholeskyBatch.solve_refined (the precision form through the public
     mirror) and its CUDA-graph capture give FP64-accurate solutions."""
-    torch = cuda
-    from nalgebra_gb300 import DeviceBatch
+    from nalgebra_gb300 import DeviceBatch, Graph, synchronize
     w = W.ragged_spd(50, 8, 200, nrhs=4, seed=9)
     mats = [w["a_flat"][o:o + k * k].reshape(k, k).T for o, k in zip(w["a_offsets"], w["ns"])]
     rhs = [w["b_flat"][o:o + 4 * k].reshape(4, k).T for o, k in zip(w["b_offsets"], w["ns"])]
@@ -105,12 +104,12 @@ def test_mirror_solve_refined_and_graph_capture(cuda):
     b = DeviceBatch.from_numpy(rhs)
     out = b.clone_owned()
     chol.solve_refined_into(b, out)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
+    g = Graph()
+    with g.capture():
         chol.solve_refined_into(b, out)
     out.data.zero_()
     g.replay()
-    torch.cuda.synchronize()
+    synchronize()
     xs = out.to_numpy()
     for m, r, x in zip(mats, rhs, xs):
         assert O.backward_error(m, x, r) <= m.shape[0] * EPS64
