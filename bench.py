@@ -1226,6 +1226,96 @@ def bench_qr_square_ours(args, rank, world):
     return res
 
 
+def bench_qr_large_ours(args, rank, world):
+    """QR::new + QR::solve of one large matrix (nacu_dqr, then nacu_dqr_solve:
+    src/linalg/qr.rs:55-76, 204-256): n = 4096 square, one vector, entries
+    U[0, 1) as DMatrix::new_random plus n on the diagonal; also n = 1000 and
+    the reference's wide qr_decompose_100x500 shape (factor only).  The
+    factorization is in place: each step restores A from a pristine device
+    copy outside the timed events (the 134 MB matrix is about the size of L2).
+    Work: 4/3 n^3 flops for the factor, 5 n^2 for Q^T b and the upper solve;
+    FP64 roofline."""
+    import time
+
+    import torch
+
+    import oracle as O
+    from nalgebra_gb300 import _lib
+
+    L = _lib.load()
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    rng = np.random.default_rng(rank)
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    forms, cpu = {}, {}
+    for (m, n, solve) in ((4096, 4096, True), (1000, 1000, True), (100, 500, False)):
+        a = rng.random((m, n)) + (n * np.eye(m, n) if m == n else 0.0)
+        b = rng.random(m)
+        a0 = torch.from_numpy(np.asfortranarray(a).ravel(order="F")).cuda()
+        b0 = torch.from_numpy(b).cuda()
+        A, B = a0.clone(), b0.clone()
+        diag = torch.zeros(min(m, n), dtype=torch.float64, device="cuda")
+        ws = torch.empty(max(L.nacu_qr_solve_workspace_bytes(n), 1), dtype=torch.uint8, device="cuda")
+
+        def launch():
+            _lib.call("nacu_dqr", m, n, A.data_ptr(), m, diag.data_ptr(), 0, sp)
+            if solve:
+                _lib.call("nacu_dqr_solve", m, n, 1, A.data_ptr(), m, diag.data_ptr(), B.data_ptr(), m,
+                          info.data_ptr(), ws.data_ptr(), ws.numel(), 0, sp)
+
+        steps = args.steps if n >= 4096 else max(args.steps, 10)
+        for _ in range(args.warmup):
+            A.copy_(a0); B.copy_(b0); launch()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            for i in range(steps):
+                A.copy_(a0); B.copy_(b0)
+                ev[i][0].record(stream)
+                launch()
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()
+        ms = float(np.mean([e0.elapsed_time(e1) for e0, e1 in ev]))
+        key = f"{m}x{n}" + ("_factor_solve" if solve else "_factor")
+        f = {"ms": ms, "per_s": 1e3 / ms, "clocks": clk.summary(), "launches_per_step": min(m, n) + 1 + (4 if solve else 0)}
+        if solve:
+            x = B.cpu().numpy()[:n]
+            f["backward_error_in_eps"] = float(np.abs(a @ x - b).max() / (np.abs(a).max() * np.abs(x).max() * n)
+                                               / np.finfo(float).eps)
+            f["info"] = int(info.item())
+        forms[key] = f
+        if rank == 0 and not args.no_cpu_baseline and n <= 1000:
+            t0 = time.perf_counter()
+            qr, d = O.qr(a)
+            if solve:
+                O.qr_solve(qr, d, b)
+            cpu[key] = (time.perf_counter() - t0) * 1e3
+        del A, a0, ws
+        torch.cuda.empty_cache()
+    head = forms["4096x4096_factor_solve"]
+    n = 4096
+    flops = 4.0 / 3 * n ** 3 + 5.0 * n ** 2
+    peak = ctypes_probe(L)
+    res = {"metric": "solves/s (QR::new + QR::solve, one 4096x4096 f64 matrix, one vector)",
+           "value": 1e3 / head["ms"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (U[0,1) entries, n added on the diagonal)",
+           "config": {"workload": "qr_large", "shapes": ["4096x4096", "1000x1000", "100x500"], "nrhs": 1,
+                      "l2": "A restored from a pristine copy before each step (134 MB at n = 4096)"},
+           "forms": forms,
+           "roofline": {"bound": "fp64", "achieved": flops / (head["ms"] * 1e-3) / 1e12, "peak": peak / 1e12,
+                        "unit": "TFLOP/s", "frac": flops / (head["ms"] * 1e-3) / peak, "traffic": None,
+                        "peak_source": fp64_peak_source(),
+                        "note": "one launch per Householder step; 4/3 n^3 + 5 n^2 flops per solve"},
+           "gpu_launches": args.steps * head["launches_per_step"], "clocks": head["clocks"]}
+    if cpu:
+        res["cpu_baseline"] = {"value": 1e3 / cpu["1000x1000_factor_solve"], "unit": "solves/s at n = 1000",
+                               "cores": 1, "kind": "port", "ms": cpu,
+                               "sample": "oracle QR::new + QR::solve at 1000x1000, and QR::new at 100x500, "
+                                         "one thread, one run each"}
+    return res
+
+
 # ----------------------------------------------------------------------------- QR least squares
 
 def bench_ls_ours(args, rank, world):
@@ -1673,6 +1763,7 @@ def other_configs(args, rank, world) -> dict:
         ("f2_trsv_large_1000", bench_trsv_large_ours, dict(count=0, steps=min(args.steps, 5)),
          ("forms", "cpu_baseline")),
         ("f_qr_square_100", bench_qr_square_ours, dict(count=0), ("cpu_baseline", "backward_error_sample_in_eps")),
+        ("a8_qr_large_4096", bench_qr_large_ours, dict(count=0, steps=min(args.steps, 3)), ("forms", "cpu_baseline")),
     )
     for name, fn, over, keep in plan:
         a = copy.copy(args)
@@ -1703,7 +1794,7 @@ def main():
     ap.add_argument("--workload", default="ragged_cholesky", choices=["ragged_cholesky", "lu_batched", "ls_qr", "adjoint", "gemm",
                                                                   "mixed_lu", "lu_inverse", "trsv_batched", "chol_update",
                                                                         "full_piv_lu", "col_piv_qr", "mul_batched",
-                                                                        "trsv_large", "qr_square"])
+                                                                        "trsv_large", "qr_square", "qr_large"])
     ap.add_argument("--exact", action="store_true")
     ap.add_argument("--single-launch", action="store_true",
                     help="ragged_cholesky: one launch over a host-sorted order with the default tile "
@@ -1742,15 +1833,16 @@ def main():
         torch.distributed.barrier()
 
     if args.workload in ("lu_batched", "ls_qr", "adjoint", "gemm", "mixed_lu", "lu_inverse", "trsv_batched",
-                         "chol_update", "full_piv_lu", "col_piv_qr", "mul_batched", "trsv_large", "qr_square"):
+                         "chol_update", "full_piv_lu", "col_piv_qr", "mul_batched", "trsv_large", "qr_square",
+                         "qr_large"):
         res = {"lu_batched": bench_lu_ours, "ls_qr": bench_ls_ours, "adjoint": bench_adjoint_ours,
                "gemm": bench_gemm_ours, "mixed_lu": bench_mixed_lu_ours,
                "lu_inverse": bench_lu_inverse_ours, "trsv_batched": bench_trsv_ours,
                "chol_update": bench_chol_update_ours,
                "full_piv_lu": bench_full_piv_lu_ours,
                "col_piv_qr": bench_col_piv_qr_ours, "mul_batched": bench_mul_batched_ours,
-               "trsv_large": bench_trsv_large_ours, "qr_square": bench_qr_square_ours}[args.workload](args, rank,
-                                                                                                       world)
+               "trsv_large": bench_trsv_large_ours, "qr_square": bench_qr_square_ours,
+               "qr_large": bench_qr_large_ours}[args.workload](args, rank, world)
         if rank == 0:
             print(json.dumps(res))
         return

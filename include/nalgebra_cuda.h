@@ -201,6 +201,32 @@ int nacu_dqr_batched(int n, int nrhs, double* A, int64_t strideA, double* diag, 
 int nacu_dqr_solve_batched(int n, int nrhs, const double* QR, int64_t strideA, const double* diag, double* B,
                            int64_t strideB, int32_t* info, int batch, int flags, nacu_stream_t stream);
 
+/* ---- Householder QR of one matrix of any shape ------------------------------ */
+
+/* QR::new (src/linalg/qr.rs:55-76) of one m x n matrix, any m and n (wide
+ * matrices too, e.g. the reference's qr_decompose_100x500): A (lda >= m) is
+ * overwritten with the unit Householder axes on and below the diagonal and R's
+ * strict upper part above it; diag[0 .. min(m, n)) receives the signed
+ * diagonal (R's diagonal is |diag|, qr.rs:81-89; 0 where a column was zero,
+ * nalgebra's is_invertible false, qr.rs:281-292).  One launch per Householder
+ * step, no workspace.  NACU_FLAG_EXACT: nalgebra's arithmetic, bit for bit. */
+int nacu_dqr(int m, int n, double* A, int64_t lda, double* diag, int flags, nacu_stream_t stream);
+
+/* Bytes of device scratch nacu_dqr_solve needs for an n-column factor. */
+size_t nacu_qr_solve_workspace_bytes(int n);
+
+/* Solve from the factors of nacu_dqr, m >= n, m <= 16384: B (m x nrhs,
+ * ldb >= m) <- Q^T B (QR::q_tr_mul, qr.rs:157-171), then its top n rows <-
+ * R^-1 (Q^T B)[0:n] (the upper solve by |diag_i| of qr.rs:224-256).  m == n is
+ * QR::solve_mut; m > n the least-squares solution, as nalgebra-lapack's QR
+ * solve (nalgebra-lapack/src/qr_util.rs:167-239).  *info (device) = the
+ * 1-based index of the zero |diag_i| that stops nalgebra's backward
+ * substitution (the last one; B then holds partial results), 0, or -1000 if
+ * an internal wait between thread blocks ran out.  FMA arithmetic:
+ * NACU_FLAG_EXACT returns -12. */
+int nacu_dqr_solve(int m, int n, int nrhs, const double* QR, int64_t lda, const double* diag, double* B, int64_t ldb,
+                   int32_t* info, void* workspace, size_t workspace_bytes, int flags, nacu_stream_t stream);
+
 /* Inverse from getrf factors: `lu.try_inverse()` (src/linalg/lu.rs:266-297:
  * out = I, then solve_mut(out)), and with nacu_dgetrf_batched before it
  * `m.try_inverse()` for n > 4 (src/linalg/inverse.rs:135-137).  Ainv + s*strideInv

@@ -83,6 +83,12 @@ extern "C" {
     pub fn nacu_dqr_solve_batched(n: c_int, nrhs: c_int, qr: *const f64, stride_a: i64, diag: *const f64,
                                   b: *mut f64, stride_b: i64, info: *mut i32, batch: c_int, flags: c_int,
                                   s: Stream) -> c_int;
+    // QR::new of one matrix of any shape, and its square / least-squares solve
+    pub fn nacu_dqr(m: c_int, n: c_int, a: *mut f64, lda: i64, diag: *mut f64, flags: c_int, s: Stream) -> c_int;
+    pub fn nacu_qr_solve_workspace_bytes(n: c_int) -> usize;
+    pub fn nacu_dqr_solve(m: c_int, n: c_int, nrhs: c_int, qr: *const f64, lda: i64, diag: *const f64,
+                          b: *mut f64, ldb: i64, info: *mut i32, ws: *mut c_void, ws_bytes: usize, flags: c_int,
+                          s: Stream) -> c_int;
     pub fn nacu_getrf_workspace_bytes(n: c_int) -> usize;
     pub fn nacu_dgetrf(n: c_int, a: *mut f64, lda: i64, ipiv: *mut i32, info: *mut i32,
                        ws: *mut c_void, ws_bytes: usize, s: Stream) -> c_int;

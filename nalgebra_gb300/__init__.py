@@ -185,11 +185,9 @@ class DeviceMatrix:
         return FullPivLU(self, flags)
 
     def qr(self, flags: int = 0) -> "QR":
-        """Matrix::qr (src/linalg/decomposition.rs:56-62): factors in place
-        (square, n <= 128).  Tall least-squares batches go through
+        """Matrix::qr (src/linalg/decomposition.rs:56-62): factors in place,
+        any shape.  Batches of tall least-squares systems go through
         DeviceBatch.qr."""
-        if not self.is_square():
-            raise NotImplementedError("the square QR kernel takes n x n matrices; use DeviceBatch.qr for least squares")
         return QR(self, flags)
 
     def col_piv_qr(self, flags: int = 0) -> "ColPivQR":
@@ -394,21 +392,35 @@ class FullPivLU:
 
 
 class QR:
-    """Householder QR of one square matrix (n <= 128): the axes and R in the
-    matrix buffer, the signed diagonal on the device (src/linalg/qr.rs:34-40)."""
+    """Householder QR of one matrix (src/linalg/qr.rs:34-40): the axes and R in
+    the matrix buffer, the signed diagonal on the device.  A square matrix of
+    order <= 128 runs on the shared-memory batched kernel (batch of one); any
+    other shape (larger, tall or wide) on the one-launch-per-step kernel
+    (nacu_dqr)."""
 
     def __init__(self, m: DeviceMatrix, flags: int = 0):
-        assert m.is_square(), "the batched QR kernel takes square matrices"
-        n = m.nrows
         self.qr, self.flags = m, flags
-        self.diag = _f64(n)
+        self.large = not m.is_square() or m.nrows > 128
+        k = min(m.nrows, m.ncols)
+        self.diag = _f64(k)
         self.info = _i32(1)
-        _lib.call("nacu_dqr_batched", n, 0, m.data.data_ptr(), n * n, self.diag.data_ptr(), 0, 0,
-                  self.info.data_ptr(), 1, flags, _stream_ptr())
+        if self.large:
+            _lib.call("nacu_dqr", m.nrows, m.ncols, m.data.data_ptr(), max(m.nrows, 1), self.diag.data_ptr(), flags,
+                      _stream_ptr())
+        else:
+            n = m.nrows
+            _lib.call("nacu_dqr_batched", n, 0, m.data.data_ptr(), n * n, self.diag.data_ptr(), 0, 0,
+                      self.info.data_ptr(), 1, flags, _stream_ptr())
 
     def _solve_cols(self, b: DeviceMatrix) -> bool:
-        n = self.qr.nrows
+        m, n = self.qr.shape
         info = _i32(1)
+        if self.large:
+            ws = _bytes(_lib.load().nacu_qr_solve_workspace_bytes(n))
+            _lib.call("nacu_dqr_solve", m, n, b.ncols, self.qr.data.data_ptr(), max(m, 1), self.diag.data_ptr(),
+                      b.data.data_ptr(), max(m, 1), info.data_ptr(), ws.data_ptr(), ws.numel(), self.flags,
+                      _stream_ptr())
+            return int(info.item()) == 0
         for c0 in range(0, b.ncols, 16):
             k = min(16, b.ncols - c0)
             _lib.call("nacu_dqr_solve_batched", n, k, self.qr.data.data_ptr(), n * n, self.diag.data_ptr(),
@@ -416,8 +428,10 @@ class QR:
         return int(info.item()) == 0
 
     def solve_mut(self, b: DeviceMatrix) -> bool:
-        """QR::solve_mut (src/linalg/qr.rs:204-222): b is overwritten even
-        when it returns False."""
+        """QR::solve_mut (src/linalg/qr.rs:204-222), square factors: b is
+        overwritten even when it returns False.  Orders above 128 solve in
+        FMA arithmetic (no FLAG_EXACT)."""
+        assert self.qr.is_square(), "The QR decomposition must be square."
         assert b.nrows == self.qr.nrows, "QR solve matrix dimension mismatch."
         return self._solve_cols(b)
 
@@ -426,38 +440,56 @@ class QR:
         res = b.clone_owned()
         return res if self.solve_mut(res) else None
 
+    def solve_least_squares(self, b: DeviceMatrix):
+        """The least-squares solution of a tall factor (m >= n), as
+        nalgebra-lapack's QR solve (qr_util.rs:167-239): an n x nrhs
+        DeviceMatrix, or None when some |diag_i| is zero."""
+        m, n = self.qr.shape
+        assert m >= n and b.nrows == m, "least squares needs m >= n and an m-row right-hand side"
+        res = b.clone_owned()
+        if not self._solve_cols(res):
+            return None
+        return DeviceMatrix.from_numpy(res.to_numpy()[:n])
+
     def try_inverse(self):
         """QR::try_inverse (qr.rs:262-279)."""
+        assert self.qr.is_square(), "The QR decomposition must be square."
         n = self.qr.nrows
         out = DeviceMatrix(np.eye(n).reshape(-1), n, n)
         return out if self._solve_cols(out) else None
 
     def is_invertible(self) -> bool:
-        """QR::is_invertible (qr.rs:281-292)."""
+        """QR::is_invertible (qr.rs:281-292): square, and no diag entry zero."""
+        if not self.qr.is_square():
+            return False
+        if self.large:
+            return bool(np.all(self.diag.to_numpy()[: self.qr.nrows] != 0))
         return int(self.info.item()) == 0
 
     def r(self) -> np.ndarray:
-        """QR::r (qr.rs:81-89): the upper triangle, |diag| on its diagonal."""
-        n = self.qr.nrows
-        r = np.triu(self.qr.to_numpy())
-        r[np.arange(n), np.arange(n)] = np.abs(self.diag.to_numpy()[:n])
+        """QR::r (qr.rs:81-89): the min(m, n) x n upper trapezoid, |diag| on its
+        diagonal."""
+        m, n = self.qr.shape
+        k = min(m, n)
+        r = np.triu(self.qr.to_numpy()[:k, :])
+        r[np.arange(k), np.arange(k)] = np.abs(self.diag.to_numpy()[:k])
         return r
 
     def to_json(self) -> str:
         """nalgebra's serde JSON form of QR (src/linalg/qr.rs:34-40)."""
-        n = self.qr.nrows
-        return factor_format.qr_to_json(self.qr.to_numpy(), self.diag.to_numpy()[:n])
+        k = min(self.qr.shape)
+        return factor_format.qr_to_json(self.qr.to_numpy(), self.diag.to_numpy()[:k])
 
     @classmethod
     def from_json(cls, s: str, flags: int = 0) -> "QR":
-        """A square QR from nalgebra's serde JSON form."""
+        """A QR from nalgebra's serde JSON form (any shape)."""
         qr, diag = factor_format.qr_from_json(s)
-        if qr.shape[0] != qr.shape[1]:
-            raise ValueError("QR.from_json: the device QR takes square factors")
-        n = qr.shape[0]
+        m, n = qr.shape
+        k = min(m, n)
         obj = cls.__new__(cls)
         obj.qr, obj.flags = DeviceMatrix.from_numpy(qr), flags
-        obj.diag = _padded_f64(diag, n)
+        obj.large = m != n or n > 128
+        obj.diag = _padded_f64(diag, k)
         zero = np.nonzero(diag == 0)[0]
         obj.info = _dev.from_numpy(np.array([int(zero[0]) + 1 if len(zero) else 0], np.int32))
         return obj

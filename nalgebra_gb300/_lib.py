@@ -66,6 +66,9 @@ SIGNATURES = {
     "nacu_trsv_workspace_bytes": (_sz, [_i]),
     "nacu_dtrsv": (_i, [_i, _i, _i, _i, _i, _d, _vp, _i64, _vp, _i64, _vp, _vp, _sz, _i, _vp]),
     "nacu_dqr_solve_batched": (_i, [_i, _i, _vp, _i64, _vp, _vp, _i64, _vp, _i, _i, _vp]),
+    "nacu_dqr": (_i, [_i, _i, _vp, _i64, _vp, _i, _vp]),
+    "nacu_qr_solve_workspace_bytes": (_sz, [_i]),
+    "nacu_dqr_solve": (_i, [_i, _i, _i, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _sz, _i, _vp]),
     "nacu_dtrsv_batched": (_i, [_i, _i, _i, _i, _i, _d, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dchol_rank1_update_batched": (_i, [_i, _vp, _i64, _vp, _i64, _vp, _i, _i, _vp]),
     "nacu_dchol_remove_column_batched": (_i, [_i, _vp, _i64, _i, _vp, _i64, _i, _i, _vp]),

@@ -760,7 +760,9 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(TrsvArgs<T> g) {
     }
     __syncthreads();
     if (s_abort) return;
-    if (tid < cs) xs[tid] = __ldcg(&g.x[c0 + tid]);
+    // all of xs: past cs it meets zero tile entries, and shared memory may
+    // still hold an earlier kernel's inf or NaN there (NaN * 0)
+    if (tid < BS) xs[tid] = tid < cs ? __ldcg(&g.x[c0 + tid]) : T(0);
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < CW; ++u) acc = axpy1<false>(acc, -xs[tc * CW + u], a[u]);

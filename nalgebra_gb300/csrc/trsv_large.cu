@@ -125,7 +125,10 @@ __global__ void __launch_bounds__(kTrsvLThreads) trsv_large_kernel(TrsvLArgs g) 
       }
       __syncthreads();
       if (s_abort) return;
-      if (tid < cs) xs[tid] = __ldcg(&g.x[c0 + tid]);
+      // the whole of xs: a short last block leaves entries past cs that meet zero
+      // tile entries, and shared memory still holds an earlier kernel's values
+      // there (inf or NaN after a solve that met a zero diagonal: NaN * 0)
+      if (tid < BS) xs[tid] = tid < cs ? __ldcg(&g.x[c0 + tid]) : 0.0;
       __syncthreads();
 #pragma unroll
       for (int u = 0; u < CW; ++u) acc = fma(-xs[tc * CW + u], a[u], acc);
@@ -167,7 +170,10 @@ __global__ void __launch_bounds__(kTrsvLThreads) trsv_large_kernel(TrsvLArgs g) 
       }
       __syncthreads();
       if (s_abort) return;
-      if (tid < cs) xs[tid] = __ldcg(&g.x[c0 + tid]);
+      // the whole of xs: a short last block leaves entries past cs that meet zero
+      // tile entries, and shared memory still holds an earlier kernel's values
+      // there (inf or NaN after a solve that met a zero diagonal: NaN * 0)
+      if (tid < BS) xs[tid] = tid < cs ? __ldcg(&g.x[c0 + tid]) : 0.0;
       __syncthreads();
       const double xv = xs[tcol];
 #pragma unroll

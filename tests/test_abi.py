@@ -57,6 +57,22 @@ def test_cholesky_argument_errors(L):
     assert L.nacu_dposv(4, 0, 0, 0, 0, 0, 0.0, 0, 0) == -2
 
 
+def test_large_qr_argument_errors(L):
+    assert L.nacu_dqr(-1, 4, None, 4, None, 0, None) == -1
+    assert L.nacu_dqr(4, -1, None, 4, None, 0, None) == -2
+    assert L.nacu_dqr(0, 9, None, 1, None, 0, None) == 0  # empty: no work, no device needed
+    assert L.nacu_dqr(5, 5, None, 5, None, 0, None) == -3
+    assert L.nacu_dqr(5, 5, 1024, 4, 1024, 0, None) == -4
+    assert L.nacu_dqr(5, 5, 1024, 5, None, 0, None) == -5
+    assert L.nacu_qr_solve_workspace_bytes(0) == 0 and L.nacu_qr_solve_workspace_bytes(100) >= 100 * 100 * 8
+    assert L.nacu_dqr_solve(16385, 4, 1, None, 1, None, None, 1, None, None, 0, 0, None) == -1
+    assert L.nacu_dqr_solve(4, 5, 1, None, 4, None, None, 4, None, None, 0, 0, None) == -2
+    assert L.nacu_dqr_solve(4, 4, -1, None, 4, None, None, 4, None, None, 0, 0, None) == -3
+    assert L.nacu_dqr_solve(4, 4, 1, None, 4, None, None, 4, None, None, 0, 0, None) == -9
+    assert L.nacu_dqr_solve(4, 4, 1, None, 4, None, None, 4, 1024, None, 0, 1, None) == -12  # EXACT
+    assert L.nacu_dqr_solve(4, 4, 1, 1024, 4, 1024, 1024, 4, 1024, 1024, 8, 0, None) == -11
+
+
 def test_product_has_no_cpu_fallback(tmp_path):
     with pytest.raises(_lib.NacuError):
         _lib.load(str(tmp_path / "missing.so"))

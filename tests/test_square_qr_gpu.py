@@ -170,8 +170,10 @@ def test_mirror_qr(cuda):
     assert np.array_equal(back.solve(DeviceMatrix.from_numpy(b)).to_numpy(), x)
     z = DeviceMatrix.from_numpy(np.zeros((3, 3))).qr()
     assert not z.is_invertible() and z.try_inverse() is None
-    with pytest.raises(NotImplementedError):
-        DeviceMatrix.from_numpy(np.ones((4, 3))).qr()
+    tall = np.arange(12, dtype=np.float64).reshape(4, 3) ** 1.5  # any shape now: the one-matrix kernel
+    qt = DeviceMatrix.from_numpy(tall).qr(flags=FLAG_EXACT)
+    ref_qr, ref_d = O.qr(tall)
+    assert np.array_equal(qt.r(), O.qr_r(ref_qr, ref_d)) and not qt.is_invertible()
 
 
 def test_argument_errors(cuda):

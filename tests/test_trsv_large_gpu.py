@@ -77,6 +77,25 @@ def test_zero_diagonal_info(cuda, upper, trans):
     assert O.triangular_solve(t, b, upper=upper, trans=trans) is None
 
 
+@pytest.mark.parametrize("upper,trans", [(False, False), (True, False), (False, True), (True, True)])
+def test_short_last_block_after_a_zero_diagonal_solve(cuda, upper, trans):
+    """A solve that meets a zero diagonal leaves inf and NaN in the kernel's
+    shared memory; the next solve with a short last block (n = 129: one row)
+    must not pick them up where the tile is zero (NaN * 0)."""
+    n0 = 2000
+    t0 = np.nan_to_num(_tri(n0, upper, 93), nan=0.0)
+    t0[np.arange(0, n0, 50), np.arange(0, n0, 50)] = 0.0
+    _, info = _solve(cuda, t0, np.ones((n0, 1)), upper, trans, None)
+    assert info != 0
+    n = 129
+    t = _tri(n, upper, 94)
+    b = np.random.default_rng(95).standard_normal((n, 2))
+    x, info = _solve(cuda, t, b, upper, trans, None)
+    ref = O.triangular_solve(np.nan_to_num(t, nan=0.0), b, upper=upper, trans=trans)
+    assert info == 0 and np.isfinite(x).all()
+    assert np.abs(x - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
 def test_with_diag_zero_leaves_b(cuda):
     n = 300
     t = np.nan_to_num(_tri(n, False, 5), nan=0.0)
