@@ -9,14 +9,18 @@
 // Factor: one launch per Householder step.  Launch i applies reflector i
 // (Reflection::reflect_with_sign with bias 0, reflection.rs:70-83; skipped
 // where the column was zero, which is where diag[i] == 0) to the trailing
-// columns i+1 .. n-1, one warp per column: a dot with the axis, then
-// y <- factor * axis + sign * y.  The warp that owns column i+1 then turns it
-// into the next axis (reflection_axis_mut, householder.rs:19-53) and writes
-// diag[i+1], so the next launch finds it ready: min(m, n) + 1 launches.  Each
-// reads and writes the trailing matrix once (the second read for the axpy
-// comes from L1/L2), 16-24 bytes per two FP64 FMAs, near the balance point of
-// GB300's FP64 pipe against HBM.  EXACT rounds every operation as Rust does,
-// the dots in dotx's order: bit-identical to nalgebra's factors.
+// columns i+1 .. n-1: a dot with the axis, then y <- factor * axis + sign * y.
+// The block that owns column i+1 then turns it into the next axis
+// (reflection_axis_mut, householder.rs:19-53) and writes diag[i+1], so the
+// next launch finds it ready: min(m, n) + 1 launches.  Each reads and writes
+// the trailing matrix once (the axpy's second read comes from L1/L2), 16-24
+// bytes per two FP64 FMAs, near the balance point of GB300's FP64 pipe against
+// HBM.  The FMA form gives each column a CTA of 256 threads (a thread owns
+// rows t, t + 256, ...; one barrier per block-wide dot): a warp per column
+// left most of the SM idle and every row chain waiting on its loads.  EXACT
+// rounds every operation as Rust does, the dots in dotx's order (eight
+// sequential accumulators), so it keeps one warp per column: bit-identical to
+// nalgebra's factors.
 //
 // Solve: Q^T B by one CTA per right-hand side, each thread owning fixed rows
 // of its column in registers across all steps (so B needs no barrier; the dot
@@ -34,72 +38,45 @@ namespace {
 
 constexpr int kQlThreads = 256;
 constexpr int kQlWarps = kQlThreads / 32;
-constexpr int kQtThreads = 512;
-constexpr int kQtRows = 32;  // rows per thread of the Q^T B kernel
+constexpr int kQcThreads = 128;  // FMA form: one CTA per column
+constexpr int kQcWarps = kQcThreads / 32;
+constexpr int kQtThreads = 1024;
+constexpr int kQtRows = 16;  // rows per thread of the Q^T B kernel
 constexpr int kQtMaxM = kQtThreads * kQtRows;
 
-// Warp dot, FMA form: four interleaved accumulators per lane, valid in every lane.
-__device__ __forceinline__ double ql_dot_fma(int len, const double* __restrict__ x, const double* __restrict__ y,
-                                             int lane) {
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-  int e = lane;
-  for (; e + 96 < len; e += 128) {
-    a0 = fma(x[e], y[e], a0);
-    a1 = fma(x[e + 32], y[e + 32], a1);
-    a2 = fma(x[e + 64], y[e + 64], a2);
-    a3 = fma(x[e + 96], y[e + 96], a3);
-  }
-  for (; e < len; e += 32) a0 = fma(x[e], y[e], a0);
-  return warp_sum((a0 + a1) + (a2 + a3));
-}
-
-template <bool EXACT>
-__device__ __forceinline__ double ql_dot(int len, const double* x, const double* y, int lane) {
-  if constexpr (EXACT) return cq_dot<true>(len, x, y, lane);
-  else return ql_dot_fma(len, x, y, lane);
-}
-
-// reflection_axis_mut on x[0 .. len) by one warp: x becomes the unit axis
-// (where the column is not zero) and *d_out the signed diagonal entry.
-template <bool EXACT>
-__device__ void ql_make_axis(int len, double* x, double* d_out, int lane) {
+// reflection_axis_mut on x[0 .. len) by one warp, EXACT form (every rounding
+// as Rust's, dots in dotx's order): x becomes the unit axis (where the column
+// is not zero) and *d_out the signed diagonal entry.
+__device__ void ql_make_axis_exact(int len, double* x, double* d_out, int lane) {
   const double x0 = x[0];
-  const double sq = cq_add<EXACT>(0.0, ql_dot<EXACT>(len, x, x, lane));  // norm_squared (norm.rs:238-250)
+  const double sq = __dadd_rn(0.0, cq_dot<true>(len, x, x, lane));  // norm_squared (norm.rs:238-250)
   const double nrm = __dsqrt_rn(sq);
   double modulus, sign;
   cq_to_exp(x0, modulus, sign);
-  const double signed_norm = cq_mul<EXACT>(sign, nrm);
-  const double factor = EXACT ? __dmul_rn(__dadd_rn(sq, __dmul_rn(modulus, nrm)), 2.0) : fma(modulus, nrm, sq) * 2.0;
-  const double x0n = cq_add<EXACT>(x0, signed_norm);
+  const double signed_norm = __dmul_rn(sign, nrm);
+  const double factor = __dmul_rn(__dadd_rn(sq, __dmul_rn(modulus, nrm)), 2.0);
+  const double x0n = __dadd_rn(x0, signed_norm);
   __syncwarp();  // every lane has read x before it changes
   const bool nz = !is_zero_bits(factor);
   if (nz) {
-    if constexpr (EXACT) {
-      const double sf = __dsqrt_rn(factor);
-      for (int r = lane; r < len; r += 32) x[r] = __ddiv_rn(r == 0 ? x0n : x[r], sf);  // unscale_mut
-      __syncwarp();
-      const double n2 = __dsqrt_rn(__dadd_rn(0.0, cq_dot<true>(len, x, x, lane)));  // normalize_mut
-      __syncwarp();
-      for (int r = lane; r < len; r += 32) x[r] = __ddiv_rn(x[r], n2);
-    } else {
-      // factor = 2 (sq + |x0| nrm) is the squared norm of the updated axis, so
-      // one scale by rsqrt(factor) leaves a unit vector; nalgebra's second
-      // normalisation only corrects rounding
-      const double rs = rsqrt(factor);
-      for (int r = lane; r < len; r += 32) x[r] = (r == 0 ? x0n : x[r]) * rs;
-    }
+    const double sf = __dsqrt_rn(factor);
+    for (int r = lane; r < len; r += 32) x[r] = __ddiv_rn(r == 0 ? x0n : x[r], sf);  // unscale_mut
+    __syncwarp();
+    const double n2 = __dsqrt_rn(__dadd_rn(0.0, cq_dot<true>(len, x, x, lane)));  // normalize_mut
+    __syncwarp();
+    for (int r = lane; r < len; r += 32) x[r] = __ddiv_rn(x[r], n2);
   } else if (lane == 0) {
     x[0] = x0n;  // x[0] += signed_norm happens whether or not the column was zero
   }
   if (lane == 0) *d_out = nz ? -signed_norm : signed_norm;
 }
 
-// Step i of the factorization: reflector i (i >= 0) on columns i+1 .. i+ncols,
-// and the axis of column i+1 when i+1 < min(m, n).
-template <bool EXACT>
+// Step i of the EXACT factorization: reflector i (i >= 0) on columns
+// i+1 .. i+ncols, one warp per column, and the axis of column i+1 when
+// i+1 < min(m, n).
 __global__ void __launch_bounds__(kQlThreads)
-    qr_large_step_kernel(int m, int n, double* __restrict__ A, int64_t lda, double* __restrict__ diag, int i,
-                         int ncols) {
+    qr_large_step_exact_kernel(int m, int n, double* __restrict__ A, int64_t lda, double* __restrict__ diag, int i,
+                               int ncols) {
   const int lane = threadIdx.x & 31;
   const int warp = blockIdx.x * kQlWarps + (threadIdx.x >> 5);
   const int nwarps = gridDim.x * kQlWarps;
@@ -112,7 +89,7 @@ __global__ void __launch_bounds__(kQlThreads)
     const double d = diag[i];
     reflect = !is_zero_bits(d);  // diag[i] == 0 exactly where reflection_axis_mut found a zero column
     sign = cq_signum(d);
-    m_two = cq_mul<EXACT>(sign, -2.0);
+    m_two = __dmul_rn(sign, -2.0);
     axis = A + (int64_t)i * lda + i;
     len = m - i;
   }
@@ -121,17 +98,127 @@ __global__ void __launch_bounds__(kQlThreads)
     double* col = A + (int64_t)j * lda;
     if (reflect) {
       double* y = col + i;
-      const double dot = ql_dot<EXACT>(len, axis, y, lane);
-      const double factor = cq_mul<EXACT>(dot, m_two);  // (dot - bias) * (sign * -2), bias 0
+      const double factor = __dmul_rn(cq_dot<true>(len, axis, y, lane), m_two);  // (dot - bias) * (sign * -2)
       __syncwarp();
-      for (int r = lane; r < len; r += 32) {
-        const double sy = cq_mul<EXACT>(sign, y[r]);
-        y[r] = EXACT ? __dadd_rn(__dmul_rn(factor, axis[r]), sy) : fma(factor, axis[r], sy);
-      }
+      for (int r = lane; r < len; r += 32) y[r] = __dadd_rn(__dmul_rn(factor, axis[r]), __dmul_rn(sign, y[r]));
     }
     if (j == i + 1 && j < mn) {
       __syncwarp();
-      ql_make_axis<EXACT>(m - j, col + j, diag + j, lane);
+      ql_make_axis_exact(m - j, col + j, diag + j, lane);
+    }
+  }
+}
+
+// Block-wide sum for the FMA form, valid in every thread.  red holds two
+// rounds of per-warp partials; consecutive calls alternate them, so one
+// barrier per call suffices (a round is rewritten only two calls later, after
+// every thread has passed the barrier in between).
+__device__ __forceinline__ double qc_block_sum(double v, double (*red)[kQcWarps], int& phase) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double* rb = red[phase];
+  phase ^= 1;
+  if (lane == 0) rb[w] = v;
+  __syncthreads();
+  double s = lane < kQcWarps ? rb[lane] : 0.0;
+#pragma unroll
+  for (int off = kQcWarps / 2; off >= 1; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  return __shfl_sync(0xffffffffu, s, 0);
+}
+
+// sum_r x[r] y[r] over this thread's rows t, t + kQcThreads, ... < len: two
+// accumulators, four loads in flight.  FP64 instructions are the scarce
+// resource here (each warp-wide one holds an SM sub-partition's FP64 unit for
+// 64 cycles), so the per-column reduction is kept short: 128 threads per
+// column, one combine, warp_sum, a two-level block sum.
+__device__ __forceinline__ double qc_dot_part(int len, const double* __restrict__ x, const double* __restrict__ y) {
+  double a0 = 0.0, a1 = 0.0;
+  int r = threadIdx.x;
+  for (; r + 3 * kQcThreads < len; r += 4 * kQcThreads) {
+    const double x0 = x[r], x1 = x[r + kQcThreads], x2 = x[r + 2 * kQcThreads], x3 = x[r + 3 * kQcThreads];
+    const double y0 = y[r], y1 = y[r + kQcThreads], y2 = y[r + 2 * kQcThreads], y3 = y[r + 3 * kQcThreads];
+    a0 = fma(x0, y0, a0);
+    a1 = fma(x1, y1, a1);
+    a0 = fma(x2, y2, a0);
+    a1 = fma(x3, y3, a1);
+  }
+  for (; r < len; r += kQcThreads) a0 = fma(x[r], y[r], a0);
+  return a0 + a1;
+}
+
+// y <- factor * v + s * y on this thread's rows, s = +-1 folded into the FMA's
+// operand sign (no FP64 multiply); s NaN only comes with a NaN factor.
+template <bool NEG>
+__device__ __forceinline__ void qc_axpy(int len, double factor, const double* __restrict__ v, double* __restrict__ y) {
+  int r = threadIdx.x;
+  for (; r + 3 * kQcThreads < len; r += 4 * kQcThreads) {
+    const double y0 = y[r], y1 = y[r + kQcThreads], y2 = y[r + 2 * kQcThreads], y3 = y[r + 3 * kQcThreads];
+    const double v0 = v[r], v1 = v[r + kQcThreads], v2 = v[r + 2 * kQcThreads], v3 = v[r + 3 * kQcThreads];
+    y[r] = fma(factor, v0, NEG ? -y0 : y0);
+    y[r + kQcThreads] = fma(factor, v1, NEG ? -y1 : y1);
+    y[r + 2 * kQcThreads] = fma(factor, v2, NEG ? -y2 : y2);
+    y[r + 3 * kQcThreads] = fma(factor, v3, NEG ? -y3 : y3);
+  }
+  for (; r < len; r += kQcThreads) y[r] = fma(factor, v[r], NEG ? -y[r] : y[r]);
+}
+
+// reflection_axis_mut on x[0 .. len) by one CTA, FMA form (one scale by
+// rsqrt(factor): factor = 2 (sq + |x0| nrm) is the squared norm of the
+// updated axis, so nalgebra's second normalisation only corrects rounding).
+__device__ void qc_make_axis(int len, double* x, double* d_out, double (*red)[kQcWarps], int& phase) {
+  const int t = threadIdx.x;
+  const double x0 = x[0];
+  const double sq = qc_block_sum(qc_dot_part(len, x, x), red, phase);  // its barrier: every read of x is done
+  const double nrm = __dsqrt_rn(sq);
+  double modulus, sign;
+  cq_to_exp(x0, modulus, sign);
+  const double signed_norm = sign * nrm;
+  const double factor = fma(modulus, nrm, sq) * 2.0;
+  const double x0n = x0 + signed_norm;
+  const bool nz = !is_zero_bits(factor);
+  if (nz) {
+    const double rs = rsqrt(factor);
+    for (int r = t; r < len; r += kQcThreads) x[r] = (r == 0 ? x0n : x[r]) * rs;
+  } else if (t == 0) {
+    x[0] = x0n;
+  }
+  if (t == 0) *d_out = nz ? -signed_norm : signed_norm;
+}
+
+// Step i of the FMA factorization: reflector i (i >= 0) on columns
+// i+1 .. i+ncols, one CTA per column, and the axis of column i+1 when
+// i+1 < min(m, n).  Every branch is uniform over the CTA.
+__global__ void __launch_bounds__(kQcThreads)
+    qr_large_step_cta_kernel(int m, int n, double* __restrict__ A, int64_t lda, double* __restrict__ diag, int i,
+                             int ncols) {
+  __shared__ double red[2][kQcWarps];
+  int phase = 0;
+  const int mn = min(m, n);
+  bool reflect = false;
+  double sign = 0.0, m_two = 0.0;
+  const double* axis = nullptr;
+  int len = 0;
+  if (i >= 0) {
+    const double d = diag[i];
+    reflect = !is_zero_bits(d);
+    sign = cq_signum(d);
+    m_two = sign * -2.0;
+    axis = A + (int64_t)i * lda + i;
+    len = m - i;
+  }
+  for (int c = blockIdx.x; c < ncols; c += gridDim.x) {
+    const int j = i + 1 + c;
+    double* col = A + (int64_t)j * lda;
+    if (reflect) {
+      double* y = col + i;
+      const double factor = qc_block_sum(qc_dot_part(len, axis, y), red, phase) * m_two;
+      // each thread updates the rows it read: no barrier between the dot and the axpy
+      if (sign < 0.0) qc_axpy<true>(len, factor, axis, y);
+      else qc_axpy<false>(len, factor, axis, y);
+    }
+    if (j == i + 1 && j < mn) {
+      __syncthreads();  // the axis reads rows other threads just wrote
+      qc_make_axis(m - j, col + j, diag + j, red, phase);
     }
   }
 }
@@ -171,15 +258,23 @@ __global__ void __launch_bounds__(kQtThreads)
     phase ^= 1;
     if (lane == 0) rb[w] = part;
     __syncthreads();
-    double dot = 0.0;
+    // the warps' partials summed by a shuffle tree in every warp (four FP64
+    // adds per warp instead of sixteen per thread)
+    double s = lane < kQtThreads / 32 ? rb[lane] : 0.0;
 #pragma unroll
-    for (int q = 0; q < kQtThreads / 32; ++q) dot += rb[q];
-    const double factor = dot * (sign * -2.0);
+    for (int off = kQtThreads / 64; off >= 1; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    const double factor = __shfl_sync(0xffffffffu, s, 0) * (sign * -2.0);
+    // sign * v as a flip of the sign bit on the integer pipe (sign = +-1; a NaN
+    // sign comes with a NaN factor)
+    const unsigned flip = sign < 0.0 ? 0x80000000u : 0u;
 #pragma unroll
     for (int k = 0; k < kQtRows; ++k) {
       if (k < kmax && wlast + k * kQtThreads >= i) {
         const int r = t + k * kQtThreads;
-        if (r >= i && r < m) v[k] = fma(factor, axis[r], sign * v[k]);
+        if (r >= i && r < m) {
+          const double sv = __hiloint2double(__double2hiint(v[k]) ^ (int)flip, __double2loint(v[k]));
+          v[k] = fma(factor, axis[r], sv);
+        }
       }
     }
   }
@@ -202,15 +297,18 @@ __global__ void qr_large_r_kernel(int n, const double* __restrict__ QR, int64_t 
 
 inline size_t ql_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
-template <bool EXACT>
-int qr_large_factor(int m, int n, double* A, int64_t lda, double* diag, cudaStream_t s) {
+int qr_large_factor(bool exact, int m, int n, double* A, int64_t lda, double* diag, cudaStream_t s) {
   const int mn = std::min(m, n);
   const int max_blocks = sm_count() * (2048 / kQlThreads);
   for (int i = -1; i < mn; ++i) {
     const int ncols = i < 0 ? 1 : n - 1 - i;  // step -1 only forms the first axis
     if (ncols <= 0) break;
-    const int blocks = std::min((ncols + kQlWarps - 1) / kQlWarps, max_blocks);
-    qr_large_step_kernel<EXACT><<<blocks, kQlThreads, 0, s>>>(m, n, A, lda, diag, i, ncols);
+    if (exact) {
+      const int blocks = std::min((ncols + kQlWarps - 1) / kQlWarps, max_blocks);
+      qr_large_step_exact_kernel<<<blocks, kQlThreads, 0, s>>>(m, n, A, lda, diag, i, ncols);
+    } else {
+      qr_large_step_cta_kernel<<<std::min(ncols, max_blocks), kQcThreads, 0, s>>>(m, n, A, lda, diag, i, ncols);
+    }
   }
   return check_launch("nacu_dqr");
 }
@@ -229,8 +327,7 @@ int nacu_dqr(int m, int n, double* A, int64_t lda, double* diag, int flags, nacu
   if (lda < m) return record_arg_error(-4, "dqr: lda < m");
   if (!diag) return record_arg_error(-5, "dqr: null diag");
   const cudaStream_t s = (cudaStream_t)stream;
-  return (flags & NACU_FLAG_EXACT) ? qr_large_factor<true>(m, n, A, lda, diag, s)
-                                   : qr_large_factor<false>(m, n, A, lda, diag, s);
+  return qr_large_factor((flags & NACU_FLAG_EXACT) != 0, m, n, A, lda, diag, s);
 }
 
 size_t nacu_qr_solve_workspace_bytes(int n) {
