@@ -1248,6 +1248,18 @@ def bench_qr_large_ours(args, rank, world):
     rng = np.random.default_rng(rank)
     info = torch.zeros(1, dtype=torch.int32, device="cuda")
     forms, cpu = {}, {}
+    if args.profile:  # one untimed factor + solve of the 4096 case, for profiler captures
+        n = 4096
+        a = rng.random((n, n)) + n * np.eye(n)
+        A = torch.from_numpy(np.asfortranarray(a).ravel(order="F")).cuda()
+        B = torch.from_numpy(rng.random(n)).cuda()
+        diag = torch.zeros(n, dtype=torch.float64, device="cuda")
+        ws = torch.empty(L.nacu_qr_solve_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+        _lib.call("nacu_dqr", n, n, A.data_ptr(), n, diag.data_ptr(), 0, sp)
+        _lib.call("nacu_dqr_solve", n, n, 1, A.data_ptr(), n, diag.data_ptr(), B.data_ptr(), n, info.data_ptr(),
+                  ws.data_ptr(), ws.numel(), 0, sp)
+        torch.cuda.synchronize()
+        return {"workload": "qr_large", "profile": True, "n": n, "info": int(info.item())}
     for (m, n, solve) in ((4096, 4096, True), (1000, 1000, True), (100, 500, False)):
         a = rng.random((m, n)) + (n * np.eye(m, n) if m == n else 0.0)
         b = rng.random(m)
