@@ -233,24 +233,29 @@ impl DeviceMatrix {
         Some(DeviceCholesky { l: self, logdet: logdet.to_vec()[0] })
     }
 
-    /// `Matrix::qr` (src/linalg/decomposition.rs:56-62).  Square n <= 128:
-    /// `QR::new` in place (the batched kernel), for `solve` / `try_inverse`.
-    /// Tall m x n with m > n, n <= 128: kept for `solve_least_squares`.
+    /// `Matrix::qr` (src/linalg/decomposition.rs:56-62): `QR::new` in place.
+    /// Square n <= 128: the shared-memory batched kernel; any other shape
+    /// (larger, tall or wide): one launch per Householder step (`nacu_dqr`).
     pub fn qr(mut self) -> DeviceQR {
-        let n = self.ncols;
-        if self.nrows == n {
-            assert!(n <= 128, "nalgebra-cuda: square QR of n <= 128");
-            let mut diag = DeviceBuffer::<f64>::zeroed(n.max(1));
+        let (m, n) = (self.nrows, self.ncols);
+        let k = m.min(n);
+        let mut diag = DeviceBuffer::<f64>::zeroed(k.max(1));
+        if m == n && n <= 128 {
             let mut info = DeviceBuffer::<i32>::zeroed(1);
             check(unsafe {
                 ffi::nacu_dqr_batched(n as c_int, 0, self.data.as_mut_ptr(), (n * n) as i64, diag.as_mut_ptr(),
                                       std::ptr::null_mut(), 0, info.as_mut_ptr(), 1, 0, std::ptr::null_mut())
             });
             let invertible = info.to_vec()[0] == 0;
-            return DeviceQR { a: self, diag: Some(diag), invertible };
+            return DeviceQR { a: self, diag, invertible, large: false };
         }
-        assert!(self.nrows > n && n <= 128, "nalgebra-cuda: QR of m x n, m >= n, n <= 128");
-        DeviceQR { a: self, diag: None, invertible: false }
+        check(unsafe {
+            ffi::nacu_dqr(m as c_int, n as c_int, self.data.as_mut_ptr(), m.max(1) as i64, diag.as_mut_ptr(), 0,
+                          std::ptr::null_mut())
+        });
+        // qr.rs:281-292: square, and no diag entry zero
+        let invertible = m == n && diag.to_vec()[..k].iter().all(|d| *d != 0.0);
+        DeviceQR { a: self, diag, invertible, large: true }
     }
 
     /// `Matrix::gemm` (src/base/blas.rs:729-746): self = alpha a b + beta self.
@@ -416,27 +421,39 @@ impl DeviceCholesky {
     }
 }
 
-/// Householder QR.  Square (n <= 128): nalgebra's `QR` (src/linalg/qr.rs),
-/// factored in place.  Tall (m > n, n <= 128): the least-squares solve of
-/// nalgebra-lapack's `QrDecomposition::solve` (src/qr/abstraction.rs:46-77).
+/// Householder QR (src/linalg/qr.rs:34-40): the axes and R in the matrix
+/// buffer, the signed diagonal on the device.  `solve` / `try_inverse` for a
+/// square factor; `solve_least_squares` for a tall one, as nalgebra-lapack's
+/// `QrDecomposition::solve` (src/qr/abstraction.rs:46-77).
 pub struct DeviceQR {
     a: DeviceMatrix,
-    diag: Option<DeviceBuffer<f64>>,
+    diag: DeviceBuffer<f64>,
     invertible: bool,
+    large: bool,
 }
 
 impl DeviceQR {
+    /// b <- Q^T b, then its top n rows <- R^-1 (Q^T b)[0:n]; false at a zero |diag_i|.
     fn solve_cols(&self, b: &mut DeviceMatrix) -> bool {
-        let n = self.a.nrows;
-        let diag = self.diag.as_ref().expect("QR solve: unable to solve a non-square system.");
+        let (m, n) = (self.a.nrows, self.a.ncols);
         let mut info = DeviceBuffer::<i32>::zeroed(1);
+        if self.large {
+            let bytes = unsafe { ffi::nacu_qr_solve_workspace_bytes(n as c_int) };
+            let mut ws = DeviceBuffer::<u8>::zeroed(bytes.max(1));
+            check(unsafe {
+                ffi::nacu_dqr_solve(m as c_int, n as c_int, b.ncols as c_int, self.a.data.as_ptr(), m.max(1) as i64,
+                                    self.diag.as_ptr(), b.data.as_mut_ptr(), m.max(1) as i64, info.as_mut_ptr(),
+                                    ws.as_mut_ptr() as *mut c_void, bytes, 0, std::ptr::null_mut())
+            });
+            return info.to_vec()[0] == 0;
+        }
         let mut ok = true;
         let mut c0 = 0;
         while c0 < b.ncols {
             let k = (b.ncols - c0).min(16);
             check(unsafe {
                 ffi::nacu_dqr_solve_batched(n as c_int, k as c_int, self.a.data.as_ptr(), (n * n) as i64,
-                                            diag.as_ptr(), b.data.as_mut_ptr().add(c0 * n), (n * k) as i64,
+                                            self.diag.as_ptr(), b.data.as_mut_ptr().add(c0 * n), (n * k) as i64,
                                             info.as_mut_ptr(), 1, 0, std::ptr::null_mut())
             });
             ok &= info.to_vec()[0] == 0;
@@ -448,6 +465,7 @@ impl DeviceQR {
     /// `QR::solve_mut` (qr.rs:204-222): b is overwritten even when it
     /// returns false.
     pub fn solve_mut(&self, b: &mut DeviceMatrix) -> bool {
+        assert!(self.a.is_square(), "The QR decomposition must be square.");
         assert!(b.nrows == self.a.nrows, "QR solve matrix dimension mismatch.");
         self.solve_cols(b)
     }
@@ -460,6 +478,7 @@ impl DeviceQR {
 
     /// `QR::try_inverse` (qr.rs:262-279).
     pub fn try_inverse(&self) -> Option<DeviceMatrix> {
+        assert!(self.a.is_square(), "The QR decomposition must be square.");
         let n = self.a.nrows;
         let mut res = DeviceMatrix::from_dmatrix(&DMatrix::<f64>::identity(n, n));
         if self.solve_cols(&mut res) { Some(res) } else { None }
@@ -470,30 +489,20 @@ impl DeviceQR {
         self.invertible
     }
 
-    /// argmin ||A x - b|| for a tall factorization: `Err` naming the first
-    /// zero R_kk when A is rank deficient.
-    pub fn solve_least_squares(mut self, b: &DeviceMatrix) -> Result<DeviceMatrix, usize> {
-        assert!(self.diag.is_none(), "solve_least_squares: a tall (m > n) QR");
-        let (m, n) = (self.a.nrows as c_int, self.a.ncols as c_int);
-        assert!(b.nrows == self.a.nrows && b.ncols == 1, "QR solve: one right-hand side of m rows");
-        let mut bb = b.clone_owned();
-        let mut x = DeviceMatrix::zeros(self.a.ncols, 1);
-        let mut diag = DeviceBuffer::<f64>::zeroed(self.a.ncols);
-        let mut info = DeviceBuffer::<i32>::zeroed(1);
-        let ms = DeviceBuffer::from_slice(&[m]);
-        let off = DeviceBuffer::from_slice(&[0i64]);
-        let bytes = unsafe { ffi::nacu_qr_workspace_bytes(1) };
-        let mut ws = DeviceBuffer::<u8>::zeroed(bytes);
-        check(unsafe {
-            ffi::nacu_dgels_batched(1, n, m, ms.as_ptr(), off.as_ptr(), self.a.data.as_mut_ptr(), off.as_ptr(),
-                                    bb.data.as_mut_ptr(), x.data.as_mut_ptr(), diag.as_mut_ptr(), info.as_mut_ptr(),
-                                    std::ptr::null(), ws.as_mut_ptr() as *mut c_void, bytes, 0,
-                                    std::ptr::null_mut())
-        });
-        match info.to_vec()[0] {
-            0 => Ok(x),
-            k => Err(k as usize),
+    /// argmin ||A x - b|| for a tall factor (m >= n, m <= 16384): the n x nrhs
+    /// solution, or `Err` naming the zero |diag_k| (1-based) when A is rank
+    /// deficient.
+    pub fn solve_least_squares(&self, b: &DeviceMatrix) -> Result<DeviceMatrix, usize> {
+        let (m, n) = (self.a.nrows, self.a.ncols);
+        assert!(m >= n && b.nrows == m, "QR least squares: m >= n and an m-row right-hand side");
+        let mut res = b.clone_owned();
+        if !self.solve_cols(&mut res) {
+            let d = self.diag.to_vec();
+            let k = (0..n).rev().find(|&i| d[i] == 0.0).unwrap_or(0);
+            return Err(k + 1);
         }
+        let top = res.to_dmatrix().rows(0, n).into_owned();
+        Ok(DeviceMatrix::from_dmatrix(&top))
     }
 }
 
