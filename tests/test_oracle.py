@@ -747,3 +747,55 @@ def test_qr_solve_zero_diagonal_returns_false():
     qr, diag = O.qr(np.zeros((3, 3)))
     _, ok = O.qr_solve(qr, diag, np.array([1.0, 2.0, 3.0]))
     assert not ok
+
+
+def _pure_python_qr(a):
+    """Independent pure-Python restatement of QR::new (src/linalg/qr.rs:55-76:
+    clear_column_unchecked per column, householder.rs:19-85, reflection.rs:70-83)
+    for small m x n matrices of any shape; columns as lists."""
+    import math
+
+    m, n = len(a), len(a[0])
+    cols = [[float(a[r][c]) for r in range(m)] for c in range(n)]
+    diag = [0.0] * min(m, n)
+    for i in range(min(m, n)):
+        x = cols[i][i:]
+        sq = 0.0 + _py_dotx(x, x)
+        nrm = math.sqrt(sq)
+        modulus, sign = (x[0], 1.0) if x[0] >= 0 else (-x[0], -1.0)
+        signed_norm = sign * nrm
+        factor = (sq + modulus * nrm) * 2.0
+        x[0] += signed_norm
+        if factor != 0.0:
+            sf = math.sqrt(factor)
+            x = [v / sf for v in x]
+            n2 = math.sqrt(0.0 + _py_dotx(x, x))
+            x = [v / n2 for v in x]
+            rnorm = -signed_norm
+            sgn = math.copysign(1.0, rnorm)
+            for c in range(i + 1, n):
+                y = cols[c][i:]
+                f = (_py_dotx(x, y) - 0.0) * (sgn * -2.0)
+                cols[c][i:] = [f * x[k] + sgn * y[k] for k in range(len(y))]
+        else:
+            rnorm = signed_norm
+        cols[i][i:] = x
+        diag[i] = rnorm
+    return np.array(cols).T, np.array(diag)
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (1, 6), (6, 1), (9, 9), (12, 5), (5, 12), (17, 11)])
+def test_qr_matches_pure_python_restatement_bitwise(m, n):
+    """The oracle's QR::new for tall, square and wide shapes (the one-matrix GPU
+    kernel's checker), with a zero column and a column whose squares underflow
+    (a zero norm over nonzero entries: no reflection, x[0] += 0)."""
+    rng = np.random.default_rng(800 + 13 * m + n)
+    a = rng.uniform(-100, 100, size=(m, n))
+    if min(m, n) >= 5:
+        a[:, 2] = 0.0
+        a[:, 4] = 1e-170
+    qr, diag = O.qr(a)
+    qr2, diag2 = _pure_python_qr(a)
+    assert np.array_equal(diag, diag2) and np.array_equal(qr, qr2)
+    if min(m, n) >= 5:
+        assert diag[2] == 0.0 and diag[4] == 0.0
