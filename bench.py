@@ -1758,8 +1758,11 @@ def other_configs(args, rank, world) -> dict:
     run with its own CUDA-event timing and clocks, so that one default bench
     line carries all of them: batched LU (4096 x 64), mixed LU + refinement
     (n = 8192 at three condition numbers), the adjoint (2048 x 128, f64 and
-    f32), GEMM 8192^3 (split and FP64) and batched QR least squares (8192
-    problems).  Steps are capped for the large single-matrix workloads."""
+    f32), GEMM 8192^3 (split and FP64), batched QR least squares (8192
+    problems), and the next rows at the reference's bench shapes: batched Mul
+    (100 x 100), the 1000 x 1000 triangular solves, the batched 100 x 100 QR
+    solve and the QR of one 4096 x 4096 matrix.  Steps are capped for the
+    large single-matrix workloads."""
     import copy
 
     import torch
