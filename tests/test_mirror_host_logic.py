@@ -113,7 +113,7 @@ def test_qr_routes_by_shape(fake):
         args = fake.named("nacu_dqr")[-1]
         assert args[:2] == (m, n) and args[3] == m and args[2] == q.qr.data.data_ptr() and q.large
         assert q.diag.numel() == min(m, n)
-    # the large square solve: one call for every column, ldb = m, the real workspace size
+    # a tall factor's least-squares solve: one call for all columns, ldb = m, the real workspace size
     b = ng.DeviceMatrix.from_numpy(np.ones((500, 3)))
     t = ng.DeviceMatrix.from_numpy(np.ones((500, 100))).qr()
     t.solve_least_squares(ng.DeviceMatrix.from_numpy(np.ones((500, 1))))
