@@ -114,3 +114,44 @@ def test_rust_crate_binds_every_entry_point_with_its_arity():
     assert set(decl) == set(bound), (set(decl) ^ set(bound))
     wrong = {k: (decl[k], bound[k]) for k in decl if decl[k] != bound[k]}
     assert not wrong, wrong
+
+
+# Entry points whose first argument is an order or a count: a negative value
+# is rejected with -1 (LAPACK's xerbla convention) before any device work, so
+# these run without a GPU.
+_FIRST_ARG_IS_SIZE = [
+    "nacu_dgetrf_batched", "nacu_dgetrs_batched", "nacu_dgesv_batched", "nacu_sgesv_batched", "nacu_dgetri_batched",
+    "nacu_dposv_ragged", "nacu_dpotrf_ragged", "nacu_dpotrs_ragged", "nacu_dposv", "nacu_dposv_ragged_noalloc",
+    "nacu_dposv_ragged_mixed", "nacu_dposv_ragged_mixed_host", "nacu_dposv_logdet_forward",
+    "nacu_sposv_logdet_forward", "nacu_dposv_logdet_backward", "nacu_sposv_logdet_backward",
+    "nacu_dchol_rank1_update_batched", "nacu_dchol_remove_column_batched", "nacu_dchol_insert_column_batched",
+    "nacu_dfullpivlu_batched", "nacu_dfullpivlu_solve_batched", "nacu_dcolpivqr_batched",
+    "nacu_dcolpivqr_solve_batched", "nacu_dqr_batched", "nacu_dqr_solve_batched", "nacu_dqr", "nacu_dqr_solve",
+    "nacu_dgels_batched", "nacu_dtrsv_batched", "nacu_dtrsv", "nacu_dgetrf", "nacu_dgetrs", "nacu_dgesv_mixed_ir",
+    "nacu_dgemm", "nacu_dgemm_batched", "nacu_dgemm_split_bf16", "nacu_test_rcp", "nacu_test_dgetrs_flag_timeout",
+]
+
+
+@pytest.mark.parametrize("name", _FIRST_ARG_IS_SIZE)
+def test_negative_size_is_argument_one(L, name):
+    restype, argtypes = _lib.SIGNATURES[name]
+    args = []
+    for t in argtypes:
+        if t in (C.c_int, C.c_int64, C.c_size_t):
+            args.append(0)
+        elif t is C.c_double:
+            args.append(0.0)
+        else:
+            args.append(None)  # pointers and streams
+    args[0] = -1
+    assert getattr(L, name)(*args) == -1, name
+    assert b"argument 1" in L.nacu_last_error(), name
+
+
+def test_plumbing_null_outputs_are_rejected(L):
+    assert L.nacu_device_count(None) == -1
+    assert L.nacu_host_alloc(None, 8) == -1
+    assert L.nacu_stream_create(None) == -1
+    assert L.nacu_graph_end_capture(None, None) == -1
+    assert L.nacu_probe_fp64_peak(None) == -1
+    assert L.nacu_ragged_get_tuning(None, 0) == -1 and L.nacu_ragged_set_tuning(None, 0) == -1
