@@ -15,12 +15,14 @@
 // next launch finds it ready: min(m, n) + 1 launches.  Each reads and writes
 // the trailing matrix once (the axpy's second read comes from L1/L2), 16-24
 // bytes per two FP64 FMAs, near the balance point of GB300's FP64 pipe against
-// HBM.  The FMA form gives each column a CTA of 256 threads (a thread owns
-// rows t, t + 256, ...; one barrier per block-wide dot): a warp per column
-// left most of the SM idle and every row chain waiting on its loads.  EXACT
-// rounds every operation as Rust does, the dots in dotx's order (eight
-// sequential accumulators), so it keeps one warp per column: bit-identical to
-// nalgebra's factors.
+// HBM.  The FMA form gives each column a CTA of 128 threads (a thread owns
+// rows t, t + 128, ...; one barrier per block-wide dot) and issues two FP64
+// instructions per element: the dot's FMA and the axpy's, the +-1 sign folded
+// into the FMA's operand (a multiply by it was a third).  Each warp-wide FP64
+// instruction holds an SM sub-partition's FP64 unit for about 64 cycles, so
+// the per-column reductions are kept short.  EXACT rounds every operation as
+// Rust does, the dots in dotx's order (eight sequential accumulators), so it
+// keeps one warp per column: bit-identical to nalgebra's factors.
 //
 // Solve: Q^T B by one CTA per right-hand side, each thread owning fixed rows
 // of its column in registers across all steps (so B needs no barrier; the dot
